@@ -1,0 +1,192 @@
+"""Case plug-ins: level set phi and initial conserved state for named problems.
+
+The reference defines each problem with three per-case hooks compiled into
+its driver (Src/Geometry/Level_Set_function.H:13-19, Src/Base/Common/
+Initialize.H:12-23 and the Global_Boundary of Src/BoundaryCondition/
+Boundary.H:22-29).  Here a case is plain data: `phi` (M*N doubles, index
+j*M+i) and `u0` (M*N*4 doubles, index (j*M+i)*4+k, k = rho, rho u, rho v, E),
+which both the GPU path and the CPU oracle consume unchanged.
+
+Cell-centre coordinates follow Src/Geometry/Psy_coord.cpp:29-44: x_i =
+Li + i*dx, y_j = Hi + j*dx with dx = (hi_x - lo_x)/N_x used in both
+directions (the reference assumes square cells).
+
+Cases that depend on the cell type (solid cells get rho = -1, E = -1, as in
+Test/InclineSod/Initialize.cpp:43-67) take the type array returned by the
+geometry set-up, in the same order as the reference calls Level_Set before
+Initialize.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+@dataclass
+class Grid:
+    n_x: int
+    n_y: int
+    ng: int = 2
+    lo_x: float = 0.0
+    lo_y: float = 0.0
+    hi_x: float = 1.0
+    hi_y: float = 1.0
+
+    @property
+    def M(self):
+        return self.n_x + 2 * self.ng
+
+    @property
+    def N(self):
+        return self.n_y + 2 * self.ng
+
+    def coords(self):
+        """x, y arrays of shape (N, M), bit-identical to Psy_coord.cpp:29-44."""
+        dx = (self.hi_x - self.lo_x) / self.n_x
+        Li = -dx * self.ng + self.lo_x + dx / 2
+        Hi = -dx * self.ng + self.lo_y + dx / 2
+        i = np.arange(self.M, dtype=np.float64)
+        j = np.arange(self.N, dtype=np.float64)
+        x = Li + i * dx
+        y = Hi + j * dx
+        return np.broadcast_to(x[None, :], (self.N, self.M)), np.broadcast_to(y[:, None], (self.N, self.M))
+
+
+def conserved(rho, u, v, p, gamma):
+    """(rho, rho u, rho v, E) with E = p/(gamma-1) + 0.5 rho (u^2+v^2) (Test/Sod/Initialize.cpp:45-48)."""
+    rho = np.asarray(rho, dtype=np.float64)
+    out = np.empty(rho.shape + (4,))
+    out[..., 0] = rho
+    out[..., 1] = rho * u
+    out[..., 2] = rho * v
+    out[..., 3] = p / (gamma - 1) + 0.5 * rho * (u * u + v * v)
+    return out
+
+
+def _solid_fill(u, types):
+    """solid cells (type 1) hold rho = -1, E = -1 (Test/InclineSod/Initialize.cpp:61-67)."""
+    if types is None:
+        return u
+    solid = ~((types < 0.5) | (types > 1.5))
+    u[solid] = (-1.0, 0.0, 0.0, -1.0)
+    return u
+
+
+# ------------------------------------------------------------------ problems
+
+
+def sod_x(g: Grid, gamma=1.4, x0=0.5, left=(1.0, 0.0, 0.0, 1.0), right=(0.125, 0.0, 0.0, 0.1), types=None):
+    """Sod shock tube split on x < x0, no immersed body (phi = 1)."""
+    x, _ = g.coords()
+    phi = np.ones((g.N, g.M))
+    L = conserved(*left, gamma)
+    R = conserved(*right, gamma)
+    u = np.where((x < x0)[..., None], L, R)
+    return phi.reshape(-1), _solid_fill(np.ascontiguousarray(u), types).reshape(-1)
+
+
+def quadrants(g: Grid, gamma=1.4, xc=0.5, yc=0.5, states=None, types=None, downward=False):
+    """Four-state 2D Riemann problem; states = upper-right, upper-left,
+    lower-left, lower-right as (rho, u, v, p).  The default states move
+    vertically faster than sound in three quadrants and slower in one, with
+    small velocity jumps (no vacuum-forming expansions); `downward` reverses
+    every vertical velocity."""
+    if states is None:
+        states = ((1.0, 0.1, 1.5, 1.0), (0.6, -0.1, 1.3, 0.7), (0.9, 0.0, 1.4, 0.9), (1.1, 0.2, 0.9, 1.1))
+    if downward:
+        states = tuple((r, u, -v, p) for (r, u, v, p) in states)
+    x, y = g.coords()
+    phi = np.ones((g.N, g.M))
+    ur, ul, ll, lr = (conserved(*s, gamma) for s in states)
+    right = x >= xc
+    top = y >= yc
+    u = np.where((top & right)[..., None], ur, np.where((top & ~right)[..., None], ul,
+                 np.where((~top & ~right)[..., None], ll, lr)))
+    return phi.reshape(-1), _solid_fill(np.ascontiguousarray(u), types).reshape(-1)
+
+
+def channel_phi(g: Grid, angle_deg=30.0, width=0.25, center=None):
+    """Inclined channel: signed distance min(d_lower, d_upper) to two walls
+    parallel to an axis through `center` at `angle_deg` (fluid inside, phi > 0)."""
+    x, y = g.coords()
+    if center is None:
+        center = (0.5 * (g.lo_x + g.hi_x), 0.5 * (g.lo_y + g.hi_y))
+    th = math.radians(angle_deg)
+    s = (x - center[0]) * (-math.sin(th)) + (y - center[1]) * math.cos(th)
+    phi = np.minimum(s + 0.5 * width, 0.5 * width - s)
+    return np.ascontiguousarray(phi).reshape(-1)
+
+
+def channel_init(g: Grid, types, gamma=1.4, angle_deg=30.0, center=None, left=(1.0, 0.0, 0.0, 1.0),
+                 right=(0.125, 0.0, 0.0, 0.1)):
+    """Sod states split perpendicular to the channel axis at the channel midpoint."""
+    x, y = g.coords()
+    if center is None:
+        center = (0.5 * (g.lo_x + g.hi_x), 0.5 * (g.lo_y + g.hi_y))
+    th = math.radians(angle_deg)
+    a = (x - center[0]) * math.cos(th) + (y - center[1]) * math.sin(th)
+    u = np.where((a < 0)[..., None], conserved(*left, gamma), conserved(*right, gamma))
+    u = np.ascontiguousarray(u)
+    return _solid_fill(u, np.asarray(types).reshape(g.N, g.M)).reshape(-1)
+
+
+def isentropic_vortex(g: Grid, gamma=1.4, beta=5.0, xc=5.0, yc=5.0, u_inf=1.0, v_inf=1.0, t=0.0, periodic=True):
+    """Isentropic vortex of strength beta on a uniform (1, u_inf, v_inf, 1)
+    stream; at time t the exact solution is the initial field moved by
+    (u_inf t, v_inf t), wrapped periodically.  phi = 1 (no body)."""
+    x, y = g.coords()
+    Lx, Ly = g.hi_x - g.lo_x, g.hi_y - g.lo_y
+    cx, cy = xc + u_inf * t, yc + v_inf * t
+    dxv = x - cx
+    dyv = y - cy
+    if periodic:
+        dxv = (dxv + 0.5 * Lx) % Lx - 0.5 * Lx
+        dyv = (dyv + 0.5 * Ly) % Ly - 0.5 * Ly
+    r2 = dxv * dxv + dyv * dyv
+    f = np.exp(0.5 * (1.0 - r2))
+    du = -beta / (2 * math.pi) * dyv * f
+    dv = beta / (2 * math.pi) * dxv * f
+    T = 1.0 - (gamma - 1.0) * beta * beta / (8.0 * gamma * math.pi * math.pi) * np.exp(1.0 - r2)
+    rho = T ** (1.0 / (gamma - 1.0))
+    p = rho * T
+    u = conserved(rho, u_inf + du, v_inf + dv, p, gamma)
+    return np.ones(g.N * g.M), np.ascontiguousarray(u).reshape(-1)
+
+
+# reference C1/C2/C3 workloads --------------------------------------------------
+
+
+@dataclass
+class Workload:
+    name: str
+    grid: Grid
+    gamma: float
+    cfl: float
+    t_end: float
+    scheme: str
+    riemann: str
+    limiter: str
+    boundary: str
+    gbc: str = "walls"
+    extra: dict = field(default_factory=dict)
+
+
+def sod_tube(n_x=400, n_y=100):
+    """2D Sod tube, 400x100 on [0,1]x[0,0.25], CFL 0.5, t_end 0.2, no body."""
+    return Workload("sod_tube_400x100", Grid(n_x, n_y, 2, 0.0, 0.0, 1.0, 0.25), 1.4, 0.5, 0.2,
+                    "MUSCL", "HLL", "minmod", "Regular")
+
+
+def inclined_channel(n_x=2048, n_y=1024, boundary="IDWBaseGFM"):
+    """Inclined Sod channel, 2048x1024 on [0,2]x[0,1], width 0.25 at 30 deg,
+    ghost-fluid walls, MUSCL + HLLC, CFL 0.45, t_end 0.2."""
+    return Workload(f"inclined_channel_{n_x}x{n_y}", Grid(n_x, n_y, 2, 0.0, 0.0, 2.0, 1.0), 1.4, 0.45, 0.2,
+                    "MUSCL", "HLLC", "minmod", boundary, extra={"angle": 30.0, "width": 0.25})
+
+
+def vortex_periodic(n=4096):
+    """Isentropic vortex, periodic n x n on [0,10]^2, beta 5, MHM + HLLC, t 10."""
+    return Workload(f"isentropic_vortex_{n}", Grid(n, n, 2, 0.0, 0.0, 10.0, 10.0), 1.4, 0.5, 10.0,
+                    "MHM", "HLLC", "minmod", "Regular", gbc="periodic", extra={"beta": 5.0})

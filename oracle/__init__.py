@@ -1,0 +1,171 @@
+"""CPU oracle (test infrastructure only).
+
+Python access to the plain-C FP64 restatement of the reference solver in
+oracle/ibtfo_oracle.c, plus a reader for the reference-harness record format.
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this package; the product (ibtfo_gb300) never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import struct
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+
+SCHEMES = {"MUSCL": 0, "MHM": 1, "Godunov": 2}
+RIEMANNS = {"HLL": 0, "HLLC": 1, "PVRS": 2, "StegerWarming": 3}
+LIMITERS = {"minmod": 0, "VanLeer": 1}
+BOUNDARIES = {"Regular": 0, "IDWBaseGFM": 1, "LinearBaseGFM": 2, "RiemannBaseGFM": 3, "BCGFM": 4, "HBCGFM": 5}
+GLOBAL_BCS = {"walls": 0, "periodic": 1}
+
+
+def build(force: bool = False) -> str:
+    """Compile liboracle.so (gcc, -O2 -ffp-contract=off -fopenmp)."""
+    src = os.path.join(HERE, "ibtfo_oracle.c")
+    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= os.path.getmtime(src):
+        return LIB_PATH
+    cmd = ["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-std=c11",
+           src, "-o", LIB_PATH, "-lm"]
+    subprocess.run(cmd, check=True)
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        P = C.POINTER(C.c_double)
+        L.or_create.restype = C.c_void_p
+        L.or_create.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                                C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
+        L.or_destroy.argtypes = [C.c_void_p]
+        L.or_set_threads.argtypes = [C.c_int]
+        L.or_num_sch.argtypes = [C.c_void_p]
+        L.or_setup_geometry.argtypes = [C.c_void_p, P]
+        L.or_set_initial_state.argtypes = [C.c_void_p, P]
+        L.or_run.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_int, P, P]
+        L.or_run.restype = C.c_int
+        L.or_advance.argtypes = [C.c_void_p, C.c_double]
+        for f in ("or_boundary", "or_global_boundary"):
+            getattr(L, f).argtypes = [C.c_void_p]
+        for f in ("or_compute_dt", "or_mass"):
+            getattr(L, f).argtypes = [C.c_void_p]
+            getattr(L, f).restype = C.c_double
+        L.or_array_len.argtypes = [C.c_void_p, C.c_int]
+        L.or_array_len.restype = C.c_long
+        L.or_get.argtypes = [C.c_void_p, C.c_int, P]
+        L.or_put.argtypes = [C.c_void_p, C.c_int, P]
+        L.or_scalars.argtypes = [C.c_void_p, P]
+        L.or_iter.argtypes = [C.c_void_p]
+        L.or_iter.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class OracleCase:
+    """One case on the CPU oracle (FP64, reference array-of-structures layout)."""
+
+    def __init__(self, n_x, n_y, ng=2, lo=(0.0, 0.0), hi=(1.0, 1.0), gamma=1.4, cfl=0.5, scheme="MUSCL",
+                 riemann="HLL", limiter="minmod", boundary="Regular", gbc="walls"):
+        self.L = lib()
+        self.n_x, self.n_y, self.ng = n_x, n_y, ng
+        self.M, self.N = n_x + 2 * ng, n_y + 2 * ng
+        h = self.L.or_create(n_x, n_y, ng, lo[0], lo[1], hi[0], hi[1], gamma, cfl, SCHEMES[scheme],
+                             RIEMANNS[riemann], LIMITERS[limiter], BOUNDARIES[boundary], GLOBAL_BCS[gbc])
+        if not h:
+            raise ValueError("oracle rejected the configuration")
+        self.h = h
+        self.nsch = self.L.or_num_sch(h)
+
+    def close(self):
+        if self.h:
+            self.L.or_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def setup_geometry(self, phi):
+        phi = np.ascontiguousarray(phi, dtype=np.float64).reshape(-1)
+        assert phi.size == self.M * self.N
+        self.L.or_setup_geometry(self.h, _p(phi))
+
+    def set_initial_state(self, u0):
+        u0 = np.ascontiguousarray(u0, dtype=np.float64).reshape(-1)
+        assert u0.size == self.M * self.N * 4
+        self.L.or_set_initial_state(self.h, _p(u0))
+
+    def run(self, nsteps, t_end=1e300, max_iter=2 ** 31 - 1):
+        dts = np.zeros(max(nsteps, 1))
+        ms = np.zeros(max(nsteps, 1))
+        n = self.L.or_run(self.h, nsteps, t_end, max_iter, _p(dts), _p(ms))
+        return dts[:n], ms[:n]
+
+    def get(self, which):
+        idx = {"U_OLD": 0, "U_NEW": 1, "XYCOORD": 2, "SCHEME_IDX": 3, "U_TMP": 4}[which]
+        n = self.L.or_array_len(self.h, idx)
+        out = np.empty(n)
+        self.L.or_get(self.h, idx, _p(out))
+        return out
+
+    def put(self, which, arr):
+        idx = {"U_OLD": 0, "U_NEW": 1, "XYCOORD": 2, "SCHEME_IDX": 3, "U_TMP": 4}[which]
+        arr = np.ascontiguousarray(arr, dtype=np.float64).reshape(-1)
+        assert arr.size == self.L.or_array_len(self.h, idx)
+        self.L.or_put(self.h, idx, _p(arr))
+
+    def scalars(self):
+        out = np.zeros(4)
+        self.L.or_scalars(self.h, _p(out))
+        return {"dt": out[0], "now_t": out[1], "mass_start": out[2], "mass_now": out[3],
+                "iter": self.L.or_iter(self.h)}
+
+
+def set_threads(n: int):
+    lib().or_set_threads(int(n))
+
+
+def read_ref_record(path: str) -> dict:
+    """Reads one record written by oracle/harness/harness_main.cpp."""
+    with open(path, "rb") as f:
+        data = f.read()
+    assert data[:8] == b"IBTFOREF", "not a reference-harness record"
+    M, N, ng, nsch, iters, _ver = struct.unpack_from("<6i", data, 8)
+    off = 8 + 24
+    now_t, dt = struct.unpack_from("<2d", data, off)
+    off += 16
+    cells = M * N
+
+    def take(n):
+        nonlocal off
+        a = np.frombuffer(data, dtype="<f8", count=n, offset=off).copy()
+        off += 8 * n
+        return a
+
+    rec = {"M": M, "N": N, "ng": ng, "num_sch": nsch, "iters": iters, "now_t": now_t, "dt": dt}
+    rec["dts"] = take(iters + 1)
+    rec["masses"] = take(iters + 1)
+    rec["phi"] = take(cells)
+    rec["u_init"] = take(cells * 4)
+    rec["xycoord"] = take(cells * 6)
+    rec["scheme_idx"] = take(cells * nsch)
+    rec["u_old"] = take(cells * 4)
+    rec["u_new"] = take(cells * 4)
+    assert off == len(data)
+    return rec
