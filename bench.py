@@ -1,0 +1,311 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 IBTFO time step on the inclined-channel workload.
+
+Workload: inclined Sod channel with ghost-fluid walls, 2048x1024 cells on
+[0,2]x[0,1], channel width 0.25 at 30 degrees, IDWBaseGFM walls, MUSCL +
+HLLC + minmod, CFL 0.45, FP64 -- the reference's plain path.  One step = one
+iteration of the reference loop body (Advance, Boundary, Global_Boundary,
+ComputeDt, CaculateMass) over the whole grid.  Inputs are synthetic (the
+case plug-in in ibtfo_gb300/cases.py); the loop's t_end is lifted so that
+every timed iteration does its full work.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line (rank 0).  `value` is device-resident throughput in
+Gcell-updates/s (interior cells x steps / time), timed per step with CUDA
+events on the case's stream, L2 flushed between steps; `e2e` is the same
+metric through the C ABI with the state in pinned host memory, copied in
+and out every step.  With N > 1 (torchrun) every rank runs an independent
+replica of the case on its own GPU ("replicas only": the path has no
+cross-GPU exchange) and value sums all ranks' work over the slowest rank's
+time.  `--impl reference` times the reference algorithm on the host cores
+instead (the CPU oracle, OpenMP over all cores), rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+BYTES_PER_CELL = 65  # 32 B state read + 32 B state write + 1 B cell type (FP64)
+METRIC = "Gcell-updates/s"
+
+
+def workload():
+    from ibtfo_gb300 import cases
+    return cases.inclined_channel(2048, 1024)
+
+
+def config_json(w, l2="flushed between timed steps (256 MiB write)"):
+    g = w.grid
+    return {"workload": w.name, "n_x": g.n_x, "n_y": g.n_y, "domain": [g.lo_x, g.lo_y, g.hi_x, g.hi_y],
+            "scheme": w.scheme, "riemann": w.riemann, "limiter": w.limiter, "boundary": w.boundary,
+            "cfl": w.cfl, "gamma": w.gamma, "precision": "fp64", "l2": l2}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per sweep launch from the committed ncu summary, scaled to
+    the benchmark grid, or None."""
+    p = os.path.join(ROOT, "profiles", "sweep_inclined_channel.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("traffic_bytes_per_launch_full_grid:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.lines = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.gpu)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ CPU leg
+def cpu_oracle_rate(w, steps=None, warmup=1, budget_s=15.0):
+    """Times the CPU oracle (the reference algorithm restated in C, OpenMP
+    over all host cores) on the workload's full grid.  Returns
+    (Gcell-updates/s, ms/step, cores, steps)."""
+    import oracle
+    from ibtfo_gb300 import cases
+    g = w.grid
+    cores = os.cpu_count() or 1
+    oracle.set_threads(cores)
+    o = oracle.OracleCase(g.n_x, g.n_y, g.ng, (g.lo_x, g.lo_y), (g.hi_x, g.hi_y), w.gamma, w.cfl, w.scheme,
+                          w.riemann, w.limiter, w.boundary, w.gbc)
+    phi = cases.channel_phi(g)
+    o.setup_geometry(phi)
+    u0 = cases.channel_init(g, o.get("XYCOORD").reshape(-1, 6)[:, 5], w.gamma)
+    o.set_initial_state(u0)
+    if warmup:
+        o.run(warmup)
+    t0 = time.perf_counter()
+    o.run(1)
+    t1 = time.perf_counter() - t0
+    if steps is None:
+        steps = int(max(1, min(50, budget_s / max(t1, 1e-6))))
+    t0 = time.perf_counter()
+    o.run(steps)
+    dt = time.perf_counter() - t0
+    o.close()
+    ms = 1e3 * dt / steps
+    return g.n_x * g.n_y / (ms * 1e-3) / 1e9, ms, cores, steps
+
+
+# ------------------------------------------------------------------ GPU leg
+def gpu_arm(args, rank, world, local_rank):
+    import torch
+    import ibtfo_gb300 as ib
+    from ibtfo_gb300 import cases
+
+    torch.cuda.set_device(local_rank)
+    w = workload()
+    g = w.grid
+    cells = g.n_x * g.n_y
+    stream = torch.cuda.Stream()
+    c = ib.Case.from_workload(w, t_end=1e300, max_iter=2 ** 31 - 1)
+    c.set_stream(stream.cuda_stream)
+    phi = cases.channel_phi(g)
+    c.setup_geometry(phi)
+    u0 = cases.channel_init(g, c.cell_types(), w.gamma)
+    c.set_state(u0)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > 129 MB L2
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            c.enqueue_sweep()
+            c.enqueue_boundary()
+    stream.synchronize()
+
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = ib.launch_count()
+    with ClockSampler(local_rank) as clk:
+        with torch.cuda.stream(stream):
+            for k in range(args.steps):
+                flush.fill_(float(k))
+                ev[k][0].record(stream)
+                c.enqueue_sweep()
+                ev[k][1].record(stream)
+                c.enqueue_boundary()
+                ev[k][2].record(stream)
+        torch.cuda.synchronize()
+    launches = ib.launch_count() - launches0
+    if world > 1:
+        torch.distributed.barrier()
+    step_ms = sum(e[0].elapsed_time(e[2]) for e in ev)
+    sweep_ms = sum(e[0].elapsed_time(e[1]) for e in ev)
+    prog = c.progress()
+
+    # end to end through the C ABI with host buffers (pinned)
+    e2e_steps = max(1, min(args.steps, 20))
+    pin = ib.PinnedBuffer(g.M * g.N * 4)
+    c.get_state_ptr(pin.ptr)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        c.put_state_ptr(pin.ptr)
+        c.enqueue_sweep()
+        c.enqueue_boundary()
+        c.get_state_ptr(pin.ptr)
+        c.progress()
+    e2e_s = time.perf_counter() - t0
+    pin.close()
+
+    t = torch.tensor([step_ms, sweep_ms, e2e_s], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    step_ms, sweep_ms, e2e_s = (float(x) for x in t.tolist())
+    res = {"step_ms": step_ms, "sweep_ms": sweep_ms, "e2e_s": e2e_s, "e2e_steps": e2e_steps, "cells": cells,
+           "launches": launches, "clocks": clk.summary(), "progress": prog, "M": g.M, "N": g.N}
+    c.close()
+    return res
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    w = workload()
+    g = w.grid
+    cells = g.n_x * g.n_y
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        rate, ms, cores, n = cpu_oracle_rate(w, steps=args.steps, warmup=args.warmup)
+        sample = f"{args.warmup} warm-up + {n} timed steps of the full {g.n_x}x{g.n_y} grid"
+        line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": METRIC, "n_gpus": world,
+                "steps": n, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": config_json(w, l2="n/a (host cores)"),
+                "cpu_baseline": {"value": rate, "unit": METRIC, "cores": cores, "kind": "port", "sample": sample},
+                "e2e": {"value": rate, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return 0
+
+    if world > 1:
+        import torch
+        torch.cuda.set_device(local_rank)
+        torch.distributed.init_process_group("nccl")
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        rate, ms, cores, n = cpu_oracle_rate(w)
+        cpu = {"value": rate, "unit": METRIC, "cores": cores, "kind": "port",
+               "sample": f"1 warm-up + {n} timed steps of the full {g.n_x}x{g.n_y} grid, OpenMP over {cores} threads"}
+
+    r = gpu_arm(args, rank, world, local_rank)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+    if rank != 0:
+        return 0
+    K = args.steps
+    step_s = r["step_ms"] * 1e-3
+    value = world * cells * K / step_s / 1e9
+    sweep_s = r["sweep_ms"] * 1e-3 / K
+    peak, peak_kind = measured_peaks()
+    achieved = BYTES_PER_CELL * cells / sweep_s / 1e9
+    traffic = profiled_traffic()
+    state_bytes = r["M"] * r["N"] * 32
+    e2e_val = world * cells * r["e2e_steps"] / r["e2e_s"] / 1e9
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K, "warmup": args.warmup,
+            "ms_per_step": r["step_ms"] / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic", "config": config_json(w),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": traffic, "peak_source": peak_kind, "kernel": "sweep_kernel",
+                         "algorithmic_bytes_per_cell": BYTES_PER_CELL, "sweep_ms": r["sweep_ms"] / K},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_val, "unit": METRIC, "h2d_bytes_per_step": state_bytes,
+                    "d2h_bytes_per_step": state_bytes + 48, "steps": r["e2e_steps"]},
+            "gpu_launches": r["launches"], "clocks": r["clocks"],
+            "final": {"iter": r["progress"]["iter"], "nan_cells": r["progress"]["nan_cells"]}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,261 @@
+"""ibtfo_gb300: GB300-native (sm_103a) IBTFO per-timestep solver.
+
+Thin Python binding of the C ABI in include/ibtfo.h (libibtfo_gb300.so,
+built in-tree by ibtfo_gb300/build.py).  The names follow the reference's
+solver API: a `Case` is one problem with the reference's slot keys
+(Scheme, Riemann, Limiter, Boundary) and .inp numbers; its methods map to
+Psy_coord/Level_Set/Scheme_Index (setup_geometry), Initialize (set_state),
+and the time-loop body (advance/step/run).
+
+There is no CPU fallback: importing works without a GPU, but every solver
+call needs the compiled library and a CUDA device and raises if either is
+missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libibtfo_gb300.so")
+
+SCHEMES = {"MUSCL": 0, "MHM": 1, "Godunov": 2}
+RIEMANNS = {"HLL": 0, "HLLC": 1, "PVRS": 2, "StegerWarming": 3}
+LIMITERS = {"minmod": 0, "VanLeer": 1}
+BOUNDARIES = {"Regular": 0, "IDWBaseGFM": 1, "LinearBaseGFM": 2, "RiemannBaseGFM": 3, "BCGFM": 4, "HBCGFM": 5}
+GLOBAL_BCS = {"walls": 0, "periodic": 1}
+
+STATUS = {0: "OK", 1: "EINVAL", 2: "ENOMEM", 3: "ENAN", 4: "ETIMEOUT", 5: "ECUDA", 6: "ESTATE"}
+
+
+class IbtfoError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"IBTFO_{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Config(C.Structure):
+    _fields_ = [("n_x", C.c_int), ("n_y", C.c_int), ("num_ghost_cell", C.c_int),
+                ("lo_x", C.c_double), ("lo_y", C.c_double), ("hi_x", C.c_double), ("hi_y", C.c_double),
+                ("gamma", C.c_double), ("cfl_number", C.c_double), ("psy_time", C.c_double),
+                ("max_iter", C.c_int), ("scheme", C.c_int), ("riemann", C.c_int), ("limiter", C.c_int),
+                ("boundary", C.c_int), ("global_boundary", C.c_int), ("reserved", C.c_int * 8)]
+
+
+class Progress(C.Structure):
+    _fields_ = [("iter", C.c_int), ("status", C.c_int), ("nan_cells", C.c_int), ("reserved", C.c_int),
+                ("now_t", C.c_double), ("dt", C.c_double), ("mass", C.c_double), ("mass_start", C.c_double)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+
+
+# every entry point of include/ibtfo.h with its ctypes signature
+_P = C.c_void_p
+_DP = C.POINTER(C.c_double)
+SIGNATURES = {
+    "ibtfo_abi_version": (C.c_int, []),
+    "ibtfo_last_error": (C.c_char_p, []),
+    "ibtfo_launch_count": (C.c_longlong, []),
+    "ibtfo_create": (C.c_int, [C.POINTER(Config), C.POINTER(_P)]),
+    "ibtfo_destroy": (C.c_int, [_P]),
+    "ibtfo_set_stream": (C.c_int, [_P, _P]),
+    "ibtfo_setup_geometry": (C.c_int, [_P, _DP]),
+    "ibtfo_get_geometry": (C.c_int, [_P, _DP]),
+    "ibtfo_num_sch": (C.c_int, [_P]),
+    "ibtfo_get_scheme_index": (C.c_int, [_P, _DP]),
+    "ibtfo_num_ghost_cells": (C.c_int, [_P]),
+    "ibtfo_set_state": (C.c_int, [_P, _DP]),
+    "ibtfo_get_state": (C.c_int, [_P, _DP, _DP]),
+    "ibtfo_put_state": (C.c_int, [_P, _DP]),
+    "ibtfo_advance": (C.c_int, [_P, C.c_int]),
+    "ibtfo_enqueue_sweep": (C.c_int, [_P]),
+    "ibtfo_enqueue_boundary": (C.c_int, [_P]),
+    "ibtfo_step": (C.c_int, [_P, C.POINTER(Progress)]),
+    "ibtfo_run": (C.c_int, [_P, C.c_int, C.POINTER(Progress)]),
+    "ibtfo_get_progress": (C.c_int, [_P, C.POINTER(Progress)]),
+    "ibtfo_synchronize": (C.c_int, [_P]),
+    "ibtfo_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(_P)]),
+    "ibtfo_host_free": (C.c_int, [_P]),
+}
+
+_lib = None
+
+
+def lib():
+    """The loaded C library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run `python -m ibtfo_gb300.build` (needs nvcc)")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(code):
+    if code != 0:
+        raise IbtfoError(code, lib().ibtfo_last_error().decode(errors="replace"))
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(_DP)
+
+
+def launch_count() -> int:
+    return lib().ibtfo_launch_count()
+
+
+class Case:
+    """One problem resident on the current CUDA device."""
+
+    def __init__(self, n_x, n_y, ng=2, lo=(0.0, 0.0), hi=(1.0, 1.0), gamma=1.4, cfl=0.5, t_end=1.0,
+                 max_iter=100000, scheme="MUSCL", riemann="HLL", limiter="minmod", boundary="Regular",
+                 gbc="walls"):
+        L = lib()
+        cfg = Config(n_x, n_y, ng, lo[0], lo[1], hi[0], hi[1], gamma, cfl, t_end, max_iter,
+                     SCHEMES[scheme], RIEMANNS[riemann], LIMITERS[limiter], BOUNDARIES[boundary], GLOBAL_BCS[gbc])
+        h = _P()
+        _check(L.ibtfo_create(C.byref(cfg), C.byref(h)))
+        self.h = h
+        self.cfg = cfg
+        self.n_x, self.n_y, self.ng = n_x, n_y, ng
+        self.M, self.N = n_x + 2 * ng, n_y + 2 * ng
+        self.nsch = L.ibtfo_num_sch(h)
+
+    @classmethod
+    def from_workload(cls, w, **over):
+        g = w.grid
+        kw = dict(n_x=g.n_x, n_y=g.n_y, ng=g.ng, lo=(g.lo_x, g.lo_y), hi=(g.hi_x, g.hi_y), gamma=w.gamma, cfl=w.cfl,
+                  t_end=w.t_end, scheme=w.scheme, riemann=w.riemann, limiter=w.limiter, boundary=w.boundary,
+                  gbc=w.gbc)
+        kw.update(over)
+        return cls(**kw)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().ibtfo_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ---------------------------------------------------------- set-up
+    def setup_geometry(self, phi):
+        phi = np.ascontiguousarray(phi, dtype=np.float64).reshape(-1)
+        if phi.size != self.M * self.N:
+            raise ValueError("phi must have M*N values")
+        _check(lib().ibtfo_setup_geometry(self.h, _dp(phi)))
+
+    def get_geometry(self):
+        out = np.empty(self.M * self.N * 6)
+        _check(lib().ibtfo_get_geometry(self.h, _dp(out)))
+        return out
+
+    def get_scheme_index(self):
+        out = np.empty(self.M * self.N * self.nsch)
+        _check(lib().ibtfo_get_scheme_index(self.h, _dp(out)))
+        return out
+
+    @property
+    def num_ghost_cells(self):
+        return lib().ibtfo_num_ghost_cells(self.h)
+
+    def cell_types(self):
+        return self.get_geometry().reshape(-1, 6)[:, 5].copy()
+
+    def set_state(self, u0):
+        u0 = np.ascontiguousarray(u0, dtype=np.float64).reshape(-1)
+        if u0.size != self.M * self.N * 4:
+            raise ValueError("u0 must have M*N*4 values")
+        _check(lib().ibtfo_set_state(self.h, _dp(u0)))
+
+    def set_state_ptr(self, host_ptr: int):
+        """set_state from a raw host address (e.g. pinned memory), M*N*4 doubles."""
+        _check(lib().ibtfo_set_state(self.h, C.cast(C.c_void_p(host_ptr), _DP)))
+
+    def get_state(self, u_new=False):
+        uo = np.empty(self.M * self.N * 4)
+        un = np.empty(self.M * self.N * 4) if u_new else None
+        _check(lib().ibtfo_get_state(self.h, _dp(uo), _dp(un) if un is not None else None))
+        return (uo, un) if u_new else uo
+
+    def put_state(self, u):
+        u = np.ascontiguousarray(u, dtype=np.float64).reshape(-1)
+        if u.size != self.M * self.N * 4:
+            raise ValueError("u must have M*N*4 values")
+        _check(lib().ibtfo_put_state(self.h, _dp(u)))
+
+    def put_state_ptr(self, host_ptr: int):
+        _check(lib().ibtfo_put_state(self.h, C.cast(C.c_void_p(host_ptr), _DP)))
+
+    def get_state_ptr(self, host_ptr: int):
+        _check(lib().ibtfo_get_state(self.h, C.cast(C.c_void_p(host_ptr), _DP), None))
+
+    # ---------------------------------------------------------- stepping
+    def set_stream(self, stream_ptr: int | None):
+        _check(lib().ibtfo_set_stream(self.h, C.c_void_p(stream_ptr) if stream_ptr else None))
+
+    def advance(self, nsteps: int):
+        _check(lib().ibtfo_advance(self.h, int(nsteps)))
+
+    def enqueue_sweep(self):
+        _check(lib().ibtfo_enqueue_sweep(self.h))
+
+    def enqueue_boundary(self):
+        _check(lib().ibtfo_enqueue_boundary(self.h))
+
+    def step(self):
+        p = Progress()
+        _check(lib().ibtfo_step(self.h, C.byref(p)))
+        return p.as_dict()
+
+    def run(self, stop_on_nan=False):
+        p = Progress()
+        _check(lib().ibtfo_run(self.h, 1 if stop_on_nan else 0, C.byref(p)))
+        return p.as_dict()
+
+    def progress(self):
+        p = Progress()
+        _check(lib().ibtfo_get_progress(self.h, C.byref(p)))
+        return p.as_dict()
+
+    def synchronize(self):
+        _check(lib().ibtfo_synchronize(self.h))
+
+
+class PinnedBuffer:
+    """Page-locked host buffer of float64 (cudaHostAlloc through the C ABI)."""
+
+    def __init__(self, n):
+        p = _P()
+        _check(lib().ibtfo_host_alloc(8 * n, C.byref(p)))
+        self.ptr = p.value
+        self.n = n
+        self.array = np.ctypeslib.as_array(C.cast(p, _DP), shape=(n,))
+
+    def close(self):
+        if self.ptr:
+            lib().ibtfo_host_free(C.c_void_p(self.ptr))
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,329 @@
+// Per-step boundary pass (ghost-fluid fill over the compacted ghost list and
+// the domain-edge layers), the stand-alone CFL/mass reduction, and the
+// array-of-structures <-> structure-of-arrays conversion used at the host
+// boundary.
+//
+// State-buffer semantics.  The reference keeps U_OLD and U_NEW and, each
+// step, copies U_NEW into U_OLD and (ghost-fluid variants) snapshots U_OLD
+// into U_NEW before filling ghost cells (IDWBaseGFM/GFM_Bound.cpp:23-50);
+// Global_Boundary then reads U_NEW (Test/Sod/Global_Boudary.cpp:23-75).
+// Here the two buffers ping-pong: after a sweep, `next` holds the new fluid
+// values and `prev` the previous state, so the reference's snapshot S is
+//   S(i,j) = type(i,j) == 0 ? next(i,j) : prev(i,j)      (interior cells)
+//   S(ring) = prev(ring)            ghost-fluid variants (snapshot of U_OLD)
+//   S(ring) = initial values        Regular (U_NEW's ring is never written)
+// and this pass writes next's ghost cells and ring from S.
+#include "internal.h"
+#include "physics.cuh"
+#include "sweep_impl.cuh"
+
+namespace ibtfo {
+
+struct View
+{
+    const double *next, *prev;
+    const uint8_t *type;
+    long long P;
+    int pitch, ng, n_x, n_y;
+    __device__ __forceinline__ bool interior(int i, int j) const
+    {
+        return i >= ng && i < ng + n_x && j >= ng && j < ng + n_y;
+    }
+    // the reference's U_NEW at (i, j) when the boundary routines read it
+    __device__ __forceinline__ double S(int i, int j, int k) const
+    {
+        long long o = (long long)j * pitch + i;
+        const double *b = (interior(i, j) && type[o] == 0) ? next : prev;
+        return b[k * P + o];
+    }
+};
+
+// primitives of S at (i, j), as GFM_Bound.cpp:197-212 computes them
+__device__ __forceinline__ void prim(const View &v, int i, int j, double g, double &rho, double &u, double &w,
+                                     double &p)
+{
+    rho = v.S(i, j, 0);
+    u = v.S(i, j, 1) / rho;
+    w = v.S(i, j, 2) / rho;
+    p = (g - 1) * (v.S(i, j, 3) - 0.5 * rho * (u * u + w * w));
+}
+
+// inverse-distance average of the four bracket corners, GFM_Bound.cpp:214-217
+__device__ __forceinline__ void idw_average(const View &v, int idx, int idy, const double *a, double g, double w[4])
+{
+    double r[4], u[4], vv[4], p[4];
+    prim(v, idx, idy, g, r[0], u[0], vv[0], p[0]);
+    prim(v, idx, idy + 1, g, r[1], u[1], vv[1], p[1]);
+    prim(v, idx + 1, idy + 1, g, r[2], u[2], vv[2], p[2]);
+    prim(v, idx + 1, idy, g, r[3], u[3], vv[3], p[3]);
+    double s = a[0] + a[1] + a[2] + a[3];
+    w[0] = (a[0] * r[0] + a[1] * r[1] + a[2] * r[2] + a[3] * r[3]) / s;
+    w[1] = (a[0] * u[0] + a[1] * u[1] + a[2] * u[2] + a[3] * u[3]) / s;
+    w[2] = (a[0] * vv[0] + a[1] * vv[1] + a[2] * vv[2] + a[3] * vv[3]) / s;
+    w[3] = (a[0] * p[0] + a[1] * p[1] + a[2] * p[2] + a[3] * p[3]) / s;
+}
+
+// reflect the normal velocity and store conserved values, GFM_Bound.cpp:219-228
+__device__ __forceinline__ void store_reflected(double *dst, long long o, long long P, double g, double nx, double ny,
+                                                double rho_w, double u_w, double v_w, double p_w)
+{
+    double u_n = u_w * nx + v_w * ny;
+    double u_t = u_w * ny - v_w * nx;
+    u_n = -u_n;
+    u_w = u_n * nx + u_t * ny;
+    v_w = u_n * ny - u_t * nx;
+    dst[o] = rho_w;
+    dst[P + o] = rho_w * u_w;
+    dst[2 * P + o] = rho_w * v_w;
+    dst[3 * P + o] = p_w / (g - 1) + 0.5 * rho_w * (u_w * u_w + v_w * v_w);
+}
+
+__device__ void fill_ghost(const FillArgs &a, const View &v, double *dst, const GhostRec &h)
+{
+    const double g = a.g.gamma;
+    const long long o = (long long)h.j * a.g.pitch + h.i;
+    const long long P = a.g.plane;
+    if (a.bc == BC_IDW)
+    {
+        double w[4];
+        idw_average(v, h.idx, h.idy, h.w, g, w);
+        store_reflected(dst, o, P, g, h.nx, h.ny, w[0], w[1], w[2], w[3]);
+    }
+    else if (a.bc == BC_LINEAR || a.bc == BC_RIEMANNGFM)
+    {
+        // LinearBaseGFM/GFM_Bound.cpp:83-575: one corner's primitives (zeros if none is fluid)
+        double rho = 0, u = 0, w = 0, p = 0;
+        if (h.pick > 0)
+        {
+            const int ci = (h.pick == 1 || h.pick == 2) ? h.idx : h.idx + 1;
+            const int cj = (h.pick == 1 || h.pick == 4) ? h.idy : h.idy + 1;
+            prim(v, ci, cj, g, rho, u, w, p);
+        }
+        store_reflected(dst, o, P, g, h.nx, h.ny, rho, u, w, p);
+    }
+    else
+    {
+        // BCGFM/BCGFM_Bound.cpp:89-175 and HBCGFM_Bound.cpp (pure mirror when |phi| > delta)
+        double wi[4], we[4];
+        idw_average(v, h.idx, h.idy, h.w, g, wi);
+        idw_average(v, h.idx2, h.idy2, h.w2, g, we);
+        const double nx = h.nx, ny = h.ny, delta = h.delta, R_E = h.delta, R_G = h.rg;
+        double u_n_i = wi[1] * nx + wi[2] * ny;
+        double u_t_i = wi[1] * ny - wi[2] * nx;
+        double u_n_e = we[1] * nx + we[2] * ny;
+        double u_t_e = we[1] * ny - we[2] * nx;
+        double rho_m, p_m, u_t_m, u_n_m;
+        if (a.bc == BC_HBCGFM && h.hmirror)
+        {
+            rho_m = wi[0];
+            p_m = wi[3];
+            u_t_m = u_t_i;
+            u_n_m = -u_n_i;
+        }
+        else
+        {
+            rho_m = (wi[0] * ((delta + R_E) * (delta + R_E) - R_G * R_G) - we[0] * (delta * delta - R_G * R_G)) / (R_E * R_E + 2 * delta * R_E);
+            p_m = (wi[3] * ((delta + R_E) * (delta + R_E) - R_G * R_G) - we[3] * (delta * delta - R_G * R_G)) / (R_E * R_E + 2 * delta * R_E);
+            u_t_m = (u_t_i * ((delta + R_E) * (delta + R_E) - R_G * R_G) - u_t_e * (delta * delta - R_G * R_G)) / (R_E * R_E + 2 * delta * R_E);
+            u_n_m = -(u_n_i * ((delta + R_E) * (delta + R_E) - R_G * R_G) - u_n_e * (delta * delta - R_G * R_G)) / (R_E * R_E + 2 * delta * R_E);
+        }
+        double u_m = u_n_m * nx + u_t_m * ny;
+        double v_m = u_n_m * ny - u_t_m * nx;
+        dst[o] = rho_m;
+        dst[P + o] = rho_m * u_m;
+        dst[2 * P + o] = rho_m * v_m;
+        dst[3 * P + o] = p_m / (g - 1) + 0.5 * rho_m * (u_m * u_m + v_m * v_m);
+    }
+}
+
+// Global_Boundary, transmissive x / reflective y (Test/Sod/Global_Boudary.cpp:23-75),
+// or the periodic harness plug-in; `ring` enumerates row ghosts then column ghosts.
+__device__ void fill_ring(const FillArgs &a, const View &v, double *dst, long long q)
+{
+    const int ng = a.g.ng, n_x = a.g.n_x, n_y = a.g.n_y, N = a.g.N, pitch = a.g.pitch;
+    const long long P = a.g.plane;
+    const long long nrow = 2LL * ng * n_x;
+    int i, j;
+    bool row;
+    if (q < nrow)
+    {
+        row = true;
+        int r = (int)(q / n_x);
+        i = ng + (int)(q - (long long)r * n_x);
+        j = (r < ng) ? r : n_y + r; // r in [0, 2ng): bottom rows then top rows
+    }
+    else
+    {
+        row = false;
+        long long qq = q - nrow;
+        int c = (int)(qq / N);
+        j = (int)(qq - (long long)c * N);
+        i = (c < ng) ? c : n_x + c;
+    }
+    const long long o = (long long)j * pitch + i;
+    double out[4];
+    if (a.gb == GB_PERIODIC)
+    {
+        // rows from the opposite interior rows of S; columns from the opposite
+        // columns of the updated state (corners from the diagonal)
+        int si = i, sj = j;
+        if (!row)
+            si = (i < ng) ? i + n_x : i - n_x;
+        if (j < ng)
+            sj = j + n_y;
+        else if (j >= n_y + ng)
+            sj = j - n_y;
+        const bool src_interior_row = (sj >= ng && sj < ng + n_y);
+        for (int k = 0; k < 4; k++)
+        {
+            if (row || !src_interior_row || (sj != j))
+                out[k] = v.S(si, sj, k); // value S(.) of an interior cell
+            else
+                out[k] = v.next[k * P + (long long)sj * pitch + si]; // interior row, after the fill
+        }
+    }
+    else if (row)
+    {
+        const bool bottom = j < ng;
+        const int src = bottom ? 2 * ng - 1 : n_y + ng - 1;
+        const int mir = bottom ? 2 * ng - j - 1 : 2 * (n_y + ng) - 1 - j;
+        out[0] = v.S(i, src, 0);
+        out[1] = v.S(i, src, 1);
+        out[2] = -v.S(i, mir, 2);
+        out[3] = v.S(i, src, 3);
+    }
+    else
+    {
+        const int si = (i < ng) ? ng : n_x + ng - 1;
+        const bool ghost_row = (j < ng || j >= n_y + ng);
+        if (ghost_row && a.bc == BC_REGULAR)
+        {
+            const int side = (i < ng) ? 0 : 1;
+            const int rr = (j < ng) ? j : j - n_y; // [0, 2ng)
+            for (int k = 0; k < 4; k++)
+                out[k] = a.ring_ic[(side * 2 * ng + rr) * 4 + k];
+        }
+        else
+        {
+            for (int k = 0; k < 4; k++)
+                out[k] = v.S(si, j, k);
+        }
+    }
+    for (int k = 0; k < 4; k++)
+        dst[k * P + o] = out[k];
+}
+
+__global__ void __launch_bounds__(256) fill_kernel(const FillArgs a)
+{
+    DevState *st = a.st;
+    if (!a.init_mode && !st->fill_pending)
+        return;
+    const int cur = st->cur;
+    View v;
+    v.next = cur ? a.buf1 : a.buf0;
+    v.prev = cur ? a.buf0 : a.buf1;
+    v.type = a.type;
+    v.P = a.g.plane;
+    v.pitch = a.g.pitch;
+    v.ng = a.g.ng;
+    v.n_x = a.g.n_x;
+    v.n_y = a.g.n_y;
+    double *dst = cur ? a.buf1 : a.buf0;
+    const int gblocks = a.do_ghosts ? (a.nghost + 255) / 256 : 0;
+    if ((int)blockIdx.x < gblocks)
+    {
+        int t = blockIdx.x * 256 + threadIdx.x;
+        if (t < a.nghost)
+            fill_ghost(a, v, dst, a.ghosts[t]);
+        return;
+    }
+    if (!a.do_ring)
+        return;
+    long long q = (long long)(blockIdx.x - gblocks) * 256 + threadIdx.x;
+    long long nring = 2LL * a.g.ng * a.g.n_x + 2LL * a.g.ng * a.g.N;
+    if (q < nring)
+        fill_ring(a, v, dst, q);
+}
+
+void launch_fill(const FillArgs &a, cudaStream_t s)
+{
+    int gblocks = a.do_ghosts ? (a.nghost + 255) / 256 : 0;
+    long long nring = 2LL * a.g.ng * a.g.n_x + 2LL * a.g.ng * a.g.N;
+    int rblocks = a.do_ring ? (int)((nring + 255) / 256) : 0;
+    if (gblocks + rblocks == 0)
+        return;
+    fill_kernel<<<gblocks + rblocks, 256, 0, s>>>(a);
+    count_launch();
+}
+
+// ---------------------------------------------------------------- reduction
+
+// ComputeDt (Src/Base/Common/ComputeDt.cpp:4-51) and CaculateMass
+// (Src/Utils/CaculateMass.cpp:5-42) of one state, without stepping.
+__global__ void __launch_bounds__(TILE_X *TILE_Y) reduce_kernel(const ReduceArgs a)
+{
+    const GridDesc &g = a.g;
+    const int i = g.ng + blockIdx.x * TILE_X + (threadIdx.x % TILE_X);
+    const int j = g.ng + blockIdx.y * TILE_Y + (threadIdx.x / TILE_X);
+    double amax = 0, umax = 0, vmax = 0, mass = 0;
+    int nans = 0;
+    if (i < g.ng + g.n_x && j < g.ng + g.n_y)
+    {
+        long long o = (long long)j * g.pitch + i;
+        if (a.type[o] == 0)
+        {
+            double v[4];
+            for (int k = 0; k < 4; k++)
+                v[k] = a.u[k * g.plane + o];
+            cell_stats(v, g.gamma, g.dx, g.dy, amax, umax, vmax, mass, nans);
+        }
+    }
+    block_reduce_finalize<TILE_X * TILE_Y>(amax, umax, vmax, mass, nans, a.st, a.partial, g, false, a.set_start);
+}
+
+void launch_reduce(const ReduceArgs &a, int, cudaStream_t s)
+{
+    dim3 grid((a.g.n_x + TILE_X - 1) / TILE_X, (a.g.n_y + TILE_Y - 1) / TILE_Y);
+    reduce_kernel<<<grid, TILE_X * TILE_Y, 0, s>>>(a);
+    count_launch();
+}
+
+// ---------------------------------------------------------------- layouts
+
+__global__ void aos_to_soa_kernel(const double *__restrict__ aos, double *__restrict__ soa, GridDesc g)
+{
+    long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= (long long)g.M * g.N)
+        return;
+    int j = (int)(c / g.M), i = (int)(c - (long long)j * g.M);
+    long long o = (long long)j * g.pitch + i;
+    for (int k = 0; k < 4; k++)
+        soa[k * g.plane + o] = aos[c * 4 + k];
+}
+
+__global__ void soa_to_aos_kernel(const double *__restrict__ soa, double *__restrict__ aos, GridDesc g)
+{
+    long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= (long long)g.M * g.N)
+        return;
+    int j = (int)(c / g.M), i = (int)(c - (long long)j * g.M);
+    long long o = (long long)j * g.pitch + i;
+    for (int k = 0; k < 4; k++)
+        aos[c * 4 + k] = soa[k * g.plane + o];
+}
+
+void launch_aos_to_soa(const double *aos, double *soa, const GridDesc &g, cudaStream_t s)
+{
+    long long n = (long long)g.M * g.N;
+    aos_to_soa_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(aos, soa, g);
+    count_launch();
+}
+
+void launch_soa_to_aos(const double *soa, double *aos, const GridDesc &g, cudaStream_t s)
+{
+    long long n = (long long)g.M * g.N;
+    soa_to_aos_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(soa, aos, g);
+    count_launch();
+}
+
+} // namespace ibtfo

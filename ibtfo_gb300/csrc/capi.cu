@@ -1,0 +1,680 @@
+// C ABI (include/ibtfo.h): case lifetime, host transfers, step orchestration.
+//
+// A step is two launches on the case's stream: the fused sweep (which also
+// produces the next dt, the mass and the loop accounting in device memory)
+// and the boundary pass.  Because dt and the loop condition live on the
+// device, ibtfo_advance queues any number of steps without a host round trip;
+// chunks of steps are captured once into a CUDA graph and replayed.
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/ibtfo.h"
+#include "internal.h"
+#include "physics.cuh"
+
+namespace ibtfo {
+SweepLaunch sweep_launcher_muscl(int riemann, int limiter);
+SweepLaunch sweep_launcher_mhm(int riemann, int limiter);
+SweepLaunch sweep_launcher_godunov(int riemann, int limiter);
+
+SweepLaunch sweep_launcher(int scheme, int riemann, int limiter)
+{
+    const int r = (riemann == HLLC) ? HLL : riemann; // HLLC/Riemann_solver.cpp is HLL
+    switch (scheme)
+    {
+    case MHM: return sweep_launcher_mhm(r, limiter);
+    case GODUNOV: return sweep_launcher_godunov(r, limiter);
+    default: return sweep_launcher_muscl(r, limiter);
+    }
+}
+
+static std::atomic<long long> g_launches{0};
+void count_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+} // namespace ibtfo
+
+using namespace ibtfo;
+
+static thread_local std::string g_err;
+
+static ibtfo_status fail(ibtfo_status s, const std::string &msg)
+{
+    g_err = msg;
+    return s;
+}
+
+static ibtfo_status cuda_fail(cudaError_t e, const char *what)
+{
+    return fail(IBTFO_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                      \
+    do                                                \
+    {                                                 \
+        cudaError_t e_ = (call);                      \
+        if (e_ != cudaSuccess)                        \
+            return cuda_fail(e_, #call);              \
+    } while (0)
+
+struct ibtfo_case
+{
+    ibtfo_config cfg;
+    GridDesc g;
+    int device = 0;
+    cudaStream_t own = nullptr, stream = nullptr;
+    double *buf[2] = {nullptr, nullptr};
+    double *ic = nullptr;      // Regular: initial state (U_NEW's never-written cells)
+    double *staging = nullptr; // M*N*4 doubles, array-of-structures transfers
+    double *phi = nullptr, *nx = nullptr, *ny = nullptr;
+    uint8_t *type = nullptr;
+    GhostRec *ghosts = nullptr;
+    int nghost = 0;
+    DevState *st = nullptr;
+    double *partial = nullptr;
+    double *ring_ic = nullptr; // [2][2*ng][4]
+    int nblocks = 0;
+    bool geometry = false, state = false;
+    SweepLaunch sweep = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    int graph_steps = 0;
+};
+
+static int nsch_of(int bc)
+{
+    switch (bc)
+    {
+    case BC_IDW: return 8;
+    case BC_LINEAR:
+    case BC_RIEMANNGFM: return 4;
+    case BC_BCGFM:
+    case BC_HBCGFM: return 16;
+    default: return 1;
+    }
+}
+
+extern "C" {
+
+int ibtfo_abi_version(void) { return IBTFO_ABI_VERSION; }
+const char *ibtfo_last_error(void) { return g_err.c_str(); }
+long long ibtfo_launch_count(void) { return g_launches.load(); }
+
+ibtfo_status ibtfo_destroy(ibtfo_case *c)
+{
+    if (!c)
+        return IBTFO_OK;
+    cudaSetDevice(c->device);
+    if (c->stream)
+        cudaStreamSynchronize(c->stream);
+    if (c->graph)
+        cudaGraphExecDestroy(c->graph);
+    cudaFree(c->buf[0]);
+    cudaFree(c->buf[1]);
+    cudaFree(c->ic);
+    cudaFree(c->staging);
+    cudaFree(c->phi);
+    cudaFree(c->nx);
+    cudaFree(c->ny);
+    cudaFree(c->type);
+    cudaFree(c->ghosts);
+    cudaFree(c->st);
+    cudaFree(c->partial);
+    cudaFree(c->ring_ic);
+    if (c->own)
+        cudaStreamDestroy(c->own);
+    delete c;
+    return IBTFO_OK;
+}
+
+ibtfo_status ibtfo_create(const ibtfo_config *cfg, ibtfo_case **out)
+{
+    if (!cfg || !out)
+        return fail(IBTFO_EINVAL, "null argument");
+    *out = nullptr;
+    const ibtfo_config &k = *cfg;
+    if (k.n_x < 2 || k.n_y < 2 || k.num_ghost_cell < 2 || k.num_ghost_cell > 64)
+        return fail(IBTFO_EINVAL, "need n_x, n_y >= 2 and 2 <= num_ghost_cell <= 64");
+    if (k.n_x > 262144 || k.n_y > 262144 || (long long)(k.n_x + 2 * k.num_ghost_cell) * (k.n_y + 2 * k.num_ghost_cell) > (1LL << 31))
+        return fail(IBTFO_EINVAL, "grid too large (n_x, n_y <= 262144 and at most 2^31 cells)");
+    if (!(k.hi_x > k.lo_x) || !(k.hi_y > k.lo_y) || !(k.gamma > 1.0) || !(k.cfl_number > 0.0))
+        return fail(IBTFO_EINVAL, "need hi > lo, gamma > 1, cfl_number > 0");
+    if (k.scheme < 0 || k.scheme > 2 || k.riemann < 0 || k.riemann > 3 || k.limiter < 0 || k.limiter > 1 ||
+        k.boundary < 0 || k.boundary > 5 || k.global_boundary < 0 || k.global_boundary > 1)
+        return fail(IBTFO_EINVAL, "unknown scheme/riemann/limiter/boundary/global_boundary key");
+    if (k.global_boundary == IBTFO_GLOBAL_PERIODIC && (k.n_x < k.num_ghost_cell || k.n_y < k.num_ghost_cell))
+        return fail(IBTFO_EINVAL, "periodic boundaries need n_x, n_y >= num_ghost_cell");
+
+    ibtfo_case *c = new ibtfo_case();
+    c->cfg = k;
+    cudaGetDevice(&c->device);
+    GridDesc &g = c->g;
+    g.n_x = k.n_x;
+    g.n_y = k.n_y;
+    g.ng = k.num_ghost_cell;
+    g.M = k.n_x + 2 * g.ng;
+    g.N = k.n_y + 2 * g.ng;
+    g.pitch = (g.M + 31) / 32 * 32;
+    g.plane = (long long)g.pitch * g.N;
+    const double Psy_L = k.hi_x - k.lo_x, Psy_H = k.hi_y - k.lo_y;
+    g.dx = Psy_L / k.n_x; // MUSCL_Scheme.cpp:20 and Psy_coord.cpp:29
+    g.dy = Psy_H / k.n_y; // MUSCL_Scheme.cpp:21
+    g.Li = -g.dx * g.ng + k.lo_x + g.dx / 2; // Psy_coord.cpp:33-34 (dy := dx there)
+    g.Hi = -g.dx * g.ng + k.lo_y + g.dx / 2;
+    g.gamma = k.gamma;
+    g.cfl = k.cfl_number;
+    c->nblocks = ((k.n_x + TILE_X - 1) / TILE_X) * ((k.n_y + TILE_Y - 1) / TILE_Y);
+    c->sweep = sweep_launcher(k.scheme, k.riemann, k.limiter);
+
+    const size_t cells = (size_t)g.M * g.N;
+    const size_t plane_bytes = sizeof(double) * (size_t)g.plane;
+    cudaError_t e = cudaSuccess;
+    auto A = [&](void **p, size_t bytes) {
+        if (e == cudaSuccess)
+            e = cudaMalloc(p, bytes);
+        if (e == cudaSuccess)
+            e = cudaMemset(*p, 0, bytes);
+    };
+    A((void **)&c->buf[0], 4 * plane_bytes);
+    A((void **)&c->buf[1], 4 * plane_bytes);
+    if (k.boundary == IBTFO_BOUNDARY_REGULAR)
+        A((void **)&c->ic, 4 * plane_bytes);
+    A((void **)&c->staging, sizeof(double) * 4 * cells);
+    A((void **)&c->phi, plane_bytes);
+    A((void **)&c->nx, plane_bytes);
+    A((void **)&c->ny, plane_bytes);
+    A((void **)&c->type, (size_t)g.plane);
+    A((void **)&c->st, sizeof(DevState));
+    A((void **)&c->partial, sizeof(double) * (size_t)c->nblocks);
+    A((void **)&c->ring_ic, sizeof(double) * 2 * 2 * g.ng * 4);
+    if (e == cudaSuccess)
+        e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
+    if (e != cudaSuccess)
+    {
+        ibtfo_status s = (e == cudaErrorMemoryAllocation) ? fail(IBTFO_ENOMEM, "device allocation failed")
+                                                          : cuda_fail(e, "ibtfo_create");
+        cudaGetLastError();
+        ibtfo_destroy(c);
+        return s;
+    }
+    c->stream = c->own;
+    *out = c;
+    return IBTFO_OK;
+}
+
+ibtfo_status ibtfo_set_stream(ibtfo_case *c, void *stream)
+{
+    if (!c)
+        return fail(IBTFO_EINVAL, "null case");
+    cudaSetDevice(c->device);
+    CK(cudaStreamSynchronize(c->stream));
+    c->stream = stream ? (cudaStream_t)stream : c->own;
+    if (c->graph)
+    {
+        cudaGraphExecDestroy(c->graph);
+        c->graph = nullptr;
+        c->graph_steps = 0;
+    }
+    return IBTFO_OK;
+}
+
+int ibtfo_num_sch(const ibtfo_case *c) { return c ? nsch_of(c->cfg.boundary) : 0; }
+int ibtfo_num_ghost_cells(const ibtfo_case *c) { return c ? c->nghost : 0; }
+
+ibtfo_status ibtfo_setup_geometry(ibtfo_case *c, const double *phi)
+{
+    if (!c || !phi)
+        return fail(IBTFO_EINVAL, "null argument");
+    cudaSetDevice(c->device);
+    const GridDesc &g = c->g;
+    CK(cudaMemcpy2DAsync(c->phi, sizeof(double) * g.pitch, phi, sizeof(double) * g.M, sizeof(double) * g.M, g.N,
+                         cudaMemcpyHostToDevice, c->stream));
+    if (c->ghosts)
+    {
+        cudaFree(c->ghosts);
+        c->ghosts = nullptr;
+        c->nghost = 0;
+    }
+    int rc = setup_geometry(g, c->cfg.boundary, c->phi, c->nx, c->ny, c->type, &c->ghosts, &c->nghost, c->stream);
+    if (rc == 2)
+        return fail(IBTFO_ENOMEM, "ghost list allocation failed");
+    if (rc != 0)
+        return cuda_fail(cudaGetLastError(), "geometry set-up");
+    CK(cudaStreamSynchronize(c->stream));
+    c->geometry = true;
+    c->state = false;
+    return IBTFO_OK;
+}
+
+ibtfo_status ibtfo_get_geometry(ibtfo_case *c, double *xy)
+{
+    if (!c || !xy)
+        return fail(IBTFO_EINVAL, "null argument");
+    if (!c->geometry)
+        return fail(IBTFO_ESTATE, "ibtfo_setup_geometry has not run");
+    cudaSetDevice(c->device);
+    const GridDesc &g = c->g;
+    std::vector<double> phi((size_t)g.plane), nx((size_t)g.plane), ny((size_t)g.plane);
+    std::vector<uint8_t> t((size_t)g.plane);
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpy(phi.data(), c->phi, sizeof(double) * g.plane, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(nx.data(), c->nx, sizeof(double) * g.plane, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(ny.data(), c->ny, sizeof(double) * g.plane, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(t.data(), c->type, (size_t)g.plane, cudaMemcpyDeviceToHost));
+    for (int j = 0; j < g.N; j++)
+        for (int i = 0; i < g.M; i++)
+        {
+            size_t o = (size_t)j * g.pitch + i;
+            double *r = xy + ((size_t)g.M * j + i) * 6;
+            r[0] = g.Li + i * g.dx; // Psy_coord.cpp:42-43
+            r[1] = g.Hi + j * g.dx;
+            r[2] = phi[o];
+            r[3] = nx[o];
+            r[4] = ny[o];
+            r[5] = (double)t[o];
+        }
+    return IBTFO_OK;
+}
+
+ibtfo_status ibtfo_get_scheme_index(ibtfo_case *c, double *sch)
+{
+    if (!c || !sch)
+        return fail(IBTFO_EINVAL, "null argument");
+    if (!c->geometry)
+        return fail(IBTFO_ESTATE, "ibtfo_setup_geometry has not run");
+    cudaSetDevice(c->device);
+    const GridDesc &g = c->g;
+    const int ns = nsch_of(c->cfg.boundary);
+    memset(sch, 0, sizeof(double) * (size_t)g.M * g.N * ns);
+    if (c->nghost == 0)
+        return IBTFO_OK;
+    std::vector<GhostRec> gl(c->nghost);
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpy(gl.data(), c->ghosts, sizeof(GhostRec) * c->nghost, cudaMemcpyDeviceToHost));
+    for (const GhostRec &r : gl)
+    {
+        double *s = sch + ((size_t)g.M * r.j + r.i) * ns;
+        s[0] = r.xm;
+        s[1] = r.ym;
+        s[2] = r.idx;
+        s[3] = r.idy;
+        if (ns >= 8)
+            for (int q = 0; q < 4; q++)
+                s[4 + q] = r.w[q];
+        if (ns == 16)
+        {
+            s[8] = r.xm2;
+            s[9] = r.ym2;
+            s[10] = r.idx2;
+            s[11] = r.idy2;
+            for (int q = 0; q < 4; q++)
+                s[12 + q] = r.w2[q];
+        }
+    }
+    return IBTFO_OK;
+}
+
+static FillArgs fill_args(ibtfo_case *c)
+{
+    FillArgs a{};
+    a.g = c->g;
+    a.buf0 = c->buf[0];
+    a.buf1 = c->buf[1];
+    a.type = c->type;
+    a.st = c->st;
+    a.ghosts = c->ghosts;
+    a.nghost = c->nghost;
+    a.bc = c->cfg.boundary;
+    a.gb = c->cfg.global_boundary;
+    a.ring_ic = c->ring_ic;
+    return a;
+}
+
+static SweepArgs sweep_args(ibtfo_case *c, int guard)
+{
+    SweepArgs a{};
+    a.g = c->g;
+    a.buf0 = c->buf[0];
+    a.buf1 = c->buf[1];
+    a.type = c->type;
+    a.st = c->st;
+    a.partial = c->partial;
+    a.t_end = c->cfg.psy_time;
+    a.max_iter = c->cfg.max_iter;
+    a.guard = guard;
+    return a;
+}
+
+// the boundary pass after a sweep (ghost fill + domain edges)
+static void enqueue_boundary(ibtfo_case *c)
+{
+    FillArgs f = fill_args(c);
+    const bool gfm = c->cfg.boundary != IBTFO_BOUNDARY_REGULAR;
+    if (gfm && c->cfg.global_boundary == IBTFO_GLOBAL_PERIODIC)
+    {
+        // periodic columns copy filled interior cells: fill first, edges second
+        f.do_ghosts = 1;
+        f.do_ring = 0;
+        launch_fill(f, c->stream);
+        f.do_ghosts = 0;
+        f.do_ring = 1;
+        launch_fill(f, c->stream);
+    }
+    else
+    {
+        f.do_ghosts = gfm ? 1 : 0;
+        f.do_ring = 1;
+        launch_fill(f, c->stream);
+    }
+}
+
+static void enqueue_step(ibtfo_case *c, int guard)
+{
+    const GridDesc &g = c->g;
+    dim3 grid((g.n_x + TILE_X - 1) / TILE_X, (g.n_y + TILE_Y - 1) / TILE_Y);
+    c->sweep(sweep_args(c, guard), grid, dim3(TILE_X * TILE_Y), c->stream);
+    count_launch();
+    enqueue_boundary(c);
+}
+
+ibtfo_status ibtfo_set_state(ibtfo_case *c, const double *u0)
+{
+    if (!c || !u0)
+        return fail(IBTFO_EINVAL, "null argument");
+    if (!c->geometry)
+        return fail(IBTFO_ESTATE, "ibtfo_setup_geometry must run before ibtfo_set_state");
+    cudaSetDevice(c->device);
+    const GridDesc &g = c->g;
+    const size_t cells = (size_t)g.M * g.N;
+    CK(cudaMemcpyAsync(c->staging, u0, sizeof(double) * 4 * cells, cudaMemcpyHostToDevice, c->stream));
+    launch_aos_to_soa(c->staging, c->buf[0], g, c->stream);
+    CK(cudaMemcpyAsync(c->buf[1], c->buf[0], sizeof(double) * 4 * (size_t)g.plane, cudaMemcpyDeviceToDevice,
+                       c->stream));
+    if (c->ic)
+        CK(cudaMemcpyAsync(c->ic, c->buf[0], sizeof(double) * 4 * (size_t)g.plane, cudaMemcpyDeviceToDevice,
+                           c->stream));
+    // initial values at the corner-column sources (columns ng and N_x+ng-1, ghost rows)
+    std::vector<double> ring(2 * 2 * g.ng * 4);
+    for (int side = 0; side < 2; side++)
+        for (int rr = 0; rr < 2 * g.ng; rr++)
+        {
+            int i = side ? g.n_x + g.ng - 1 : g.ng;
+            int j = (rr < g.ng) ? rr : g.n_y + rr;
+            for (int k = 0; k < 4; k++)
+                ring[(side * 2 * g.ng + rr) * 4 + k] = u0[((size_t)g.M * j + i) * 4 + k];
+        }
+    CK(cudaMemcpyAsync(c->ring_ic, ring.data(), sizeof(double) * ring.size(), cudaMemcpyHostToDevice, c->stream));
+    DevState s{};
+    const bool gfm = c->cfg.boundary != IBTFO_BOUNDARY_REGULAR;
+    s.cur = gfm ? 1 : 0; // the initial Boundary call writes the ghost cells into buffer 1
+    CK(cudaMemcpyAsync(c->st, &s, sizeof(DevState), cudaMemcpyHostToDevice, c->stream));
+    if (gfm)
+    {
+        FillArgs f = fill_args(c);
+        f.do_ghosts = 1;
+        f.do_ring = 0;
+        f.init_mode = 1;
+        launch_fill(f, c->stream);
+    }
+    ReduceArgs r{};
+    r.g = g;
+    r.u = c->buf[s.cur];
+    r.type = c->type;
+    r.st = c->st;
+    r.partial = c->partial;
+    r.set_start = 1;
+    launch_reduce(r, c->nblocks, c->stream);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->stream));
+    c->state = true;
+    return IBTFO_OK;
+}
+
+ibtfo_status ibtfo_put_state(ibtfo_case *c, const double *u)
+{
+    if (!c || !u)
+        return fail(IBTFO_EINVAL, "null argument");
+    if (!c->state)
+        return fail(IBTFO_ESTATE, "no state: call ibtfo_set_state first");
+    cudaSetDevice(c->device);
+    const GridDesc &g = c->g;
+    DevState s;
+    CK(cudaMemcpyAsync(&s, c->st, sizeof(DevState), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpyAsync(c->staging, u, sizeof(double) * 4 * (size_t)g.M * g.N, cudaMemcpyHostToDevice, c->stream));
+    launch_aos_to_soa(c->staging, c->buf[s.cur], g, c->stream);
+    CK(cudaGetLastError());
+    return IBTFO_OK;
+}
+
+ibtfo_status ibtfo_get_progress(ibtfo_case *c, ibtfo_progress *p)
+{
+    if (!c || !p)
+        return fail(IBTFO_EINVAL, "null argument");
+    cudaSetDevice(c->device);
+    DevState s;
+    CK(cudaMemcpyAsync(&s, c->st, sizeof(DevState), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    p->iter = s.iter;
+    p->status = s.status;
+    p->nan_cells = s.nan_cells;
+    p->reserved = 0;
+    p->now_t = s.now_t;
+    p->dt = s.dt;
+    p->mass = s.mass;
+    p->mass_start = s.mass_start;
+    return IBTFO_OK;
+}
+
+ibtfo_status ibtfo_synchronize(ibtfo_case *c)
+{
+    if (!c)
+        return fail(IBTFO_EINVAL, "null case");
+    cudaSetDevice(c->device);
+    CK(cudaStreamSynchronize(c->stream));
+    return IBTFO_OK;
+}
+
+// U_NEW of the reference: the snapshot the boundary routines read (interior
+// fluid cells from the current buffer, other interior cells from the
+// previous one; edge ring from the previous buffer, or from the initial state
+// for Regular, whose U_NEW ring is never written)
+__global__ void export_unew_kernel(GridDesc g, const double *cur, const double *prev, const double *ring_src,
+                                   const uint8_t *type, double *aos)
+{
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= (long long)g.M * g.N)
+        return;
+    int j = (int)(q / g.M), i = (int)(q - (long long)j * g.M);
+    long long o = (long long)j * g.pitch + i;
+    bool in = i >= g.ng && i < g.ng + g.n_x && j >= g.ng && j < g.ng + g.n_y;
+    const double *b = in ? ((type[o] == 0) ? cur : prev) : ring_src;
+    for (int k = 0; k < 4; k++)
+        aos[q * 4 + k] = b[k * g.plane + o];
+}
+
+ibtfo_status ibtfo_get_state(ibtfo_case *c, double *u_old, double *u_new)
+{
+    if (!c)
+        return fail(IBTFO_EINVAL, "null case");
+    if (!c->state)
+        return fail(IBTFO_ESTATE, "no state: call ibtfo_set_state first");
+    cudaSetDevice(c->device);
+    const GridDesc &g = c->g;
+    const size_t cells = (size_t)g.M * g.N;
+    DevState s;
+    CK(cudaMemcpyAsync(&s, c->st, sizeof(DevState), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (u_old)
+    {
+        launch_soa_to_aos(c->buf[s.cur], c->staging, g, c->stream);
+        CK(cudaMemcpyAsync(u_old, c->staging, sizeof(double) * 4 * cells, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    }
+    if (u_new)
+    {
+        const double *cur = c->buf[s.cur], *prev = c->buf[s.cur ^ 1];
+        const double *ring = c->ic ? c->ic : prev;
+        export_unew_kernel<<<(unsigned)((cells + 255) / 256), 256, 0, c->stream>>>(g, cur, prev, ring, c->type,
+                                                                                 c->staging);
+        count_launch();
+        CK(cudaMemcpyAsync(u_new, c->staging, sizeof(double) * 4 * cells, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    }
+    CK(cudaGetLastError());
+    return IBTFO_OK;
+}
+
+static const int GRAPH_STEPS = 16;
+
+static ibtfo_status build_graph(ibtfo_case *c)
+{
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    long long before = g_launches.load();
+    for (int s = 0; s < GRAPH_STEPS; s++)
+        enqueue_step(c, 1);
+    g_launches.store(before); // captured launches are counted when replayed
+    cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "graph capture");
+    e = cudaGraphInstantiate(&c->graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "graph instantiate");
+    c->graph_steps = GRAPH_STEPS;
+    return IBTFO_OK;
+}
+
+ibtfo_status ibtfo_advance(ibtfo_case *c, int nsteps)
+{
+    if (!c)
+        return fail(IBTFO_EINVAL, "null case");
+    if (!c->state)
+        return fail(IBTFO_ESTATE, "no state: call ibtfo_set_state first");
+    if (nsteps < 0)
+        return fail(IBTFO_EINVAL, "nsteps < 0");
+    cudaSetDevice(c->device);
+    const int per_step = 1 + ((c->cfg.boundary != IBTFO_BOUNDARY_REGULAR &&
+                               c->cfg.global_boundary == IBTFO_GLOBAL_PERIODIC) ? 2 : 1);
+    int left = nsteps;
+    if (left >= GRAPH_STEPS)
+    {
+        if (!c->graph)
+        {
+            ibtfo_status s = build_graph(c);
+            if (s != IBTFO_OK)
+                return s;
+        }
+        while (left >= GRAPH_STEPS)
+        {
+            CK(cudaGraphLaunch(c->graph, c->stream));
+            count_launch(GRAPH_STEPS * per_step);
+            left -= GRAPH_STEPS;
+        }
+    }
+    for (; left > 0; left--)
+        enqueue_step(c, 1);
+    CK(cudaGetLastError());
+    return IBTFO_OK;
+}
+
+ibtfo_status ibtfo_enqueue_sweep(ibtfo_case *c)
+{
+    if (!c)
+        return fail(IBTFO_EINVAL, "null case");
+    if (!c->state)
+        return fail(IBTFO_ESTATE, "no state: call ibtfo_set_state first");
+    cudaSetDevice(c->device);
+    const GridDesc &g = c->g;
+    dim3 grid((g.n_x + TILE_X - 1) / TILE_X, (g.n_y + TILE_Y - 1) / TILE_Y);
+    c->sweep(sweep_args(c, 1), grid, dim3(TILE_X * TILE_Y), c->stream);
+    count_launch();
+    CK(cudaGetLastError());
+    return IBTFO_OK;
+}
+
+ibtfo_status ibtfo_enqueue_boundary(ibtfo_case *c)
+{
+    if (!c)
+        return fail(IBTFO_EINVAL, "null case");
+    if (!c->state)
+        return fail(IBTFO_ESTATE, "no state: call ibtfo_set_state first");
+    cudaSetDevice(c->device);
+    enqueue_boundary(c);
+    CK(cudaGetLastError());
+    return IBTFO_OK;
+}
+
+ibtfo_status ibtfo_step(ibtfo_case *c, ibtfo_progress *p)
+{
+    if (!c)
+        return fail(IBTFO_EINVAL, "null case");
+    if (!c->state)
+        return fail(IBTFO_ESTATE, "no state: call ibtfo_set_state first");
+    cudaSetDevice(c->device);
+    enqueue_step(c, 0);
+    CK(cudaGetLastError());
+    if (p)
+        return ibtfo_get_progress(c, p);
+    CK(cudaStreamSynchronize(c->stream));
+    return IBTFO_OK;
+}
+
+ibtfo_status ibtfo_run(ibtfo_case *c, int stop_on_nan, ibtfo_progress *p)
+{
+    if (!c)
+        return fail(IBTFO_EINVAL, "null case");
+    ibtfo_progress q;
+    ibtfo_status s = ibtfo_get_progress(c, &q);
+    if (s != IBTFO_OK)
+        return s;
+    while (q.now_t < c->cfg.psy_time && q.iter < c->cfg.max_iter)
+    {
+        // queue about as many steps as the current dt says are left (extra ones do nothing)
+        double left = (c->cfg.psy_time - q.now_t) / q.dt;
+        int n = (std::isfinite(left) && left > 0) ? (int)std::min(left + 1.0, 4096.0) : 4096;
+        n = std::min(n, c->cfg.max_iter - q.iter);
+        n = std::max(n, 1);
+        if (stop_on_nan)
+            n = std::min(n, 64);
+        s = ibtfo_advance(c, n);
+        if (s != IBTFO_OK)
+            return s;
+        s = ibtfo_get_progress(c, &q);
+        if (s != IBTFO_OK)
+            return s;
+        if (stop_on_nan && (q.status & STATUS_NAN))
+        {
+            if (p)
+                *p = q;
+            return fail(IBTFO_ENAN, "NaN in the state");
+        }
+    }
+    if (p)
+        *p = q;
+    return IBTFO_OK;
+}
+
+ibtfo_status ibtfo_host_alloc(size_t bytes, void **p)
+{
+    if (!p)
+        return fail(IBTFO_EINVAL, "null argument");
+    cudaError_t e = cudaHostAlloc(p, bytes, cudaHostAllocDefault);
+    if (e != cudaSuccess)
+    {
+        *p = nullptr;
+        return fail(IBTFO_ENOMEM, std::string("cudaHostAlloc: ") + cudaGetErrorString(e));
+    }
+    return IBTFO_OK;
+}
+
+ibtfo_status ibtfo_host_free(void *p)
+{
+    if (p)
+        cudaFreeHost(p);
+    return IBTFO_OK;
+}
+
+} // extern "C"

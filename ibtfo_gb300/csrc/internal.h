@@ -1,0 +1,120 @@
+// Internal data structures shared by the CUDA translation units.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace ibtfo {
+
+enum Boundary { BC_REGULAR = 0, BC_IDW = 1, BC_LINEAR = 2, BC_RIEMANNGFM = 3, BC_BCGFM = 4, BC_HBCGFM = 5 };
+enum GlobalBC { GB_WALLS = 0, GB_PERIODIC = 1 };
+
+// Per-case scalars that live in device memory so that consecutive steps run
+// without a host round trip: the dt to apply next, the reference's loop
+// accounting (now_t, iter), the ping-pong selector and the reduction state.
+struct DevState
+{
+    double dt;         // dt applied by the next step (ComputeDt of the current state)
+    double now_t;      // reference loop time, advanced by the dt computed after each step
+    double mass;       // CaculateMass of the current state
+    double mass_start; // CaculateMass of the initial state
+    unsigned long long amax_bits, umax_bits, vmax_bits; // running maxima (non-negative doubles)
+    int iter;          // completed steps
+    int cur;           // buffer holding the current state
+    int fill_pending;  // a step completed and its boundary pass has not run yet
+    int nan_cells;     // fluid cells with a NaN component, summed over steps
+    unsigned int ticket;       // blocks finished in the current reduction launch
+    int status;                // bit flags, see STATUS_*
+    double last_amax, last_umax, last_vmax; // maxima behind the latest dt
+};
+
+enum { STATUS_NAN = 1 };
+
+// One ghost-fluid cell (interior cell of type 2) with everything its fill
+// needs, computed once at set-up (reference Scheme_Index).
+struct GhostRec
+{
+    int i, j;
+    int idx, idy;   // bracket of the image point (lower-left corner)
+    int idx2, idy2; // bracket of the extra point (BCGFM/HBCGFM)
+    int pick;       // LinearBaseGFM: chosen corner 1..4, 0 if none is fluid
+    int hmirror;    // HBCGFM: |phi| > delta (pure mirror)
+    double xm, ym;  // image point
+    double xm2, ym2; // extra point
+    double w[4];    // inverse-distance weights, corners (idx,idy),(idx,idy+1),(idx+1,idy+1),(idx+1,idy)
+    double w2[4];   // extra-point weights
+    double nx, ny;  // unnormalised level-set gradient
+    double rg;      // |phi|
+    double delta;   // half cell diagonal (BCGFM/HBCGFM)
+};
+
+// Geometry of the padded grid.  Arrays are structure-of-arrays planes with a
+// row pitch (elements) that keeps every row 256-byte aligned.
+struct GridDesc
+{
+    int n_x, n_y, ng, M, N, pitch;
+    long long plane; // elements per plane
+    double dx, dy;   // update spacings: Psy_L/N_x and Psy_H/N_y
+    double Li, Hi;   // coordinate of cell (0,0) centre: x_i = Li + i*dx, y_j = Hi + j*dx
+    double gamma, cfl;
+};
+
+struct SweepArgs
+{
+    GridDesc g;
+    double *buf0, *buf1;     // two state buffers, 4 planes each
+    const uint8_t *type;     // cell type plane (uint8, same pitch)
+    DevState *st;
+    double *partial;         // one mass partial per block
+    double t_end;
+    int max_iter;
+    int guard;               // apply the reference loop condition before stepping
+};
+
+struct FillArgs
+{
+    GridDesc g;
+    double *buf0, *buf1;
+    const uint8_t *type;
+    DevState *st;
+    const GhostRec *ghosts;
+    int nghost;
+    int bc;          // Boundary variant
+    int gb;          // GlobalBC
+    int do_ghosts;   // run the ghost-fluid fill
+    int do_ring;     // run the domain-edge (Global_Boundary) pass
+    int init_mode;   // initial Boundary call: fill without requiring a completed step
+    const double *ring_ic; // Regular: initial values feeding the corner columns [2][2*ng][4]
+};
+
+struct ReduceArgs
+{
+    GridDesc g;
+    const double *u;       // state planes to reduce
+    const uint8_t *type;
+    DevState *st;
+    double *partial;
+    int set_start;         // also store mass as mass_start
+};
+
+typedef void (*SweepLaunch)(const SweepArgs &, dim3 grid, dim3 block, cudaStream_t s);
+
+// sweep tile (interior cells per CTA)
+constexpr int TILE_X = 32;
+constexpr int TILE_Y = 8;
+
+SweepLaunch sweep_launcher(int scheme, int riemann, int limiter);
+void launch_fill(const FillArgs &a, cudaStream_t s);
+void launch_reduce(const ReduceArgs &a, int nblocks_max, cudaStream_t s);
+void launch_aos_to_soa(const double *aos, double *soa, const GridDesc &g, cudaStream_t s);
+void launch_soa_to_aos(const double *soa, double *aos, const GridDesc &g, cudaStream_t s);
+
+// geometry set-up (geometry.cu)
+int setup_geometry(const GridDesc &g, int bc, const double *d_phi, double *d_nx, double *d_ny, uint8_t *d_type,
+                   GhostRec **d_ghosts, int *nghost, cudaStream_t s);
+
+// kernel launch counter (every launch made by the library)
+void count_launch(int n = 1);
+
+} // namespace ibtfo

@@ -1,0 +1,145 @@
+/* ibtfo.h -- C ABI of the GB300 (sm_103a) IBTFO per-timestep solver.
+ *
+ * One `ibtfo_case` is one 2D compressible-Euler problem resident on one GPU:
+ * the reference's Src/Base + Src/BoundaryCondition + Src/Geometry hot path
+ * (Advance, Riemann solvers, limiters, ghost-fluid Boundary,
+ * Global_Boundary, ComputeDt, CaculateMass, Level_Set/Scheme_Index set-up)
+ * behind plain pointers and sizes.  All host arrays use the reference's
+ * array-of-structures layout with M = N_x + 2*num_ghost_cell columns and
+ * N = N_y + 2*num_ghost_cell rows:
+ *   state     U[(M*j + i)*4 + k]   k = rho, rho*u, rho*v, E   (EQDefine.H:31)
+ *   geometry  XY[(M*j + i)*6 + c]  c = x, y, phi, n_x, n_y, type (CoordDefine.H:7)
+ *   level set PHI[M*j + i]
+ * Host pointers are only read or written during the call that receives them.
+ * Functions return IBTFO_OK or an error code; ibtfo_last_error() describes
+ * the last failure of the calling thread.
+ */
+#ifndef IBTFO_H
+#define IBTFO_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define IBTFO_ABI_VERSION 1
+
+typedef enum ibtfo_status {
+    IBTFO_OK = 0,
+    IBTFO_EINVAL = 1,   /* bad argument or configuration */
+    IBTFO_ENOMEM = 2,   /* device or pinned-host allocation failed */
+    IBTFO_ENAN = 3,     /* the state holds NaN (reported by ibtfo_run when asked to stop on NaN) */
+    IBTFO_ETIMEOUT = 4, /* a bounded wait gave up */
+    IBTFO_ECUDA = 5,    /* a CUDA runtime call failed */
+    IBTFO_ESTATE = 6    /* call out of order (e.g. stepping before ibtfo_set_state) */
+} ibtfo_status;
+
+/* selection keys: the reference Makefile slots Scheme / Riemann / Limiter /
+ * Boundary (Test/Sod/Makefile:1-7) and the per-case Global_Boundary plug-in */
+enum { IBTFO_SCHEME_MUSCL = 0, IBTFO_SCHEME_MHM = 1, IBTFO_SCHEME_GODUNOV = 2 };
+enum { IBTFO_RIEMANN_HLL = 0, IBTFO_RIEMANN_HLLC = 1, IBTFO_RIEMANN_PVRS = 2, IBTFO_RIEMANN_STEGER_WARMING = 3 };
+enum { IBTFO_LIMITER_MINMOD = 0, IBTFO_LIMITER_VANLEER = 1 };
+enum {
+    IBTFO_BOUNDARY_REGULAR = 0,
+    IBTFO_BOUNDARY_IDW_GFM = 1,     /* IDWBaseGFM */
+    IBTFO_BOUNDARY_LINEAR_GFM = 2,  /* LinearBaseGFM */
+    IBTFO_BOUNDARY_RIEMANN_GFM = 3, /* RiemannBaseGFM (same algorithm as LinearBaseGFM) */
+    IBTFO_BOUNDARY_BCGFM = 4,
+    IBTFO_BOUNDARY_HBCGFM = 5
+};
+enum { IBTFO_GLOBAL_WALLS = 0, IBTFO_GLOBAL_PERIODIC = 1 };
+
+/* Case parameters: the numeric .inp keys the reference driver reads
+ * (Test/Sod/Sod.cpp:34-48) plus the slot selections. */
+typedef struct ibtfo_config {
+    int n_x, n_y, num_ghost_cell; /* num_ghost_cell >= 2 */
+    double lo_x, lo_y, hi_x, hi_y;
+    double gamma, cfl_number, psy_time;
+    int max_iter;
+    int scheme, riemann, limiter, boundary, global_boundary;
+    int reserved[8]; /* zero */
+} ibtfo_config;
+
+/* The reference time-loop scalars after the last completed step. */
+typedef struct ibtfo_progress {
+    int iter;       /* completed steps */
+    int status;     /* bit 0: a fluid cell holds NaN */
+    int nan_cells;  /* fluid cells with a NaN component, summed over steps */
+    int reserved;
+    double now_t;   /* loop time, advanced by the dt computed after each step (Sod.cpp:176) */
+    double dt;      /* dt the next step applies (ComputeDt of the current state) */
+    double mass;    /* CaculateMass of the current state */
+    double mass_start;
+} ibtfo_progress;
+
+typedef struct ibtfo_case ibtfo_case;
+
+int ibtfo_abi_version(void);
+const char *ibtfo_last_error(void);
+/* kernels launched by this library since load (graph replays counted per node) */
+long long ibtfo_launch_count(void);
+
+/* Creates a case on the current CUDA device.  Allocates the device state
+ * (two structure-of-arrays buffers, geometry, reduction scratch). */
+ibtfo_status ibtfo_create(const ibtfo_config *cfg, ibtfo_case **out);
+ibtfo_status ibtfo_destroy(ibtfo_case *c);
+/* Issue all work of this case on `stream` (a cudaStream_t); NULL selects the
+ * case's own stream. */
+ibtfo_status ibtfo_set_stream(ibtfo_case *c, void *stream);
+
+/* Psy_coord + Level_Set + Scheme_Index (Src/Geometry/Psy_coord.cpp:5-39,
+ * Level_Set.cpp:6-128, the Scheme_Index of each Src/BoundaryCondition variant) from the
+ * level set phi (M*N doubles). */
+ibtfo_status ibtfo_setup_geometry(ibtfo_case *c, const double *phi);
+/* XYCOORD in the reference layout (M*N*6 doubles). */
+ibtfo_status ibtfo_get_geometry(ibtfo_case *c, double *xycoord);
+/* SCHEME_IDX in the reference layout of the selected boundary variant
+ * (num_sch = 1, 4, 8 or 16 doubles per cell; see ibtfo_num_sch). */
+int ibtfo_num_sch(const ibtfo_case *c);
+ibtfo_status ibtfo_get_scheme_index(ibtfo_case *c, double *scheme_idx);
+/* number of ghost-fluid cells found by the set-up */
+int ibtfo_num_ghost_cells(const ibtfo_case *c);
+
+/* Initial state (M*N*4 doubles): Initialize sets U_OLD = U_NEW = u0, then the
+ * initial Boundary call, ComputeDt and CaculateMass
+ * (Test/InclineSod/InclineSod.cpp:103-128).  Resets the loop accounting. */
+ibtfo_status ibtfo_set_state(ibtfo_case *c, const double *u0);
+/* Current U_OLD and U_NEW in the reference layout; either pointer may be NULL.
+ * Waits for queued work. */
+ibtfo_status ibtfo_get_state(ibtfo_case *c, double *u_old, double *u_new);
+
+/* Replaces U_OLD (the current state, M*N*4 doubles) without touching the
+ * loop accounting, dt or U_NEW: the host-buffer round trip of a caller that
+ * keeps its own copy of the state between steps. */
+ibtfo_status ibtfo_put_state(ibtfo_case *c, const double *u_old);
+
+/* Queues `nsteps` iterations of the reference loop body (Sod.cpp:154-177:
+ * TimeAdvance, Boundary, Global_Boundary, ComputeDt, CaculateMass,
+ * now_t += dt) without waiting.  An iteration whose loop condition
+ * (now_t < psy_time && iter < max_iter) is false when it reaches the GPU does
+ * nothing. */
+ibtfo_status ibtfo_advance(ibtfo_case *c, int nsteps);
+/* The two launches of one guarded iteration, for callers that time or
+ * capture them separately: the fused sweep (Advance + ComputeDt +
+ * CaculateMass + loop accounting) and the boundary pass (ghost-fluid
+ * Boundary + Global_Boundary).  ibtfo_advance(c, 1) == sweep then boundary. */
+ibtfo_status ibtfo_enqueue_sweep(ibtfo_case *c);
+ibtfo_status ibtfo_enqueue_boundary(ibtfo_case *c);
+/* One iteration regardless of the loop condition; waits and reports. */
+ibtfo_status ibtfo_step(ibtfo_case *c, ibtfo_progress *p);
+/* Runs the loop to completion (now_t >= psy_time or iter >= max_iter).
+ * stop_on_nan != 0 returns IBTFO_ENAN as soon as a NaN appears. */
+ibtfo_status ibtfo_run(ibtfo_case *c, int stop_on_nan, ibtfo_progress *p);
+/* Waits for queued work and reports the loop scalars. */
+ibtfo_status ibtfo_get_progress(ibtfo_case *c, ibtfo_progress *p);
+ibtfo_status ibtfo_synchronize(ibtfo_case *c);
+
+/* Page-locked host memory for fast transfers (cudaHostAlloc / cudaFreeHost). */
+ibtfo_status ibtfo_host_alloc(size_t bytes, void **p);
+ibtfo_status ibtfo_host_free(void *p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,213 @@
+"""GPU parity: the CUDA path against the reference's own outputs (golden
+fixtures) and against the CPU oracle on the same seeded inputs.
+
+Tolerance (the bar for the plain FP64 path): relative L-infinity error
+<= 1e-12 per conserved variable after the fixture's steps, with NaN exactly
+where the reference has NaN; dt and mass sequences to 1e-12 relative.  The
+kernels evaluate the reference's expressions in the same order without
+fused multiply-adds, so most values agree to the last bit; square roots
+replace pow(x, 0.5), which can differ in the last bit.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from golden_util import load, names
+
+ib = pytest.importorskip("ibtfo_gb300")
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-12
+
+
+def rel_linf(a, b):
+    """max over conserved variables of max|a-b| / max|b| on cells where b is finite."""
+    a = np.asarray(a).reshape(-1, 4)
+    b = np.asarray(b).reshape(-1, 4)
+    worst = 0.0
+    for k in range(4):
+        m = np.isfinite(b[:, k])
+        if not m.any():
+            continue
+        scale = np.abs(b[m, k]).max()
+        if scale == 0:
+            scale = 1.0
+        worst = max(worst, float(np.abs(a[m, k] - b[m, k]).max() / scale))
+    return worst
+
+
+def assert_state_close(a, b, what, tol=RTOL):
+    a = np.asarray(a).reshape(-1, 4)
+    b = np.asarray(b).reshape(-1, 4)
+    fa, fb = np.isfinite(a), np.isfinite(b)
+    assert np.array_equal(fa, fb), f"{what}: non-finite pattern differs ({(fa != fb).sum()} values)"
+    same_nonfinite = np.array_equal(a[~fb], b[~fb], equal_nan=True)
+    assert same_nonfinite, f"{what}: inf/NaN values differ"
+    err = rel_linf(a, b)
+    assert err <= tol, f"{what}: relative L-inf {err:.3e} > {tol:.0e}"
+    return err
+
+
+def seq_close(a, b, tol=RTOL):
+    a, b = np.asarray(a, dtype=float), np.asarray(b, dtype=float)
+    if a.shape != b.shape:
+        return False
+    fa, fb = np.isfinite(a), np.isfinite(b)
+    if not np.array_equal(fa, fb):
+        return False
+    return np.allclose(a[fa], b[fb], rtol=tol, atol=0) and np.array_equal(a[~fa], b[~fb], equal_nan=True)
+
+
+def make_case(cfg):
+    return ib.Case(cfg["N_x"], cfg["N_y"], cfg["num_ghost_cell"], (cfg["lo_x"], cfg["lo_y"]),
+                   (cfg["hi_x"], cfg["hi_y"]), cfg["gamma"], cfg["CFL_number"], cfg["Psy_time"], cfg["max_iter"],
+                   cfg["scheme"], cfg["riemann"], cfg["limiter"], cfg["boundary"], cfg["gbc"])
+
+
+def run_steps(case, n):
+    dts, ms = [], []
+    for _ in range(n):
+        case.advance(1)
+        p = case.progress()
+        dts.append(p["dt"])
+        ms.append(p["mass"])
+    return np.array(dts), np.array(ms), case.progress()
+
+
+# fixtures where the PVRS Y-solver branch at PVRS/Riemann_solver.cpp:547-550
+# fires: its stray store lands in another cell's flux slot, which the GPU path
+# does not reproduce (the local effect of the branch is reproduced)
+PVRS_STRAY = {"quaddown_MUSCL_PVRS_minmod", "quaddown_MHM_PVRS_minmod"}
+
+
+@pytest.mark.parametrize("name", names())
+def test_gpu_matches_reference_fixture(name):
+    fx = load(name)
+    cfg = fx["config"]
+    if name in PVRS_STRAY:
+        pytest.xfail("PVRS :547-550 stray store into a remote flux slot is not reproduced")
+    with make_case(cfg) as c:
+        c.setup_geometry(fx["phi"])
+        if "xycoord" in fx:
+            assert np.array_equal(c.get_geometry(), fx["xycoord"]), "geometry differs"
+            assert np.array_equal(c.get_scheme_index(), fx["scheme_idx"], equal_nan=True), "SCHEME_IDX differs"
+        c.set_state(fx["u_init"])
+        p0 = c.progress()
+        assert seq_close([p0["dt"]], fx["dts"][:1]) and seq_close([p0["mass"]], fx["masses"][:1])
+        dts, ms, p = run_steps(c, fx["iters"])
+        assert p["iter"] == fx["iters"]
+        assert seq_close(dts, fx["dts"][1:]), "dt sequence differs"
+        assert seq_close(ms, fx["masses"][1:]), "mass sequence differs"
+        assert seq_close([p["now_t"]], [fx["now_t"]])
+        uo, un = c.get_state(u_new=True)
+        assert_state_close(uo, fx["u_old"], "U_OLD")
+        assert_state_close(un, fx["u_new"], "U_NEW")
+
+
+def oracle_case(w, **kw):
+    g = w.grid
+    return oracle.OracleCase(g.n_x, g.n_y, g.ng, (g.lo_x, g.lo_y), (g.hi_x, g.hi_y), w.gamma, w.cfl, w.scheme,
+                             w.riemann, w.limiter, w.boundary, w.gbc)
+
+
+@pytest.mark.parametrize("boundary", ["IDWBaseGFM", "LinearBaseGFM", "BCGFM", "HBCGFM"])
+def test_gpu_matches_oracle_inclined_channel(boundary):
+    """Inclined channel at 512x256 (the benchmark workload's geometry at a
+    quarter of its resolution), 20 steps, against the oracle."""
+    from ibtfo_gb300 import cases
+    w = cases.inclined_channel(512, 256, boundary)
+    oracle.set_threads(4)
+    phi = cases.channel_phi(w.grid)
+    o = oracle_case(w)
+    o.setup_geometry(phi)
+    types = o.get("XYCOORD").reshape(-1, 6)[:, 5]
+    u0 = cases.channel_init(w.grid, types, w.gamma)
+    o.set_initial_state(u0)
+    odts, oms = o.run(20)
+    with ib.Case.from_workload(w) as c:
+        c.setup_geometry(phi)
+        assert np.array_equal(c.get_geometry(), o.get("XYCOORD"))
+        c.set_state(u0)
+        dts, ms, p = run_steps(c, 20)
+        assert seq_close(dts, odts) and seq_close(ms, oms)
+        uo, un = c.get_state(u_new=True)
+        assert_state_close(uo, o.get("U_OLD"), "U_OLD")
+        assert_state_close(un, o.get("U_NEW"), "U_NEW")
+
+
+def test_advance_queue_equals_single_steps():
+    """ibtfo_advance(n) (CUDA-graph replays + loop guard on the device) gives
+    the same bytes as n separate steps."""
+    from ibtfo_gb300 import cases
+    w = cases.inclined_channel(256, 128)
+    phi = cases.channel_phi(w.grid)
+    res = []
+    for mode in ("queue", "single"):
+        with ib.Case.from_workload(w) as c:
+            c.setup_geometry(phi)
+            u0 = cases.channel_init(w.grid, c.cell_types(), w.gamma)
+            c.set_state(u0)
+            if mode == "queue":
+                c.advance(37)
+            else:
+                for _ in range(37):
+                    c.advance(1)
+            res.append((c.get_state(), c.progress()))
+    assert np.array_equal(res[0][0], res[1][0])
+    assert res[0][1] == res[1][1]
+
+
+def test_loop_guard_stops_at_t_end():
+    """Queued iterations past now_t >= t_end do nothing (Test/Sod/Sod.cpp:123)."""
+    from ibtfo_gb300 import cases
+    w = cases.sod_tube(80, 20)
+    g = w.grid
+    phi, u0 = cases.sod_x(g)
+    o = oracle_case(w)
+    o.setup_geometry(phi)
+    o.set_initial_state(u0)
+    odts, _ = o.run(10 ** 6, w.t_end)
+    with ib.Case.from_workload(w) as c:
+        c.setup_geometry(phi)
+        c.set_state(u0)
+        c.advance(len(odts) + 50)
+        p = c.progress()
+        assert p["iter"] == len(odts)
+        assert seq_close([p["now_t"]], [o.scalars()["now_t"]])
+        assert_state_close(c.get_state(), o.get("U_OLD"), "U_OLD at t_end")
+
+
+def test_run_to_t_end_sod_tube_l1():
+    """Sod tube 400x100 to t_end = 0.2: L1 density error <= 1e-10 vs the oracle."""
+    from ibtfo_gb300 import cases
+    w = cases.sod_tube()
+    phi, u0 = cases.sod_x(w.grid)
+    oracle.set_threads(4)
+    o = oracle_case(w)
+    o.setup_geometry(phi)
+    o.set_initial_state(u0)
+    o.run(10 ** 6, w.t_end)
+    with ib.Case.from_workload(w) as c:
+        c.setup_geometry(phi)
+        c.set_state(u0)
+        p = c.run()
+        assert p["iter"] == o.scalars()["iter"]
+        a = c.get_state().reshape(-1, 4)[:, 0]
+        b = o.get("U_OLD").reshape(-1, 4)[:, 0]
+        l1 = np.abs(a - b).sum() / np.abs(b).sum()
+        assert l1 <= 1e-10, l1
+
+
+def test_deterministic_repeat():
+    from ibtfo_gb300 import cases
+    w = cases.inclined_channel(384, 192)
+    phi = cases.channel_phi(w.grid)
+    outs = []
+    for _ in range(2):
+        with ib.Case.from_workload(w) as c:
+            c.setup_geometry(phi)
+            c.set_state(cases.channel_init(w.grid, c.cell_types(), w.gamma))
+            c.advance(25)
+            outs.append((c.get_state(), c.progress()["mass"]))
+    assert np.array_equal(outs[0][0], outs[1][0]) and outs[0][1] == outs[1][1]
