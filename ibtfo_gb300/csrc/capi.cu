@@ -75,6 +75,8 @@ struct ibtfo_case
     DevState *st = nullptr;
     double *partial = nullptr;
     double *ring_ic = nullptr; // [2][2*ng][4]
+    unsigned *tiles = nullptr; // active sweep tiles
+    int ntiles = 0;
     int nblocks = 0;
     bool geometry = false, state = false;
     SweepLaunch sweep = nullptr;
@@ -122,6 +124,7 @@ ibtfo_status ibtfo_destroy(ibtfo_case *c)
     cudaFree(c->st);
     cudaFree(c->partial);
     cudaFree(c->ring_ic);
+    cudaFree(c->tiles);
     if (c->own)
         cudaStreamDestroy(c->own);
     delete c;
@@ -237,10 +240,18 @@ ibtfo_status ibtfo_setup_geometry(ibtfo_case *c, const double *phi)
         c->nghost = 0;
     }
     int rc = setup_geometry(g, c->cfg.boundary, c->phi, c->nx, c->ny, c->type, &c->ghosts, &c->nghost, c->stream);
+    if (rc == 0)
+        rc = active_tiles(g, c->type, &c->tiles, &c->ntiles, c->stream);
     if (rc == 2)
-        return fail(IBTFO_ENOMEM, "ghost list allocation failed");
+        return fail(IBTFO_ENOMEM, "geometry allocation failed");
     if (rc != 0)
         return cuda_fail(cudaGetLastError(), "geometry set-up");
+    if (c->graph)
+    {
+        cudaGraphExecDestroy(c->graph);
+        c->graph = nullptr;
+        c->graph_steps = 0;
+    }
     CK(cudaStreamSynchronize(c->stream));
     c->geometry = true;
     c->state = false;
@@ -340,6 +351,7 @@ static SweepArgs sweep_args(ibtfo_case *c, int guard)
     a.type = c->type;
     a.st = c->st;
     a.partial = c->partial;
+    a.tiles = c->tiles;
     a.t_end = c->cfg.psy_time;
     a.max_iter = c->cfg.max_iter;
     a.guard = guard;
@@ -371,9 +383,7 @@ static void enqueue_boundary(ibtfo_case *c)
 
 static void enqueue_step(ibtfo_case *c, int guard)
 {
-    const GridDesc &g = c->g;
-    dim3 grid((g.n_x + TILE_X - 1) / TILE_X, (g.n_y + TILE_Y - 1) / TILE_Y);
-    c->sweep(sweep_args(c, guard), grid, dim3(TILE_X * TILE_Y), c->stream);
+    c->sweep(sweep_args(c, guard), dim3(c->ntiles), dim3(TILE_X * TILE_Y), c->stream);
     count_launch();
     enqueue_boundary(c);
 }
@@ -587,9 +597,7 @@ ibtfo_status ibtfo_enqueue_sweep(ibtfo_case *c)
     if (!c->state)
         return fail(IBTFO_ESTATE, "no state: call ibtfo_set_state first");
     cudaSetDevice(c->device);
-    const GridDesc &g = c->g;
-    dim3 grid((g.n_x + TILE_X - 1) / TILE_X, (g.n_y + TILE_Y - 1) / TILE_Y);
-    c->sweep(sweep_args(c, 1), grid, dim3(TILE_X * TILE_Y), c->stream);
+    c->sweep(sweep_args(c, 1), dim3(c->ntiles), dim3(TILE_X * TILE_Y), c->stream);
     count_launch();
     CK(cudaGetLastError());
     return IBTFO_OK;

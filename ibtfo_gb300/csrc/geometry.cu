@@ -246,6 +246,58 @@ __global__ void scheme_index_kernel(GridDesc g, int bc, const double *__restrict
 
 static inline unsigned nblk(long long n, int b) { return (unsigned)((n + b - 1) / b); }
 
+// one flag per sweep tile: does it hold an interior fluid cell?
+__global__ void tile_flags_kernel(GridDesc g, const uint8_t *__restrict__ type, int ntx, int nty, uint8_t *flags)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntx * nty)
+        return;
+    int bx = t % ntx, by = t / ntx;
+    int i0 = g.ng + bx * TILE_X, j0 = g.ng + by * TILE_Y;
+    uint8_t f = 0;
+    for (int j = j0; j < j0 + TILE_Y && j < g.ng + g.n_y && !f; j++)
+        for (int i = i0; i < i0 + TILE_X && i < g.ng + g.n_x; i++)
+            if (type[(long long)j * g.pitch + i] == 0)
+            {
+                f = 1;
+                break;
+            }
+    flags[t] = f;
+}
+
+int active_tiles(const GridDesc &g, const uint8_t *d_type, unsigned **d_tiles, int *ntiles, cudaStream_t s)
+{
+    const int ntx = (g.n_x + TILE_X - 1) / TILE_X, nty = (g.n_y + TILE_Y - 1) / TILE_Y;
+    const int n = ntx * nty;
+    uint8_t *d_flags = nullptr;
+    if (cudaMalloc(&d_flags, n) != cudaSuccess)
+        return 2;
+    tile_flags_kernel<<<nblk(n, 256), 256, 0, s>>>(g, d_type, ntx, nty, d_flags);
+    count_launch();
+    std::vector<uint8_t> flags(n);
+    cudaError_t e = cudaMemcpyAsync(flags.data(), d_flags, n, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(s);
+    cudaFree(d_flags);
+    if (e != cudaSuccess)
+        return 5;
+    std::vector<unsigned> list;
+    for (int t = 0; t < n; t++)
+        if (flags[t])
+            list.push_back((unsigned)(t % ntx) | ((unsigned)(t / ntx) << 16));
+    if (list.empty())
+        list.push_back(0u); // a tile without fluid still runs the loop accounting
+    if (*d_tiles)
+        cudaFree(*d_tiles);
+    *d_tiles = nullptr;
+    if (cudaMalloc(d_tiles, sizeof(unsigned) * list.size()) != cudaSuccess)
+        return 2;
+    if (cudaMemcpy(*d_tiles, list.data(), sizeof(unsigned) * list.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+        return 5;
+    *ntiles = (int)list.size();
+    return 0;
+}
+
 int setup_geometry(const GridDesc &g, int bc, const double *d_phi, double *d_nx, double *d_ny, uint8_t *d_type,
                    GhostRec **d_ghosts, int *nghost, cudaStream_t s)
 {

@@ -67,6 +67,7 @@ struct SweepArgs
     const uint8_t *type;     // cell type plane (uint8, same pitch)
     DevState *st;
     double *partial;         // one mass partial per block
+    const unsigned *tiles;   // active tiles (bx | by << 16): tiles holding at least one fluid cell
     double t_end;
     int max_iter;
     int guard;               // apply the reference loop condition before stepping
@@ -111,6 +112,7 @@ void launch_aos_to_soa(const double *aos, double *soa, const GridDesc &g, cudaSt
 void launch_soa_to_aos(const double *soa, double *aos, const GridDesc &g, cudaStream_t s);
 
 // geometry set-up (geometry.cu)
+int active_tiles(const GridDesc &g, const uint8_t *d_type, unsigned **d_tiles, int *ntiles, cudaStream_t s);
 int setup_geometry(const GridDesc &g, int bc, const double *d_phi, double *d_nx, double *d_ny, uint8_t *d_type,
                    GhostRec **d_ghosts, int *nghost, cudaStream_t s);
 

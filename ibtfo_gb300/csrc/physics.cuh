@@ -20,10 +20,16 @@ enum Limiter { MINMOD = 0, VANLEER = 1 };
 // pow(x, 0.5): +0 for a zero of either sign (as pow gives), sqrt otherwise
 __device__ __forceinline__ double pow_half(double x) { return (x == 0.0) ? 0.0 : sqrt(x); }
 
-// Src/Base/Slope_limiter/minmod/Slope_limiter.H:4
+// Src/Base/Slope_limiter/minmod/Slope_limiter.H:4:
+//   ((a*b) > 0) ? ((a/b > 1) ? b : a) : 0
+// Where a*b > 0 (a, b non-zero, same sign), the rounded quotient a/b exceeds
+// 1 exactly when |a| > |b|: for doubles |a| > |b| implies
+// |a|/|b| >= 1 + ulp(b)/|b| > 1 + 2^-53, which rounds above 1, and
+// |a| <= |b| gives a quotient <= 1.  The comparison replaces the division
+// with the same result, infinities included.
 __device__ __forceinline__ double lim_minmod(double a, double b)
 {
-    return ((a * b) > 0) ? ((a / b > 1) ? b : a) : 0.0;
+    return ((a * b) > 0) ? ((fabs(a) > fabs(b)) ? b : a) : 0.0;
 }
 
 // Src/Base/Slope_limiter/VanLeer/Slope_limiter.H:4 as the macro expands at its

@@ -168,8 +168,12 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_kernel(const SweepArgs a
     double *__restrict__ V = cur ? a.buf0 : a.buf1;
     const long long P = g.plane;
     const int pitch = g.pitch;
-    const int i0 = g.ng + blockIdx.x * TX;
-    const int j0 = g.ng + blockIdx.y * TY;
+    // tiles without fluid cells are skipped: nothing in them is updated or
+    // counted by the reference (updates, ComputeDt and CaculateMass all test
+    // the cell type), so the launch covers the active tiles only
+    const unsigned tile = a.tiles[blockIdx.x];
+    const int i0 = g.ng + (int)(tile & 0xFFFFu) * TX;
+    const int j0 = g.ng + (int)(tile >> 16) * TY;
     const int tid = threadIdx.x;
 
     // stage the tile and its halo (always inside the padded array: ng >= 2)
