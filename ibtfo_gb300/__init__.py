@@ -77,6 +77,8 @@ SIGNATURES = {
     "ibtfo_run": (C.c_int, [_P, C.c_int, C.POINTER(Progress)]),
     "ibtfo_get_progress": (C.c_int, [_P, C.POINTER(Progress)]),
     "ibtfo_synchronize": (C.c_int, [_P]),
+    "ibtfo_dt_mass_noalloc": (C.c_int, [_P, C.c_longlong, C.c_int, _P, C.c_int, C.c_int, C.c_int, C.c_double,
+                                        C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, _P, _P]),
     "ibtfo_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(_P)]),
     "ibtfo_host_free": (C.c_int, [_P]),
 }

@@ -51,6 +51,10 @@ static ibtfo_status cuda_fail(cudaError_t e, const char *what)
     return fail(IBTFO_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+namespace ibtfo {
+void set_last_error(const char *msg) { g_err = msg; }
+} // namespace ibtfo
+
 #define CK(call)                                      \
     do                                                \
     {                                                 \

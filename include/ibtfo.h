@@ -135,6 +135,30 @@ ibtfo_status ibtfo_run(ibtfo_case *c, int stop_on_nan, ibtfo_progress *p);
 ibtfo_status ibtfo_get_progress(ibtfo_case *c, ibtfo_progress *p);
 ibtfo_status ibtfo_synchronize(ibtfo_case *c);
 
+/* CFL time step and fluid mass of a device-resident state, allocating
+ * nothing.  No counterpart in the reference: it serves callers that cannot
+ * call cudaMalloc -- code running inside a framework that owns all device
+ * memory through its own pool, or that must not let an allocation
+ * synchronise the device between its kernels -- and that already hold the
+ * state on the GPU.
+ *   d_u      four planes (rho, rho u, rho v, E), `plane` doubles apart, rows
+ *            `pitch` doubles long (pitch >= N_x + 2 ng), index j*pitch + i
+ *   d_type   cell types (0 fluid, 1 solid, 2 ghost), uint8, same pitch
+ *   d_out    two doubles on the device: dt = CFL dx / (max a + max(max|u|,
+ *            max|v|)) and mass = sum rho dx dy, both over fluid interior cells
+ * The work is queued on `stream` (a cudaStream_t, NULL for the default
+ * stream) and the call returns without waiting.  Scratch is a fixed array
+ * inside the library (512 KiB per GPU, held by every GPU that loads the
+ * library until the process exits), so grids above 65536 tiles of 32 x 8
+ * interior cells (e.g. 4096 x 4096) are rejected with IBTFO_EINVAL.  The
+ * first call on a device looks up that array's device address: make that
+ * first call before any stream capture.  Every call shares the one array and
+ * it keeps the last call's contents: calls that overlap on the GPU (other
+ * streams, other threads) race and give wrong results. */
+ibtfo_status ibtfo_dt_mass_noalloc(const double *d_u, long long plane, int pitch, const unsigned char *d_type,
+                                   int n_x, int n_y, int num_ghost_cell, double lo_x, double lo_y, double hi_x,
+                                   double hi_y, double gamma, double cfl_number, double *d_out, void *stream);
+
 /* Page-locked host memory for fast transfers (cudaHostAlloc / cudaFreeHost). */
 ibtfo_status ibtfo_host_alloc(size_t bytes, void **p);
 ibtfo_status ibtfo_host_free(void *p);
