@@ -46,11 +46,14 @@ def workload():
     return cases.inclined_channel(2048, 1024)
 
 
+PRECISION = os.environ.get("IBTFO_BENCH_PRECISION", "fp64_fast")
+
+
 def config_json(w, l2="flushed between timed steps (256 MiB write)"):
     g = w.grid
     return {"workload": w.name, "n_x": g.n_x, "n_y": g.n_y, "domain": [g.lo_x, g.lo_y, g.hi_x, g.hi_y],
             "scheme": w.scheme, "riemann": w.riemann, "limiter": w.limiter, "boundary": w.boundary,
-            "cfl": w.cfl, "gamma": w.gamma, "precision": "fp64", "l2": l2}
+            "cfl": w.cfl, "gamma": w.gamma, "precision": PRECISION, "l2": l2}
 
 
 def measured_peaks():
@@ -164,7 +167,7 @@ def cpu_oracle_rate(w, steps=None, warmup=1, budget_s=15.0):
 
 
 # ------------------------------------------------------------------ GPU leg
-def gpu_arm(args, rank, world, local_rank):
+def gpu_arm(args, rank, world, local_rank, precision=None, e2e=True):
     import torch
     import ibtfo_gb300 as ib
     from ibtfo_gb300 import cases
@@ -174,7 +177,7 @@ def gpu_arm(args, rank, world, local_rank):
     g = w.grid
     cells = g.n_x * g.n_y
     stream = torch.cuda.Stream()
-    c = ib.Case.from_workload(w, t_end=1e300, max_iter=2 ** 31 - 1)
+    c = ib.Case.from_workload(w, t_end=1e300, max_iter=2 ** 31 - 1, precision=precision or PRECISION)
     c.set_stream(stream.cuda_stream)
     phi = cases.channel_phi(g)
     c.setup_geometry(phi)
@@ -211,7 +214,7 @@ def gpu_arm(args, rank, world, local_rank):
     prog = c.progress()
 
     # end to end through the C ABI with host buffers (pinned)
-    e2e_steps = max(1, min(args.steps, 20))
+    e2e_steps = max(1, min(args.steps, 20)) if e2e else 1
     pin = ib.PinnedBuffer(g.M * g.N * 4)
     c.get_state_ptr(pin.ptr)
     torch.cuda.synchronize()
@@ -238,8 +241,8 @@ def gpu_arm(args, rank, world, local_rank):
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -278,6 +281,9 @@ def main():
                "sample": f"1 warm-up + {n} timed steps of the full {g.n_x}x{g.n_y} grid, OpenMP over {cores} threads"}
 
     r = gpu_arm(args, rank, world, local_rank)
+    # the other FP64 precision, timed the same way (steps only), for comparison
+    other = "fp64" if PRECISION == "fp64_fast" else "fp64_fast"
+    r2 = gpu_arm(args, rank, world, local_rank, precision=other, e2e=False)
     if world > 1:
         import torch
         torch.distributed.destroy_process_group()
@@ -302,6 +308,8 @@ def main():
             "e2e": {"value": e2e_val, "unit": METRIC, "h2d_bytes_per_step": state_bytes,
                     "d2h_bytes_per_step": state_bytes + 48, "steps": r["e2e_steps"]},
             "gpu_launches": r["launches"], "clocks": r["clocks"],
+            "other_precision": {"precision": other, "value": world * cells * K / (r2["step_ms"] * 1e-3) / 1e9,
+                                "unit": METRIC, "sweep_ms": r2["sweep_ms"] / K},
             "final": {"iter": r["progress"]["iter"], "nan_cells": r["progress"]["nan_cells"]}}
     print(json.dumps(line), flush=True)
     return 0

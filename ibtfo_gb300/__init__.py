@@ -26,6 +26,7 @@ RIEMANNS = {"HLL": 0, "HLLC": 1, "PVRS": 2, "StegerWarming": 3}
 LIMITERS = {"minmod": 0, "VanLeer": 1}
 BOUNDARIES = {"Regular": 0, "IDWBaseGFM": 1, "LinearBaseGFM": 2, "RiemannBaseGFM": 3, "BCGFM": 4, "HBCGFM": 5}
 GLOBAL_BCS = {"walls": 0, "periodic": 1}
+PRECISIONS = {"fp64": 0, "fp64_fast": 1}
 
 STATUS = {0: "OK", 1: "EINVAL", 2: "ENOMEM", 3: "ENAN", 4: "ETIMEOUT", 5: "ECUDA", 6: "ESTATE"}
 
@@ -41,7 +42,8 @@ class Config(C.Structure):
                 ("lo_x", C.c_double), ("lo_y", C.c_double), ("hi_x", C.c_double), ("hi_y", C.c_double),
                 ("gamma", C.c_double), ("cfl_number", C.c_double), ("psy_time", C.c_double),
                 ("max_iter", C.c_int), ("scheme", C.c_int), ("riemann", C.c_int), ("limiter", C.c_int),
-                ("boundary", C.c_int), ("global_boundary", C.c_int), ("reserved", C.c_int * 8)]
+                ("boundary", C.c_int), ("global_boundary", C.c_int), ("precision", C.c_int),
+                ("reserved", C.c_int * 7)]
 
 
 class Progress(C.Structure):
@@ -119,10 +121,11 @@ class Case:
 
     def __init__(self, n_x, n_y, ng=2, lo=(0.0, 0.0), hi=(1.0, 1.0), gamma=1.4, cfl=0.5, t_end=1.0,
                  max_iter=100000, scheme="MUSCL", riemann="HLL", limiter="minmod", boundary="Regular",
-                 gbc="walls"):
+                 gbc="walls", precision="fp64"):
         L = lib()
         cfg = Config(n_x, n_y, ng, lo[0], lo[1], hi[0], hi[1], gamma, cfl, t_end, max_iter,
-                     SCHEMES[scheme], RIEMANNS[riemann], LIMITERS[limiter], BOUNDARIES[boundary], GLOBAL_BCS[gbc])
+                     SCHEMES[scheme], RIEMANNS[riemann], LIMITERS[limiter], BOUNDARIES[boundary], GLOBAL_BCS[gbc],
+                     PRECISIONS[precision])
         h = _P()
         _check(L.ibtfo_create(C.byref(cfg), C.byref(h)))
         self.h = h

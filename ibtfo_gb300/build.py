@@ -3,9 +3,11 @@ for sm_103a into ibtfo_gb300/libibtfo_gb300.so (in-tree, git-ignored).
 
     python -m ibtfo_gb300.build [--jobs N] [--force]
 
-Translation units compile in parallel; host code is compiled without
-floating-point contraction so that coordinates and other host-side values
-match the reference bit for bit on every host architecture.
+Translation units compile in parallel.  Device code is compiled without
+floating-point contraction (the reference's expressions evaluate to the same
+binary64 values) except in the *_fast.cu units of the fp64_fast precision;
+host code is compiled without contraction so that coordinates and other
+host-side values match the reference bit for bit on every host architecture.
 """
 from __future__ import annotations
 
@@ -57,7 +59,10 @@ def build(force: bool = False, jobs: int | None = None, verbose: bool = False) -
 
     def compile_one(so):
         s, o = so
-        cmd = [nv] + NVFLAGS + ["-c", s, "-o", o]
+        flags = list(NVFLAGS)
+        if os.path.basename(s).endswith("_fast.cu"):
+            flags[flags.index("-fmad=false")] = "-fmad=true"  # fp64_fast units contract multiply-adds
+        cmd = [nv] + flags + ["-c", s, "-o", o]
         if s.endswith(".cpp"):
             cmd = [nv, "-x", "cu"] + NVFLAGS + ["-c", s, "-o", o]
         p = subprocess.run(cmd, capture_output=True, text=True)

@@ -20,15 +20,19 @@ namespace ibtfo {
 SweepLaunch sweep_launcher_muscl(int riemann, int limiter);
 SweepLaunch sweep_launcher_mhm(int riemann, int limiter);
 SweepLaunch sweep_launcher_godunov(int riemann, int limiter);
+SweepLaunch sweep_launcher_muscl_fast(int riemann, int limiter);
+SweepLaunch sweep_launcher_mhm_fast(int riemann, int limiter);
+SweepLaunch sweep_launcher_godunov_fast(int riemann, int limiter);
 
-SweepLaunch sweep_launcher(int scheme, int riemann, int limiter)
+SweepLaunch sweep_launcher(int scheme, int riemann, int limiter, int precision)
 {
     const int r = (riemann == HLLC) ? HLL : riemann; // HLLC/Riemann_solver.cpp is HLL
+    const bool fast = (precision == IBTFO_PRECISION_FP64_FAST);
     switch (scheme)
     {
-    case MHM: return sweep_launcher_mhm(r, limiter);
-    case GODUNOV: return sweep_launcher_godunov(r, limiter);
-    default: return sweep_launcher_muscl(r, limiter);
+    case MHM: return fast ? sweep_launcher_mhm_fast(r, limiter) : sweep_launcher_mhm(r, limiter);
+    case GODUNOV: return fast ? sweep_launcher_godunov_fast(r, limiter) : sweep_launcher_godunov(r, limiter);
+    default: return fast ? sweep_launcher_muscl_fast(r, limiter) : sweep_launcher_muscl(r, limiter);
     }
 }
 
@@ -148,8 +152,9 @@ ibtfo_status ibtfo_create(const ibtfo_config *cfg, ibtfo_case **out)
     if (!(k.hi_x > k.lo_x) || !(k.hi_y > k.lo_y) || !(k.gamma > 1.0) || !(k.cfl_number > 0.0))
         return fail(IBTFO_EINVAL, "need hi > lo, gamma > 1, cfl_number > 0");
     if (k.scheme < 0 || k.scheme > 2 || k.riemann < 0 || k.riemann > 3 || k.limiter < 0 || k.limiter > 1 ||
-        k.boundary < 0 || k.boundary > 5 || k.global_boundary < 0 || k.global_boundary > 1)
-        return fail(IBTFO_EINVAL, "unknown scheme/riemann/limiter/boundary/global_boundary key");
+        k.boundary < 0 || k.boundary > 5 || k.global_boundary < 0 || k.global_boundary > 1 || k.precision < 0 ||
+        k.precision > 1)
+        return fail(IBTFO_EINVAL, "unknown scheme/riemann/limiter/boundary/global_boundary/precision key");
     if (k.global_boundary == IBTFO_GLOBAL_PERIODIC && (k.n_x < k.num_ghost_cell || k.n_y < k.num_ghost_cell))
         return fail(IBTFO_EINVAL, "periodic boundaries need n_x, n_y >= num_ghost_cell");
 
@@ -172,7 +177,7 @@ ibtfo_status ibtfo_create(const ibtfo_config *cfg, ibtfo_case **out)
     g.gamma = k.gamma;
     g.cfl = k.cfl_number;
     c->nblocks = ((k.n_x + TILE_X - 1) / TILE_X) * ((k.n_y + TILE_Y - 1) / TILE_Y);
-    c->sweep = sweep_launcher(k.scheme, k.riemann, k.limiter);
+    c->sweep = sweep_launcher(k.scheme, k.riemann, k.limiter, k.precision);
 
     const size_t cells = (size_t)g.M * g.N;
     const size_t plane_bytes = sizeof(double) * (size_t)g.plane;

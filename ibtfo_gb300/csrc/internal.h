@@ -105,7 +105,7 @@ typedef void (*SweepLaunch)(const SweepArgs &, dim3 grid, dim3 block, cudaStream
 constexpr int TILE_X = 32;
 constexpr int TILE_Y = 8;
 
-SweepLaunch sweep_launcher(int scheme, int riemann, int limiter);
+SweepLaunch sweep_launcher(int scheme, int riemann, int limiter, int precision);
 void launch_fill(const FillArgs &a, cudaStream_t s);
 void launch_reduce(const ReduceArgs &a, int nblocks_max, cudaStream_t s);
 void launch_aos_to_soa(const double *aos, double *soa, const GridDesc &g, cudaStream_t s);

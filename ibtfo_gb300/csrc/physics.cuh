@@ -22,14 +22,27 @@ __device__ __forceinline__ double pow_half(double x) { return (x == 0.0) ? 0.0 :
 
 // Src/Base/Slope_limiter/minmod/Slope_limiter.H:4:
 //   ((a*b) > 0) ? ((a/b > 1) ? b : a) : 0
-// Where a*b > 0 (a, b non-zero, same sign), the rounded quotient a/b exceeds
-// 1 exactly when |a| > |b|: for doubles |a| > |b| implies
-// |a|/|b| >= 1 + ulp(b)/|b| > 1 + 2^-53, which rounds above 1, and
-// |a| <= |b| gives a quotient <= 1.  The comparison replaces the division
-// with the same result, infinities included.
+// evaluated on the integer pipe with the same result:
+// * a*b > 0 holds when a and b are non-zero, not NaN, of the same sign, and
+//   the product does not underflow to zero; for biased exponents
+//   ea + eb >= 972 (both normal) |a*b| >= 2^-1074 cannot underflow, below
+//   that the product itself is evaluated;
+// * where a*b > 0, the rounded quotient a/b exceeds 1 exactly when |a| > |b|:
+//   for doubles |a| > |b| implies |a|/|b| >= 1 + ulp(b)/|b| > 1 + 2^-53,
+//   which rounds above 1, and |a| <= |b| gives a quotient <= 1; magnitudes of
+//   non-NaN doubles order like their bit patterns.
 __device__ __forceinline__ double lim_minmod(double a, double b)
 {
-    return ((a * b) > 0) ? ((fabs(a) > fabs(b)) ? b : a) : 0.0;
+    const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+    const long long ma = ia & 0x7fffffffffffffffLL, mb = ib & 0x7fffffffffffffffLL;
+    bool pos = ((ia ^ ib) >= 0) && ma != 0 && mb != 0 && ma <= 0x7ff0000000000000LL && mb <= 0x7ff0000000000000LL;
+    if (pos)
+    {
+        const int ea = (int)(ma >> 52), eb = (int)(mb >> 52);
+        if (!(ea != 0 && eb != 0 && ea + eb >= 972))
+            pos = (a * b) > 0;
+    }
+    return pos ? ((ma > mb) ? b : a) : 0.0;
 }
 
 // Src/Base/Slope_limiter/VanLeer/Slope_limiter.H:4 as the macro expands at its

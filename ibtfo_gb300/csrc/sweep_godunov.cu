@@ -1,5 +1,5 @@
-// Instantiations of the fused sweep for Scheme=GODUNOV (one translation unit per
-// scheme so the library builds in parallel).
+// Instantiations of the fused sweep for Scheme=GODUNOV, strict FP64 (compiled without contraction).
+// One translation unit per scheme and precision so the library builds in parallel.
 #include "sweep_impl.cuh"
 
 namespace ibtfo {
@@ -9,9 +9,9 @@ SweepLaunch sweep_launcher_godunov(int riemann, int limiter)
     const bool vl = (limiter == VANLEER);
     switch (riemann)
     {
-    case PVRS: return vl ? &launch_sweep<GODUNOV, PVRS, VANLEER> : &launch_sweep<GODUNOV, PVRS, MINMOD>;
-    case SW: return vl ? &launch_sweep<GODUNOV, SW, VANLEER> : &launch_sweep<GODUNOV, SW, MINMOD>;
-    default: return vl ? &launch_sweep<GODUNOV, HLL, VANLEER> : &launch_sweep<GODUNOV, HLL, MINMOD>;
+    case PVRS: return vl ? &launch_sweep<GODUNOV, PVRS, VANLEER, 0> : &launch_sweep<GODUNOV, PVRS, MINMOD, 0>;
+    case SW: return vl ? &launch_sweep<GODUNOV, SW, VANLEER, 0> : &launch_sweep<GODUNOV, SW, MINMOD, 0>;
+    default: return vl ? &launch_sweep<GODUNOV, HLL, VANLEER, 0> : &launch_sweep<GODUNOV, HLL, MINMOD, 0>;
     }
 }
 

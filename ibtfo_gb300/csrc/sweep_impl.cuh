@@ -16,6 +16,7 @@
 
 #include "internal.h"
 #include "physics.cuh"
+#include "physics_fast.cuh"
 
 namespace ibtfo {
 
@@ -145,7 +146,22 @@ __device__ __forceinline__ void cell_stats(const double v[4], double gam, double
     nans += (isnan(v[0]) || isnan(v[1]) || isnan(v[2]) || isnan(v[3])) ? 1 : 0;
 }
 
-template <int SCH, int RIE, int LIM>
+// the same statistics with a shared reciprocal (fp64_fast)
+__device__ __forceinline__ void cell_stats_fast(const double v[4], const GasConst &K, double dxdy, double &amax,
+                                                double &umax, double &vmax, double &mass, int &nans)
+{
+    const double ir = rcp_nr(v[0]);
+    const double u = v[1] * ir, w = v[2] * ir;
+    const double p = K.gm1 * (v[3] - 0.5 * v[0] * (u * u + w * w));
+    const double a = pow_half(K.g * p * ir);
+    amax = fmax(amax, a);
+    umax = fmax(umax, fabs(u));
+    vmax = fmax(vmax, fabs(w));
+    mass += v[0] * dxdy;
+    nans += (isnan(v[0]) || isnan(v[1]) || isnan(v[2]) || isnan(v[3])) ? 1 : 0;
+}
+
+template <int SCH, int RIE, int LIM, int FAST>
 __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_kernel(const SweepArgs a)
 {
     constexpr int TX = TILE_X, TY = TILE_Y, NT = TX * TY;
@@ -191,6 +207,8 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_kernel(const SweepArgs a
     __syncthreads();
 
     const double gam = g.gamma;
+    const GasConst K(gam);
+    const double hx2 = 0.5 * dt / g.dx, hy2 = 0.5 * dt / g.dy; // fp64_fast MHM predictor
     constexpr int NXF = (TX + 1) * (TY + 1);
     constexpr int NYF = TX * (TY + 1);
     for (int q = tid; q < NXF + NYF; q += NT)
@@ -207,7 +225,10 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_kernel(const SweepArgs a
                 c2[k] = sU[k][r + 1][fc + 2];
                 c3[k] = sU[k][r + 1][fc + 3];
             }
-            x_face<SCH, RIE, LIM>(c0, c1, c2, c3, gam, dt, g.dx, f);
+            if (FAST)
+                x_face_fast<SCH, RIE, LIM>(c0, c1, c2, c3, K, dt, hx2, f);
+            else
+                x_face<SCH, RIE, LIM>(c0, c1, c2, c3, gam, dt, g.dx, f);
 #pragma unroll
             for (int k = 0; k < 4; k++)
                 sF[k][r][fc] = f[k];
@@ -225,7 +246,8 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_kernel(const SweepArgs a
                 c3[k] = sU[k][r + 3][c + 2];
             }
             double stray = 0.0;
-            int keep = y_face<SCH, RIE, LIM>(c0, c1, c2, c3, gam, dt, g.dy, f, &stray);
+            int keep = FAST ? y_face_fast<SCH, RIE, LIM>(c0, c1, c2, c3, K, dt, hy2, f, &stray)
+                            : y_face<SCH, RIE, LIM>(c0, c1, c2, c3, gam, dt, g.dy, f, &stray);
 #pragma unroll
             for (int k = 0; k < 4; k++)
                 sG[k][r][c] = f[k];
@@ -243,26 +265,38 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_kernel(const SweepArgs a
         if (i < g.ng + g.n_x && j < g.ng + g.n_y && a.type[(long long)j * pitch + i] == 0)
         {
             const int kp = sKeep[r + 1][c], km = sKeep[r][c];
+            const double lx = dt / g.dx, ly = dt / g.dy;
             double v[4];
 #pragma unroll
             for (int k = 0; k < 4; k++)
             {
-                double x = sU[k][r + 2][c + 2] - dt * (sF[k][r + 1][c + 1] - sF[k][r + 1][c]) / g.dx;
                 double gp = ((kp >> k) & 1) ? sF[k][r + 1][c + 1] : sG[k][r + 1][c];
                 double gm = ((km >> k) & 1) ? sF[k][r][c + 1] : sG[k][r][c];
-                v[k] = x - dt * (gp - gm) / g.dy;
+                if (FAST)
+                {
+                    double x = sU[k][r + 2][c + 2] - lx * (sF[k][r + 1][c + 1] - sF[k][r + 1][c]);
+                    v[k] = x - ly * (gp - gm);
+                }
+                else
+                {
+                    double x = sU[k][r + 2][c + 2] - dt * (sF[k][r + 1][c + 1] - sF[k][r + 1][c]) / g.dx;
+                    v[k] = x - dt * (gp - gm) / g.dy;
+                }
                 V[k * P + (long long)j * pitch + i] = v[k];
             }
-            cell_stats(v, gam, g.dx, g.dy, amax, umax, vmax, mass, nans);
+            if (FAST)
+                cell_stats_fast(v, K, g.dx * g.dy, amax, umax, vmax, mass, nans);
+            else
+                cell_stats(v, gam, g.dx, g.dy, amax, umax, vmax, mass, nans);
         }
     }
     block_reduce_finalize<NT>(amax, umax, vmax, mass, nans, st, a.partial, g, true, false);
 }
 
-template <int SCH, int RIE, int LIM>
+template <int SCH, int RIE, int LIM, int FAST>
 void launch_sweep(const SweepArgs &a, dim3 grid, dim3 block, cudaStream_t s)
 {
-    sweep_kernel<SCH, RIE, LIM><<<grid, block, 0, s>>>(a);
+    sweep_kernel<SCH, RIE, LIM, FAST><<<grid, block, 0, s>>>(a);
 }
 
 } // namespace ibtfo

@@ -1,5 +1,5 @@
-// Instantiations of the fused sweep for Scheme=MHM (one translation unit per
-// scheme so the library builds in parallel).
+// Instantiations of the fused sweep for Scheme=MHM, strict FP64 (compiled without contraction).
+// One translation unit per scheme and precision so the library builds in parallel.
 #include "sweep_impl.cuh"
 
 namespace ibtfo {
@@ -9,9 +9,9 @@ SweepLaunch sweep_launcher_mhm(int riemann, int limiter)
     const bool vl = (limiter == VANLEER);
     switch (riemann)
     {
-    case PVRS: return vl ? &launch_sweep<MHM, PVRS, VANLEER> : &launch_sweep<MHM, PVRS, MINMOD>;
-    case SW: return vl ? &launch_sweep<MHM, SW, VANLEER> : &launch_sweep<MHM, SW, MINMOD>;
-    default: return vl ? &launch_sweep<MHM, HLL, VANLEER> : &launch_sweep<MHM, HLL, MINMOD>;
+    case PVRS: return vl ? &launch_sweep<MHM, PVRS, VANLEER, 0> : &launch_sweep<MHM, PVRS, MINMOD, 0>;
+    case SW: return vl ? &launch_sweep<MHM, SW, VANLEER, 0> : &launch_sweep<MHM, SW, MINMOD, 0>;
+    default: return vl ? &launch_sweep<MHM, HLL, VANLEER, 0> : &launch_sweep<MHM, HLL, MINMOD, 0>;
     }
 }
 

@@ -1,5 +1,5 @@
-// Instantiations of the fused sweep for Scheme=MUSCL (one translation unit per
-// scheme so the library builds in parallel).
+// Instantiations of the fused sweep for Scheme=MUSCL, strict FP64 (compiled without contraction).
+// One translation unit per scheme and precision so the library builds in parallel.
 #include "sweep_impl.cuh"
 
 namespace ibtfo {
@@ -9,9 +9,9 @@ SweepLaunch sweep_launcher_muscl(int riemann, int limiter)
     const bool vl = (limiter == VANLEER);
     switch (riemann)
     {
-    case PVRS: return vl ? &launch_sweep<MUSCL, PVRS, VANLEER> : &launch_sweep<MUSCL, PVRS, MINMOD>;
-    case SW: return vl ? &launch_sweep<MUSCL, SW, VANLEER> : &launch_sweep<MUSCL, SW, MINMOD>;
-    default: return vl ? &launch_sweep<MUSCL, HLL, VANLEER> : &launch_sweep<MUSCL, HLL, MINMOD>;
+    case PVRS: return vl ? &launch_sweep<MUSCL, PVRS, VANLEER, 0> : &launch_sweep<MUSCL, PVRS, MINMOD, 0>;
+    case SW: return vl ? &launch_sweep<MUSCL, SW, VANLEER, 0> : &launch_sweep<MUSCL, SW, MINMOD, 0>;
+    default: return vl ? &launch_sweep<MUSCL, HLL, VANLEER, 0> : &launch_sweep<MUSCL, HLL, MINMOD, 0>;
     }
 }
 

@@ -49,6 +49,12 @@ enum {
     IBTFO_BOUNDARY_HBCGFM = 5
 };
 enum { IBTFO_GLOBAL_WALLS = 0, IBTFO_GLOBAL_PERIODIC = 1 };
+/* arithmetic of the step: FP64 evaluating the reference's expressions in
+ * their order (bit-for-bit with the reference except where the library
+ * pow(x, 0.5) and sqrt differ in the last bit), or FP64 with shared
+ * reciprocals and fused multiply-adds (rounding-level differences, well
+ * inside a 1e-12 relative bar) */
+enum { IBTFO_PRECISION_FP64 = 0, IBTFO_PRECISION_FP64_FAST = 1 };
 
 /* Case parameters: the numeric .inp keys the reference driver reads
  * (Test/Sod/Sod.cpp:34-48) plus the slot selections. */
@@ -58,7 +64,8 @@ typedef struct ibtfo_config {
     double gamma, cfl_number, psy_time;
     int max_iter;
     int scheme, riemann, limiter, boundary, global_boundary;
-    int reserved[8]; /* zero */
+    int precision;   /* IBTFO_PRECISION_* */
+    int reserved[7]; /* zero */
 } ibtfo_config;
 
 /* The reference time-loop scalars after the last completed step. */

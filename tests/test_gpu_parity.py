@@ -59,10 +59,13 @@ def seq_close(a, b, tol=RTOL):
     return np.allclose(a[fa], b[fb], rtol=tol, atol=0) and np.array_equal(a[~fa], b[~fb], equal_nan=True)
 
 
-def make_case(cfg):
+PRECISIONS = ["fp64", "fp64_fast"]
+
+
+def make_case(cfg, precision="fp64"):
     return ib.Case(cfg["N_x"], cfg["N_y"], cfg["num_ghost_cell"], (cfg["lo_x"], cfg["lo_y"]),
                    (cfg["hi_x"], cfg["hi_y"]), cfg["gamma"], cfg["CFL_number"], cfg["Psy_time"], cfg["max_iter"],
-                   cfg["scheme"], cfg["riemann"], cfg["limiter"], cfg["boundary"], cfg["gbc"])
+                   cfg["scheme"], cfg["riemann"], cfg["limiter"], cfg["boundary"], cfg["gbc"], precision)
 
 
 def run_steps(case, n):
@@ -81,13 +84,16 @@ def run_steps(case, n):
 PVRS_STRAY = {"quaddown_MUSCL_PVRS_minmod", "quaddown_MHM_PVRS_minmod"}
 
 
+@pytest.mark.parametrize("precision", PRECISIONS)
 @pytest.mark.parametrize("name", names())
-def test_gpu_matches_reference_fixture(name):
+def test_gpu_matches_reference_fixture(name, precision):
     fx = load(name)
     cfg = fx["config"]
     if name in PVRS_STRAY:
         pytest.xfail("PVRS :547-550 stray store into a remote flux slot is not reproduced")
-    with make_case(cfg) as c:
+    if precision == "fp64_fast" and not np.isfinite(fx["u_old"]).all():
+        pytest.skip("reference output holds NaN/inf: where NaN first appears depends on last-bit rounding")
+    with make_case(cfg, precision) as c:
         c.setup_geometry(fx["phi"])
         if "xycoord" in fx:
             assert np.array_equal(c.get_geometry(), fx["xycoord"]), "geometry differs"
@@ -111,8 +117,9 @@ def oracle_case(w, **kw):
                              w.riemann, w.limiter, w.boundary, w.gbc)
 
 
+@pytest.mark.parametrize("precision", PRECISIONS)
 @pytest.mark.parametrize("boundary", ["IDWBaseGFM", "LinearBaseGFM", "BCGFM", "HBCGFM"])
-def test_gpu_matches_oracle_inclined_channel(boundary):
+def test_gpu_matches_oracle_inclined_channel(boundary, precision):
     """Inclined channel at 512x256 (the benchmark workload's geometry at a
     quarter of its resolution), 20 steps, against the oracle."""
     from ibtfo_gb300 import cases
@@ -125,7 +132,7 @@ def test_gpu_matches_oracle_inclined_channel(boundary):
     u0 = cases.channel_init(w.grid, types, w.gamma)
     o.set_initial_state(u0)
     odts, oms = o.run(20)
-    with ib.Case.from_workload(w) as c:
+    with ib.Case.from_workload(w, precision=precision) as c:
         c.setup_geometry(phi)
         assert np.array_equal(c.get_geometry(), o.get("XYCOORD"))
         c.set_state(u0)
@@ -178,7 +185,8 @@ def test_loop_guard_stops_at_t_end():
         assert_state_close(c.get_state(), o.get("U_OLD"), "U_OLD at t_end")
 
 
-def test_run_to_t_end_sod_tube_l1():
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_run_to_t_end_sod_tube_l1(precision):
     """Sod tube 400x100 to t_end = 0.2: L1 density error <= 1e-10 vs the oracle."""
     from ibtfo_gb300 import cases
     w = cases.sod_tube()
@@ -188,7 +196,7 @@ def test_run_to_t_end_sod_tube_l1():
     o.setup_geometry(phi)
     o.set_initial_state(u0)
     o.run(10 ** 6, w.t_end)
-    with ib.Case.from_workload(w) as c:
+    with ib.Case.from_workload(w, precision=precision) as c:
         c.setup_geometry(phi)
         c.set_state(u0)
         p = c.run()
@@ -199,13 +207,14 @@ def test_run_to_t_end_sod_tube_l1():
         assert l1 <= 1e-10, l1
 
 
-def test_deterministic_repeat():
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_deterministic_repeat(precision):
     from ibtfo_gb300 import cases
     w = cases.inclined_channel(384, 192)
     phi = cases.channel_phi(w.grid)
     outs = []
     for _ in range(2):
-        with ib.Case.from_workload(w) as c:
+        with ib.Case.from_workload(w, precision=precision) as c:
             c.setup_geometry(phi)
             c.set_state(cases.channel_init(w.grid, c.cell_types(), w.gamma))
             c.advance(25)
