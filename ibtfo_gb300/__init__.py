@@ -81,8 +81,36 @@ SIGNATURES = {
     "ibtfo_synchronize": (C.c_int, [_P]),
     "ibtfo_dt_mass_noalloc": (C.c_int, [_P, C.c_longlong, C.c_int, _P, C.c_int, C.c_int, C.c_int, C.c_double,
                                         C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, _P, _P]),
+    "ibtfo_inp_open": (C.c_int, [C.c_char_p, C.POINTER(_P)]),
+    "ibtfo_inp_parse": (C.c_int, [C.c_char_p, C.POINTER(_P)]),
+    "ibtfo_inp_close": (None, [_P]),
+    "ibtfo_inp_get": (C.c_int, [_P, C.c_char_p, C.c_double, _DP]),
+    "ibtfo_inp_get_string": (C.c_int, [_P, C.c_char_p, C.c_char_p, C.c_int]),
+    "ibtfo_config_from_inp": (C.c_int, [_P, C.POINTER(Config)]),
+    "ibtfo_case_phi": (C.c_int, [C.c_char_p, _P, C.POINTER(Config), _DP]),
+    "ibtfo_case_init": (C.c_int, [C.c_char_p, _P, C.POINTER(Config), _DP, _DP]),
     "ibtfo_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(_P)]),
     "ibtfo_host_free": (C.c_int, [_P]),
+}
+
+_I = C.c_int
+_D = C.c_double
+# include/ibtfo_ref.h: the reference's entry points over host arrays
+REF_SIGNATURES = {
+    "ibtfo_ref_configure": (None, [_I] * 6),
+    "ibtfo_ref_status": (_I, []),
+    "ibtfo_ref_Psy_coord": (None, [_D, _D, _D, _D, _I, _I, _I, _DP, _I, _I]),
+    "ibtfo_ref_Level_Set": (None, [_I, _I, _I, _DP, _I, _I]),
+    "ibtfo_ref_Scheme_Index": (None, [_I, _I, _I, _DP, _DP, _I, _I]),
+    "ibtfo_ref_TimeAdvance": (None, [_D, _D, _I, _I, _I, _D, _D, _DP, _DP, _DP, _DP, _DP, _I, _I]),
+    "ibtfo_ref_Advance": (None, [_D, _D, _I, _I, _I, _D, _D, _DP, _DP, _DP, _DP, _I, _I]),
+    "ibtfo_ref_Boundary": (None, [_I, _I, _I, _D, _DP, _DP, _DP, _DP, _I, _I]),
+    "ibtfo_ref_Global_Boundary": (None, [_I, _I, _I, _D, _DP, _DP, _I, _I]),
+    "ibtfo_ref_ComputeDt": (None, [_D, _D, _I, _I, _I, _D, _D, _DP, _DP, _DP, _I, _I]),
+    "ibtfo_ref_CaculateMass": (None, [_D, _D, _I, _I, _I, _DP, _DP, _DP, _I, _I]),
+    "ibtfo_ref_update_self": (None, [_DP]),
+    "ibtfo_ref_update_device": (None, [_DP]),
+    "ibtfo_ref_release": (None, [_DP]),
 }
 
 _lib = None
@@ -95,7 +123,7 @@ def lib():
         if not os.path.exists(LIB_PATH):
             raise ImportError(f"{LIB_PATH} is missing: run `python -m ibtfo_gb300.build` (needs nvcc)")
         L = C.CDLL(LIB_PATH)
-        for name, (res, args) in SIGNATURES.items():
+        for name, (res, args) in list(SIGNATURES.items()) + list(REF_SIGNATURES.items()):
             f = getattr(L, name)
             f.restype = res
             f.argtypes = args
@@ -242,6 +270,63 @@ class Case:
 
     def synchronize(self):
         _check(lib().ibtfo_synchronize(self.h))
+
+
+class Inp:
+    """A parsed .inp file (the reference's ParamReader rules)."""
+
+    def __init__(self, path=None, text=None):
+        h = _P()
+        if text is not None:
+            _check(lib().ibtfo_inp_parse(text.encode(), C.byref(h)))
+        else:
+            _check(lib().ibtfo_inp_open(str(path).encode(), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().ibtfo_inp_close(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def get(self, key, default=0.0):
+        v = C.c_double()
+        found = lib().ibtfo_inp_get(self.h, key.encode(), float(default), C.byref(v))
+        return v.value, bool(found)
+
+    def get_string(self, key):
+        buf = C.create_string_buffer(256)
+        return buf.value.decode() if lib().ibtfo_inp_get_string(self.h, key.encode(), buf, 256) else None
+
+    def config(self):
+        cfg = Config()
+        _check(lib().ibtfo_config_from_inp(self.h, C.byref(cfg)))
+        return cfg
+
+
+def case_phi(name, cfg, inp=None):
+    n = (cfg.n_x + 2 * cfg.num_ghost_cell) * (cfg.n_y + 2 * cfg.num_ghost_cell)
+    out = np.empty(n)
+    _check(lib().ibtfo_case_phi(name.encode(), inp.h if inp else None, C.byref(cfg), _dp(out)))
+    return out
+
+
+def case_init(name, cfg, xycoord, inp=None):
+    xy = np.ascontiguousarray(xycoord, dtype=np.float64).reshape(-1)
+    out = np.empty(xy.size // 6 * 4)
+    _check(lib().ibtfo_case_init(name.encode(), inp.h if inp else None, C.byref(cfg), _dp(xy), _dp(out)))
+    return out
+
+
+def config(n_x, n_y, ng=2, lo=(0.0, 0.0), hi=(1.0, 1.0), gamma=1.4, cfl=0.5, t_end=1.0, max_iter=100000,
+           scheme="MUSCL", riemann="HLL", limiter="minmod", boundary="Regular", gbc="walls", precision="fp64"):
+    return Config(n_x, n_y, ng, lo[0], lo[1], hi[0], hi[1], gamma, cfl, t_end, max_iter, SCHEMES[scheme],
+                  RIEMANNS[riemann], LIMITERS[limiter], BOUNDARIES[boundary], GLOBAL_BCS[gbc], PRECISIONS[precision])
 
 
 class PinnedBuffer:

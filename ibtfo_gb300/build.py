@@ -24,6 +24,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libibtfo_gb300.so")
+CLI = os.path.join(HERE, "ibtfo_run")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "--expt-relaxed-constexpr",
@@ -84,6 +85,13 @@ def build(force: bool = False, jobs: int | None = None, verbose: bool = False) -
         if p.returncode != 0:
             raise RuntimeError("link failed:\n" + p.stdout + p.stderr)
         os.replace(tmp, LIB)
+    cli_src = os.path.join(HERE, "cli", "ibtfo_run.cpp")
+    if os.path.exists(cli_src) and (force or _newer(CLI, [cli_src, LIB])):
+        cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I" + os.path.join(ROOT, "include"), cli_src,
+               "-L" + HERE, "-libtfo_gb300", "-Wl,-rpath,$ORIGIN", "-o", CLI]
+        p = subprocess.run(cmd, capture_output=True, text=True)
+        if p.returncode != 0:
+            raise RuntimeError("ibtfo_run build failed:\n" + p.stdout + p.stderr)
     return LIB
 
 

@@ -695,3 +695,83 @@ ibtfo_status ibtfo_host_free(void *p)
 }
 
 } // extern "C"
+
+// ---------------------------------------------------------------- internal
+namespace ibtfo {
+
+static void drop_graph(ibtfo_case *c)
+{
+    if (c->graph)
+    {
+        cudaGraphExecDestroy(c->graph);
+        c->graph = nullptr;
+        c->graph_steps = 0;
+    }
+}
+
+int case_set_gas(ibtfo_case *c, double gamma, double cfl)
+{
+    if (!(gamma > 1.0) || !(cfl > 0.0))
+        return fail(IBTFO_EINVAL, "need gamma > 1 and cfl > 0");
+    if (c->g.gamma != gamma || c->g.cfl != cfl)
+    {
+        cudaSetDevice(c->device);
+        cudaStreamSynchronize(c->stream);
+        c->g.gamma = c->cfg.gamma = gamma;
+        c->g.cfl = c->cfg.cfl_number = cfl;
+        drop_graph(c);
+    }
+    return IBTFO_OK;
+}
+
+double case_cfl(const ibtfo_case *c) { return c->g.cfl; }
+double case_gamma(const ibtfo_case *c) { return c->g.gamma; }
+
+int case_set_dt(ibtfo_case *c, double dt)
+{
+    cudaSetDevice(c->device);
+    CK(cudaMemcpyAsync(&c->st->dt, &dt, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream)); // dt lives on this stack frame
+    return IBTFO_OK;
+}
+
+int case_sweep_unguarded(ibtfo_case *c)
+{
+    cudaSetDevice(c->device);
+    c->sweep(sweep_args(c, 0), dim3(c->ntiles), dim3(TILE_X * TILE_Y), c->stream);
+    count_launch();
+    CK(cudaGetLastError());
+    return IBTFO_OK;
+}
+
+int case_fill(ibtfo_case *c, int ghosts, int ring)
+{
+    cudaSetDevice(c->device);
+    FillArgs f = fill_args(c);
+    f.do_ghosts = (ghosts && c->cfg.boundary != IBTFO_BOUNDARY_REGULAR) ? 1 : 0;
+    f.do_ring = ring ? 1 : 0;
+    launch_fill(f, c->stream);
+    CK(cudaGetLastError());
+    return IBTFO_OK;
+}
+
+int case_reduce_current(ibtfo_case *c)
+{
+    cudaSetDevice(c->device);
+    DevState s;
+    CK(cudaMemcpyAsync(&s, c->st, sizeof(DevState), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    ReduceArgs r{};
+    r.g = c->g;
+    r.u = c->buf[s.cur];
+    r.type = c->type;
+    r.st = c->st;
+    r.partial = c->partial;
+    r.set_start = 0;
+    launch_reduce(r, c->nblocks, c->stream);
+    CK(cudaGetLastError());
+    return IBTFO_OK;
+}
+
+} // namespace ibtfo
+

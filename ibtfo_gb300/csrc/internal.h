@@ -120,3 +120,17 @@ int setup_geometry(const GridDesc &g, int bc, const double *d_phi, double *d_nx,
 void count_launch(int n = 1);
 
 } // namespace ibtfo
+
+// operations on a case used by the reference-signature entry points
+struct ibtfo_case;
+namespace ibtfo {
+int case_set_gas(ibtfo_case *c, double gamma, double cfl);       // 0 or an ibtfo_status
+int case_set_dt(ibtfo_case *c, double dt);
+int case_sweep_unguarded(ibtfo_case *c);
+int case_fill(ibtfo_case *c, int ghosts, int ring);
+int case_reduce_current(ibtfo_case *c);
+double case_cfl(const ibtfo_case *c);
+double case_gamma(const ibtfo_case *c);
+void set_last_error(const char *msg);
+
+} // namespace ibtfo

@@ -142,6 +142,34 @@ ibtfo_status ibtfo_run(ibtfo_case *c, int stop_on_nan, ibtfo_progress *p);
 ibtfo_status ibtfo_get_progress(ibtfo_case *c, ibtfo_progress *p);
 ibtfo_status ibtfo_synchronize(ibtfo_case *c);
 
+/* .inp files, read as the reference's ParamReader reads them
+ * (Src/Utils/ParamReader.cpp:14-68: '#' lines skipped, spaces removed, the
+ * first [+-]?(\d*\.\d+|\d+) after '=' converted with atof), plus string
+ * values for the solver-slot keys. */
+typedef struct ibtfo_inp ibtfo_inp;
+ibtfo_status ibtfo_inp_open(const char *path, ibtfo_inp **out);
+ibtfo_status ibtfo_inp_parse(const char *text, ibtfo_inp **out);
+void ibtfo_inp_close(ibtfo_inp *p);
+/* value of `key`, or `def` when absent (Params::get, ParamReader.H:47-55);
+ * returns 1 if the key is present */
+int ibtfo_inp_get(const ibtfo_inp *p, const char *key, double def, double *value);
+int ibtfo_inp_get_string(const ibtfo_inp *p, const char *key, char *buf, int size);
+/* numeric keys with the reference drivers' defaults (Test/Sod/Sod.cpp:34-48)
+ * and the slot keys Scheme (MUSCL|MHM|Godunov), Riemann (HLL|HLLC|PVRS|
+ * StegerWarming), Limiter (minmod|VanLeer), Boundary (Regular|IDWBaseGFM|
+ * LinearBaseGFM|RiemannBaseGFM|BCGFM|HBCGFM), Global_Boundary (Walls|
+ * Periodic), Precision (FP64|FP64_FAST) */
+ibtfo_status ibtfo_config_from_inp(const ibtfo_inp *p, ibtfo_config *cfg);
+
+/* Case plug-ins (the reference's per-case Level_Set_function and Initialize
+ * files): sod_ref (Test/Sod), incline_ref (Test/InclineSod), vortex_ref
+ * (Test/Vortex), sod_x, channel, isentropic_vortex; parameters from `p`
+ * (may be NULL for defaults).  phi: M*N doubles.  init: M*N*4 doubles from
+ * XYCOORD (coordinates and cell types, as Initialize reads them). */
+ibtfo_status ibtfo_case_phi(const char *name, const ibtfo_inp *p, const ibtfo_config *cfg, double *phi);
+ibtfo_status ibtfo_case_init(const char *name, const ibtfo_inp *p, const ibtfo_config *cfg, const double *xycoord,
+                             double *u0);
+
 /* CFL time step and fluid mass of a device-resident state, allocating
  * nothing.  No counterpart in the reference: it serves callers that cannot
  * call cudaMalloc -- code running inside a framework that owns all device

@@ -33,9 +33,8 @@ def test_library_exports_every_declared_symbol():
 
 def test_python_binding_covers_the_header():
     names = set(declared_functions())
-    bound = set(ib.SIGNATURES)
-    assert names - bound == set() or names - bound <= {n for n in names if n.startswith("ibtfo_ref_")}
-    assert bound <= names
+    bound = set(ib.SIGNATURES) | set(ib.REF_SIGNATURES)
+    assert names == bound, (names - bound, bound - names)
 
 
 def test_abi_version():

@@ -1,0 +1,127 @@
+"""GPU tests of the host-facing layers: the reference-signature entry points
+(include/ibtfo_ref.h) driven in the reference driver's call order, and the
+C++ time-loop executable ibtfo_run."""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+from golden_util import load
+
+ib = pytest.importorskip("ibtfo_gb300")
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-12
+
+
+def _p(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def rel_linf(a, b):
+    a, b = a.reshape(-1, 4), b.reshape(-1, 4)
+    worst = 0.0
+    for k in range(4):
+        m = np.isfinite(b[:, k])
+        if m.any():
+            worst = max(worst, float(np.abs(a[m, k] - b[m, k]).max() / max(np.abs(b[m, k]).max(), 1e-300)))
+    return worst
+
+
+@pytest.mark.parametrize("name", ["refincline_MUSCL_HLL_minmod_IDWBaseGFM", "channel_MUSCL_HLLC_minmod_BCGFM",
+                                  "channel_MUSCL_HLLC_minmod_LinearBaseGFM", "sodtube_MUSCL_HLL_minmod",
+                                  "refsod_MUSCL_HLL_minmod"])
+def test_reference_driver_sequence_through_shim(name):
+    """Test/InclineSod/InclineSod.cpp:97-189 call by call through ibtfo_ref_*."""
+    fx = load(name)
+    c = fx["config"]
+    L = ib.lib()
+    L.ibtfo_ref_configure(ib.SCHEMES[c["scheme"]], ib.RIEMANNS[c["riemann"]], ib.LIMITERS[c["limiter"]],
+                          ib.BOUNDARIES[c["boundary"]], ib.GLOBAL_BCS[c["gbc"]], 0)
+    nx, ny, ng, g = c["N_x"], c["N_y"], c["num_ghost_cell"], c["gamma"]
+    M, N = nx + 2 * ng, ny + 2 * ng
+    PL, PH = c["hi_x"] - c["lo_x"], c["hi_y"] - c["lo_y"]
+    nsch = {"Regular": 1, "IDWBaseGFM": 8, "LinearBaseGFM": 4, "RiemannBaseGFM": 4}.get(c["boundary"], 16)
+    XY = np.zeros(M * N * 6)
+    SCH = np.zeros(M * N * nsch)
+    U_OLD = np.zeros(M * N * 4)
+    U_NEW = np.zeros(M * N * 4)
+    U_TMP = np.zeros(1)
+    dt_buf, m_buf = np.zeros(1), np.zeros(1)
+    L.ibtfo_ref_Psy_coord(c["lo_x"], c["lo_y"], PL, PH, nx, ny, ng, _p(XY), 1, 0)
+    XY.reshape(-1, 6)[:, 2] = fx["phi"]  # the case's Level_Set_function
+    L.ibtfo_ref_Level_Set(nx, ny, ng, _p(XY), 1, 0)
+    assert L.ibtfo_ref_status() == 0, L.ibtfo_last_error()
+    if c["boundary"] != "Regular":
+        L.ibtfo_ref_Scheme_Index(nx, ny, ng, _p(XY), _p(SCH), 1, 0)
+        assert np.array_equal(SCH, fx["scheme_idx"])
+    if "xycoord" in fx:
+        assert np.array_equal(XY, fx["xycoord"])
+    U_OLD[:] = fx["u_init"]  # the case's Initialize
+    U_NEW[:] = fx["u_init"]
+    L.ibtfo_ref_Boundary(nx, ny, ng, g, _p(U_OLD), _p(U_NEW), _p(XY), _p(SCH), 1, 0)
+    L.ibtfo_ref_ComputeDt(PL, PH, nx, ny, ng, g, c["CFL_number"], _p(U_OLD), _p(XY), _p(dt_buf), 1, 0)
+    L.ibtfo_ref_CaculateMass(PL, PH, nx, ny, ng, _p(U_OLD), _p(XY), _p(m_buf), 1, 0)
+    assert L.ibtfo_ref_status() == 0, L.ibtfo_last_error()
+    dt = dt_buf[0]
+    assert np.isclose(dt, fx["dts"][0], rtol=RTOL, atol=0)
+    now_t, it, dts, ms = 0.0, 0, [], []
+    while now_t < c["Psy_time"] and it < fx["iters"]:
+        L.ibtfo_ref_TimeAdvance(PL, PH, nx, ny, ng, g, dt, _p(U_OLD), _p(U_TMP), _p(U_NEW), _p(XY), _p(SCH), 1, 0)
+        L.ibtfo_ref_Boundary(nx, ny, ng, g, _p(U_OLD), _p(U_NEW), _p(XY), _p(SCH), 1, 0)
+        L.ibtfo_ref_Global_Boundary(nx, ny, ng, g, _p(U_OLD), _p(U_NEW), 1, 0)
+        L.ibtfo_ref_ComputeDt(PL, PH, nx, ny, ng, g, c["CFL_number"], _p(U_OLD), _p(XY), _p(dt_buf), 1, 0)
+        L.ibtfo_ref_CaculateMass(PL, PH, nx, ny, ng, _p(U_OLD), _p(XY), _p(m_buf), 1, 0)
+        assert L.ibtfo_ref_status() == 0, L.ibtfo_last_error()
+        dt = dt_buf[0]
+        now_t += dt
+        it += 1
+        dts.append(dt)
+        ms.append(m_buf[0])
+    assert it == fx["iters"]
+    assert np.allclose(dts, fx["dts"][1:], rtol=RTOL, atol=0)
+    assert np.allclose(ms, fx["masses"][1:], rtol=RTOL, atol=0)
+    L.ibtfo_ref_update_self(_p(U_OLD))
+    L.ibtfo_ref_update_self(_p(U_NEW))
+    assert L.ibtfo_ref_status() == 0, L.ibtfo_last_error()
+    assert np.array_equal(np.isfinite(U_OLD), np.isfinite(fx["u_old"]))
+    assert rel_linf(U_OLD, fx["u_old"]) <= RTOL
+    assert rel_linf(U_NEW, fx["u_new"]) <= RTOL
+    L.ibtfo_ref_release(_p(XY))
+
+
+def test_shim_rejects_several_devices():
+    L = ib.lib()
+    XY = np.zeros(12 * 12 * 6)
+    L.ibtfo_ref_Psy_coord(0.0, 0.0, 1.0, 1.0, 8, 8, 2, _p(XY), 2, 0)
+    assert L.ibtfo_ref_status() == 1  # IBTFO_EINVAL
+
+
+def test_ibtfo_run_executable(tmp_path):
+    """The C++ driver on a channel .inp against the oracle on the same plug-in inputs."""
+    exe = os.path.join(os.path.dirname(ib.LIB_PATH), "ibtfo_run")
+    assert os.path.exists(exe), "ibtfo_run is built with the library"
+    inp = tmp_path / "channel.inp"
+    inp.write_text("#channel\nN_x=128\nN_y=64\nlo_x=0\nlo_y=0\nhi_x=2\nhi_y=1\nCFL_number=0.45\n"
+                   "Psy_time=0.2\nnum_ghost_cell=2\ngamma=1.4\nangle=30\nwidth=0.25\n"
+                   "Scheme = MUSCL\nRiemann = HLLC\nLimiter = minmod\nBoundary = IDWBaseGFM\nCase = channel\n")
+    out = tmp_path / "u.bin"
+    p = subprocess.run([exe, str(inp), "--steps", "15", "--print-every", "5", "--out", str(out)],
+                       capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr
+    lines = [ln for ln in p.stdout.splitlines() if ln.startswith("iter : ")]
+    assert len(lines) == 3 and lines[-1].startswith("iter : 15.   dt :")
+    u = np.fromfile(out, dtype=np.float64)
+
+    cfg = ib.Inp(path=str(inp)).config()
+    inpo = ib.Inp(path=str(inp))
+    phi = ib.case_phi("channel", cfg, inpo)
+    o = oracle.OracleCase(128, 64, 2, (0.0, 0.0), (2.0, 1.0), 1.4, 0.45, "MUSCL", "HLLC", "minmod", "IDWBaseGFM")
+    o.setup_geometry(phi)
+    o.set_initial_state(ib.case_init("channel", cfg, o.get("XYCOORD"), inpo))
+    o.run(15)
+    assert rel_linf(u, o.get("U_OLD")) <= RTOL
