@@ -167,22 +167,33 @@ def cpu_oracle_rate(w, steps=None, warmup=1, budget_s=15.0):
 
 
 # ------------------------------------------------------------------ GPU leg
-def gpu_arm(args, rank, world, local_rank, precision=None, e2e=True):
+def channel_inputs(w, case):
+    from ibtfo_gb300 import cases
+    phi = cases.channel_phi(w.grid)
+    case.setup_geometry(phi)
+    case.set_state(cases.channel_init(w.grid, case.cell_types(), w.gamma))
+
+
+def vortex_inputs(w, case):
+    from ibtfo_gb300 import cases
+    phi, u0 = cases.isentropic_vortex(w.grid)
+    case.setup_geometry(phi)
+    case.set_state(u0)
+
+
+def gpu_arm(args, rank, world, local_rank, precision=None, e2e=True, w=None, inputs=channel_inputs, steps=None):
     import torch
     import ibtfo_gb300 as ib
-    from ibtfo_gb300 import cases
 
     torch.cuda.set_device(local_rank)
-    w = workload()
+    w = w or workload()
     g = w.grid
     cells = g.n_x * g.n_y
     stream = torch.cuda.Stream()
     c = ib.Case.from_workload(w, t_end=1e300, max_iter=2 ** 31 - 1, precision=precision or PRECISION)
     c.set_stream(stream.cuda_stream)
-    phi = cases.channel_phi(g)
-    c.setup_geometry(phi)
-    u0 = cases.channel_init(g, c.cell_types(), w.gamma)
-    c.set_state(u0)
+    inputs(w, c)
+    K = steps or args.steps
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > 129 MB L2
 
     with torch.cuda.stream(stream):
@@ -191,14 +202,14 @@ def gpu_arm(args, rank, world, local_rank, precision=None, e2e=True):
             c.enqueue_boundary()
     stream.synchronize()
 
-    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(K)]
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     launches0 = ib.launch_count()
     with ClockSampler(local_rank) as clk:
         with torch.cuda.stream(stream):
-            for k in range(args.steps):
+            for k in range(K):
                 flush.fill_(float(k))
                 ev[k][0].record(stream)
                 c.enqueue_sweep()
@@ -214,7 +225,7 @@ def gpu_arm(args, rank, world, local_rank, precision=None, e2e=True):
     prog = c.progress()
 
     # end to end through the C ABI with host buffers (pinned)
-    e2e_steps = max(1, min(args.steps, 20)) if e2e else 1
+    e2e_steps = max(1, min(K, 20)) if e2e else 1
     pin = ib.PinnedBuffer(g.M * g.N * 4)
     c.get_state_ptr(pin.ptr)
     torch.cuda.synchronize()
@@ -284,6 +295,19 @@ def main():
     # the other FP64 precision, timed the same way (steps only), for comparison
     other = "fp64" if PRECISION == "fp64_fast" else "fp64_fast"
     r2 = gpu_arm(args, rank, world, local_rank, precision=other, e2e=False)
+    # the isentropic-vortex workload (4096^2, periodic, MHM + HLLC) in the FP64
+    # path and in the FP32 compensated precision form
+    from ibtfo_gb300 import cases as _cases
+    wv = _cases.vortex_periodic(4096)
+    kv = max(10, min(args.steps, 100))
+    forms = {}
+    for prec in ("fp64_fast", "fp32c"):
+        rv = gpu_arm(args, rank, world, local_rank, precision=prec, e2e=False, w=wv, inputs=vortex_inputs, steps=kv)
+        cv = wv.grid.n_x * wv.grid.n_y
+        sw_s = rv["sweep_ms"] * 1e-3 / kv
+        forms[prec] = {"value": world * cv * kv / (rv["step_ms"] * 1e-3) / 1e9, "unit": METRIC, "steps": kv,
+                       "sweep_ms": rv["sweep_ms"] / kv,
+                       "roofline_frac": BYTES_PER_CELL * cv / sw_s / 1e9 / measured_peaks()[0]}
     if world > 1:
         import torch
         torch.distributed.destroy_process_group()
@@ -310,6 +334,8 @@ def main():
             "gpu_launches": r["launches"], "clocks": r["clocks"],
             "other_precision": {"precision": other, "value": world * cells * K / (r2["step_ms"] * 1e-3) / 1e9,
                                 "unit": METRIC, "sweep_ms": r2["sweep_ms"] / K},
+            "forms": {"workload": wv.name, "scheme": wv.scheme, "riemann": wv.riemann, "boundary": "periodic",
+                      **forms},
             "final": {"iter": r["progress"]["iter"], "nan_cells": r["progress"]["nan_cells"]}}
     print(json.dumps(line), flush=True)
     return 0

@@ -22,11 +22,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libibtfo_gb300.so")
 
 SCHEMES = {"MUSCL": 0, "MHM": 1, "Godunov": 2}
-RIEMANNS = {"HLL": 0, "HLLC": 1, "PVRS": 2, "StegerWarming": 3}
+RIEMANNS = {"HLL": 0, "HLLC": 1, "PVRS": 2, "StegerWarming": 3, "HLLC_Toro": 4}
 LIMITERS = {"minmod": 0, "VanLeer": 1}
 BOUNDARIES = {"Regular": 0, "IDWBaseGFM": 1, "LinearBaseGFM": 2, "RiemannBaseGFM": 3, "BCGFM": 4, "HBCGFM": 5}
 GLOBAL_BCS = {"walls": 0, "periodic": 1}
-PRECISIONS = {"fp64": 0, "fp64_fast": 1}
+PRECISIONS = {"fp64": 0, "fp64_fast": 1, "fp32c": 2}
 
 STATUS = {0: "OK", 1: "EINVAL", 2: "ENOMEM", 3: "ENAN", 4: "ETIMEOUT", 5: "ECUDA", 6: "ESTATE"}
 

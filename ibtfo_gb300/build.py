@@ -5,7 +5,7 @@ for sm_103a into ibtfo_gb300/libibtfo_gb300.so (in-tree, git-ignored).
 
 Translation units compile in parallel.  Device code is compiled without
 floating-point contraction (the reference's expressions evaluate to the same
-binary64 values) except in the *_fast.cu units of the fp64_fast precision;
+binary64 values) except in the *_fast.cu and *_f32.cu units (fp64_fast and FP32 forms);
 host code is compiled without contraction so that coordinates and other
 host-side values match the reference bit for bit on every host architecture.
 """
@@ -61,8 +61,8 @@ def build(force: bool = False, jobs: int | None = None, verbose: bool = False) -
     def compile_one(so):
         s, o = so
         flags = list(NVFLAGS)
-        if os.path.basename(s).endswith("_fast.cu"):
-            flags[flags.index("-fmad=false")] = "-fmad=true"  # fp64_fast units contract multiply-adds
+        if os.path.basename(s).endswith(("_fast.cu", "_f32.cu")):
+            flags[flags.index("-fmad=false")] = "-fmad=true"  # fp64_fast and FP32 units contract multiply-adds
         cmd = [nv] + flags + ["-c", s, "-o", o]
         if s.endswith(".cpp"):
             cmd = [nv, "-x", "cu"] + NVFLAGS + ["-c", s, "-o", o]

@@ -186,7 +186,12 @@ def inclined_channel(n_x=2048, n_y=1024, boundary="IDWBaseGFM"):
                     "MUSCL", "HLLC", "minmod", boundary, extra={"angle": 30.0, "width": 0.25})
 
 
-def vortex_periodic(n=4096):
-    """Isentropic vortex, periodic n x n on [0,10]^2, beta 5, MHM + HLLC, t 10."""
+def vortex_periodic(n=4096, riemann="HLLC_Toro"):
+    """Isentropic vortex, periodic n x n on [0,10]^2, beta 5, MHM + HLLC, t 10.
+
+    The vortex's vertical velocity exceeds the sound speed in part of the
+    core; the reference's HLLC (its HLL solver, which reuses the X-face flux
+    where S_D >= 0) turns the state to NaN there within a few dozen steps, so
+    the workload runs the contact-restoring HLLC ("HLLC_Toro")."""
     return Workload(f"isentropic_vortex_{n}", Grid(n, n, 2, 0.0, 0.0, 10.0, 10.0), 1.4, 0.5, 10.0,
-                    "MHM", "HLLC", "minmod", "Regular", gbc="periodic", extra={"beta": 5.0})
+                    "MHM", riemann, "minmod", "Regular", gbc="periodic", extra={"beta": 5.0})

@@ -23,6 +23,7 @@ struct View
 {
     const double *next, *prev;
     const uint8_t *type;
+    GridDesc g;
     long long P;
     int pitch, ng, n_x, n_y;
     __device__ __forceinline__ bool interior(int i, int j) const
@@ -34,7 +35,11 @@ struct View
     {
         long long o = (long long)j * pitch + i;
         const double *b = (interior(i, j) && type[o] == 0) ? next : prev;
-        return b[k * P + o];
+        return state_ld(b, k, o, g);
+    }
+    __device__ __forceinline__ double N_(int i, int j, int k) const
+    {
+        return state_ld(next, k, (long long)j * pitch + i, g);
     }
 };
 
@@ -64,30 +69,29 @@ __device__ __forceinline__ void idw_average(const View &v, int idx, int idy, con
 }
 
 // reflect the normal velocity and store conserved values, GFM_Bound.cpp:219-228
-__device__ __forceinline__ void store_reflected(double *dst, long long o, long long P, double g, double nx, double ny,
-                                                double rho_w, double u_w, double v_w, double p_w)
+__device__ __forceinline__ void store_reflected(double *dst, long long o, const GridDesc &gd, double g, double nx,
+                                                double ny, double rho_w, double u_w, double v_w, double p_w)
 {
     double u_n = u_w * nx + v_w * ny;
     double u_t = u_w * ny - v_w * nx;
     u_n = -u_n;
     u_w = u_n * nx + u_t * ny;
     v_w = u_n * ny - u_t * nx;
-    dst[o] = rho_w;
-    dst[P + o] = rho_w * u_w;
-    dst[2 * P + o] = rho_w * v_w;
-    dst[3 * P + o] = p_w / (g - 1) + 0.5 * rho_w * (u_w * u_w + v_w * v_w);
+    state_st(dst, 0, o, rho_w, gd);
+    state_st(dst, 1, o, rho_w * u_w, gd);
+    state_st(dst, 2, o, rho_w * v_w, gd);
+    state_st(dst, 3, o, p_w / (g - 1) + 0.5 * rho_w * (u_w * u_w + v_w * v_w), gd);
 }
 
 __device__ void fill_ghost(const FillArgs &a, const View &v, double *dst, const GhostRec &h)
 {
     const double g = a.g.gamma;
     const long long o = (long long)h.j * a.g.pitch + h.i;
-    const long long P = a.g.plane;
     if (a.bc == BC_IDW)
     {
         double w[4];
         idw_average(v, h.idx, h.idy, h.w, g, w);
-        store_reflected(dst, o, P, g, h.nx, h.ny, w[0], w[1], w[2], w[3]);
+        store_reflected(dst, o, a.g, g, h.nx, h.ny, w[0], w[1], w[2], w[3]);
     }
     else if (a.bc == BC_LINEAR || a.bc == BC_RIEMANNGFM)
     {
@@ -99,7 +103,7 @@ __device__ void fill_ghost(const FillArgs &a, const View &v, double *dst, const 
             const int cj = (h.pick == 1 || h.pick == 4) ? h.idy : h.idy + 1;
             prim(v, ci, cj, g, rho, u, w, p);
         }
-        store_reflected(dst, o, P, g, h.nx, h.ny, rho, u, w, p);
+        store_reflected(dst, o, a.g, g, h.nx, h.ny, rho, u, w, p);
     }
     else
     {
@@ -129,10 +133,10 @@ __device__ void fill_ghost(const FillArgs &a, const View &v, double *dst, const 
         }
         double u_m = u_n_m * nx + u_t_m * ny;
         double v_m = u_n_m * ny - u_t_m * nx;
-        dst[o] = rho_m;
-        dst[P + o] = rho_m * u_m;
-        dst[2 * P + o] = rho_m * v_m;
-        dst[3 * P + o] = p_m / (g - 1) + 0.5 * rho_m * (u_m * u_m + v_m * v_m);
+        state_st(dst, 0, o, rho_m, a.g);
+        state_st(dst, 1, o, rho_m * u_m, a.g);
+        state_st(dst, 2, o, rho_m * v_m, a.g);
+        state_st(dst, 3, o, p_m / (g - 1) + 0.5 * rho_m * (u_m * u_m + v_m * v_m), a.g);
     }
 }
 
@@ -141,7 +145,6 @@ __device__ void fill_ghost(const FillArgs &a, const View &v, double *dst, const 
 __device__ void fill_ring(const FillArgs &a, const View &v, double *dst, long long q)
 {
     const int ng = a.g.ng, n_x = a.g.n_x, n_y = a.g.n_y, N = a.g.N, pitch = a.g.pitch;
-    const long long P = a.g.plane;
     const long long nrow = 2LL * ng * n_x;
     int i, j;
     bool row;
@@ -179,7 +182,7 @@ __device__ void fill_ring(const FillArgs &a, const View &v, double *dst, long lo
             if (row || !src_interior_row || (sj != j))
                 out[k] = v.S(si, sj, k); // value S(.) of an interior cell
             else
-                out[k] = v.next[k * P + (long long)sj * pitch + si]; // interior row, after the fill
+                out[k] = v.N_(si, sj, k); // interior row, after the fill
         }
     }
     else if (row)
@@ -210,7 +213,7 @@ __device__ void fill_ring(const FillArgs &a, const View &v, double *dst, long lo
         }
     }
     for (int k = 0; k < 4; k++)
-        dst[k * P + o] = out[k];
+        state_st(dst, k, o, out[k], a.g);
 }
 
 __global__ void __launch_bounds__(256) fill_kernel(const FillArgs a)
@@ -223,6 +226,7 @@ __global__ void __launch_bounds__(256) fill_kernel(const FillArgs a)
     v.next = cur ? a.buf1 : a.buf0;
     v.prev = cur ? a.buf0 : a.buf1;
     v.type = a.type;
+    v.g = a.g;
     v.P = a.g.plane;
     v.pitch = a.g.pitch;
     v.ng = a.g.ng;
@@ -274,7 +278,7 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) reduce_kernel(const ReduceArgs
         {
             double v[4];
             for (int k = 0; k < 4; k++)
-                v[k] = a.u[k * g.plane + o];
+                v[k] = state_ld(a.u, k, o, g);
             cell_stats(v, g.gamma, g.dx, g.dy, amax, umax, vmax, mass, nans);
         }
     }
@@ -298,7 +302,7 @@ __global__ void aos_to_soa_kernel(const double *__restrict__ aos, double *__rest
     int j = (int)(c / g.M), i = (int)(c - (long long)j * g.M);
     long long o = (long long)j * g.pitch + i;
     for (int k = 0; k < 4; k++)
-        soa[k * g.plane + o] = aos[c * 4 + k];
+        state_st(soa, k, o, aos[c * 4 + k], g);
 }
 
 __global__ void soa_to_aos_kernel(const double *__restrict__ soa, double *__restrict__ aos, GridDesc g)
@@ -309,7 +313,7 @@ __global__ void soa_to_aos_kernel(const double *__restrict__ soa, double *__rest
     int j = (int)(c / g.M), i = (int)(c - (long long)j * g.M);
     long long o = (long long)j * g.pitch + i;
     for (int k = 0; k < 4; k++)
-        aos[c * 4 + k] = soa[k * g.plane + o];
+        aos[c * 4 + k] = state_ld(soa, k, o, g);
 }
 
 void launch_aos_to_soa(const double *aos, double *soa, const GridDesc &g, cudaStream_t s)

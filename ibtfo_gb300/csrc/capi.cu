@@ -23,11 +23,23 @@ SweepLaunch sweep_launcher_godunov(int riemann, int limiter);
 SweepLaunch sweep_launcher_muscl_fast(int riemann, int limiter);
 SweepLaunch sweep_launcher_mhm_fast(int riemann, int limiter);
 SweepLaunch sweep_launcher_godunov_fast(int riemann, int limiter);
+SweepLaunch sweep_launcher_muscl_f32(int riemann, int limiter);
+SweepLaunch sweep_launcher_mhm_f32(int riemann, int limiter);
+SweepLaunch sweep_launcher_godunov_f32(int riemann, int limiter);
 
 SweepLaunch sweep_launcher(int scheme, int riemann, int limiter, int precision)
 {
     const int r = (riemann == HLLC) ? HLL : riemann; // HLLC/Riemann_solver.cpp is HLL
     const bool fast = (precision == IBTFO_PRECISION_FP64_FAST);
+    if (precision == IBTFO_PRECISION_FP32_COMPENSATED)
+    {
+        switch (scheme)
+        {
+        case MHM: return sweep_launcher_mhm_f32(r, limiter);
+        case GODUNOV: return sweep_launcher_godunov_f32(r, limiter);
+        default: return sweep_launcher_muscl_f32(r, limiter);
+        }
+    }
     switch (scheme)
     {
     case MHM: return fast ? sweep_launcher_mhm_fast(r, limiter) : sweep_launcher_mhm(r, limiter);
@@ -151,10 +163,12 @@ ibtfo_status ibtfo_create(const ibtfo_config *cfg, ibtfo_case **out)
         return fail(IBTFO_EINVAL, "grid too large (n_x, n_y <= 262144 and at most 2^31 cells)");
     if (!(k.hi_x > k.lo_x) || !(k.hi_y > k.lo_y) || !(k.gamma > 1.0) || !(k.cfl_number > 0.0))
         return fail(IBTFO_EINVAL, "need hi > lo, gamma > 1, cfl_number > 0");
-    if (k.scheme < 0 || k.scheme > 2 || k.riemann < 0 || k.riemann > 3 || k.limiter < 0 || k.limiter > 1 ||
+    if (k.scheme < 0 || k.scheme > 2 || k.riemann < 0 || k.riemann > 4 || k.limiter < 0 || k.limiter > 1 ||
         k.boundary < 0 || k.boundary > 5 || k.global_boundary < 0 || k.global_boundary > 1 || k.precision < 0 ||
-        k.precision > 1)
+        k.precision > 2)
         return fail(IBTFO_EINVAL, "unknown scheme/riemann/limiter/boundary/global_boundary/precision key");
+    if (k.precision == IBTFO_PRECISION_FP32_COMPENSATED && k.riemann == IBTFO_RIEMANN_PVRS)
+        return fail(IBTFO_EINVAL, "PVRS is available in the FP64 precisions only");
     if (k.global_boundary == IBTFO_GLOBAL_PERIODIC && (k.n_x < k.num_ghost_cell || k.n_y < k.num_ghost_cell))
         return fail(IBTFO_EINVAL, "periodic boundaries need n_x, n_y >= num_ghost_cell");
 
@@ -176,6 +190,7 @@ ibtfo_status ibtfo_create(const ibtfo_config *cfg, ibtfo_case **out)
     g.Hi = -g.dx * g.ng + k.lo_y + g.dx / 2;
     g.gamma = k.gamma;
     g.cfl = k.cfl_number;
+    g.f32 = (k.precision == IBTFO_PRECISION_FP32_COMPENSATED) ? 1 : 0;
     c->nblocks = ((k.n_x + TILE_X - 1) / TILE_X) * ((k.n_y + TILE_Y - 1) / TILE_Y);
     c->sweep = sweep_launcher(k.scheme, k.riemann, k.limiter, k.precision);
 
@@ -510,7 +525,7 @@ __global__ void export_unew_kernel(GridDesc g, const double *cur, const double *
     bool in = i >= g.ng && i < g.ng + g.n_x && j >= g.ng && j < g.ng + g.n_y;
     const double *b = in ? ((type[o] == 0) ? cur : prev) : ring_src;
     for (int k = 0; k < 4; k++)
-        aos[q * 4 + k] = b[k * g.plane + o];
+        aos[q * 4 + k] = state_ld(b, k, o, g);
 }
 
 ibtfo_status ibtfo_get_state(ibtfo_case *c, double *u_old, double *u_new)

@@ -58,7 +58,34 @@ struct GridDesc
     double dx, dy;   // update spacings: Psy_L/N_x and Psy_H/N_y
     double Li, Hi;   // coordinate of cell (0,0) centre: x_i = Li + i*dx, y_j = Hi + j*dx
     double gamma, cfl;
+    int f32;         // state stored as float (hi, lo) pairs: planes 0-3 hi, 4-7 lo
 };
+
+// One conserved component of one cell of a state buffer, as a double.  FP64
+// states hold four double planes; FP32 compensated states hold eight float
+// planes with the same byte size (hi then lo), value = hi + lo.
+__device__ __forceinline__ double state_ld(const double *b, int k, long long o, const GridDesc &g)
+{
+    if (g.f32)
+    {
+        const float *f = reinterpret_cast<const float *>(b);
+        return (double)f[k * g.plane + o] + (double)f[(4 + k) * g.plane + o];
+    }
+    return b[k * g.plane + o];
+}
+
+__device__ __forceinline__ void state_st(double *b, int k, long long o, double v, const GridDesc &g)
+{
+    if (g.f32)
+    {
+        float *f = reinterpret_cast<float *>(b);
+        const float hi = (float)v;
+        f[k * g.plane + o] = hi;
+        f[(4 + k) * g.plane + o] = (float)(v - (double)hi);
+        return;
+    }
+    b[k * g.plane + o] = v;
+}
 
 struct SweepArgs
 {

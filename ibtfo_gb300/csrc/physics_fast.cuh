@@ -1,13 +1,16 @@
-// FP64 physics with fewer FP64 instructions, for the `fp64_fast` precision.
+// Physics with fewer floating-point instructions, templated on the
+// arithmetic type: T = double for the `fp64_fast` precision, T = float for
+// the FP32 compensated precision form.
 //
 // Same algorithm and branches as physics.cuh (the reference's), evaluated
 // with shared reciprocals, precomputed gamma constants, fused multiply-adds
-// (this header is compiled with contraction on) and the limiter's sign and
-// magnitude tests done on integer bit patterns.  The results differ from the
-// reference in rounding only: relative differences of order 1e-15 per step,
-// inside the plain path's 1e-12 parity bar (checked by the GPU parity tests
-// for this precision).  Degenerate inputs (zero or non-finite density or
-// pressure) may produce a different mix of inf and NaN than the reference.
+// (these units are compiled with contraction on) and the limiter's sign and
+// magnitude tests done on integer bit patterns.  For T = double the results
+// differ from the reference in rounding only: relative differences of order
+// 1e-15 per step, inside the plain path's 1e-12 parity bar (checked by the GPU
+// parity tests for this precision).  Degenerate inputs (zero or non-finite
+// density or pressure) may produce a different mix of inf and NaN than the
+// reference.
 #pragma once
 
 #include "physics.cuh"
@@ -15,21 +18,21 @@
 namespace ibtfo {
 
 // gamma-dependent constants, computed once per thread
+template <typename T>
 struct GasConst
 {
-    double g, gm1, c1, c2, g_over_gm1;
+    T g, gm1, c1, c2;
     __device__ __forceinline__ explicit GasConst(double gamma)
     {
-        g = gamma;
-        gm1 = gamma - 1;
-        c1 = (gamma + 1) / (2 * gamma); // HLL wave speed: (g+1)/(2g) * p*/p + (g-1)/(2g)
-        c2 = (gamma - 1) / (2 * gamma);
-        g_over_gm1 = gamma / (gamma - 1);
+        g = (T)gamma;
+        gm1 = (T)(gamma - 1);
+        c1 = (T)((gamma + 1) / (2 * gamma)); // HLL wave speed: (g+1)/(2g) * p*/p + (g-1)/(2g)
+        c2 = (T)((gamma - 1) / (2 * gamma));
     }
 };
 
 // 1/x: hardware seed + two Newton steps (within an ulp of the rounded value)
-__device__ __forceinline__ double rcp_nr(double x)
+__device__ __forceinline__ double rcp_t(double x)
 {
     double y;
     asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
@@ -38,11 +41,16 @@ __device__ __forceinline__ double rcp_nr(double x)
     e = fma(-x, y, 1.0);
     return fma(y, e, y);
 }
+__device__ __forceinline__ float rcp_t(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double sqrt_t(double x) { return sqrt(x); }
+__device__ __forceinline__ float sqrt_t(float x) { return sqrtf(x); }
+__device__ __forceinline__ double fma_t(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
 
 // minmod with the sign and magnitude tests on the integer pipe:
 // (a*b > 0) ? (|a| > |b| ? b : a) : 0, treating a product that would
-// underflow to zero as positive (only for |a|,|b| below ~1e-154)
-__device__ __forceinline__ double minmod_int(double a, double b)
+// underflow to zero as positive (only for |a|,|b| below ~1e-154 in double)
+__device__ __forceinline__ double minmod_t(double a, double b)
 {
     const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
     const long long ma = ia & 0x7fffffffffffffffLL, mb = ib & 0x7fffffffffffffffLL;
@@ -50,10 +58,26 @@ __device__ __forceinline__ double minmod_int(double a, double b)
                     mb <= 0x7ff0000000000000LL;
     return ok ? ((ma > mb) ? b : a) : 0.0;
 }
+__device__ __forceinline__ float minmod_t(float a, float b)
+{
+    const int ia = __float_as_int(a), ib = __float_as_int(b);
+    const int ma = ia & 0x7fffffff, mb = ib & 0x7fffffff;
+    const bool ok = ((ia ^ ib) >= 0) && ma != 0 && mb != 0 && ma <= 0x7f800000 && mb <= 0x7f800000;
+    return ok ? ((ma > mb) ? b : a) : 0.0f;
+}
 
-template <int SCH, int LIM>
-__device__ __forceinline__ void face_states_fast(const double c0[4], const double c1[4], const double c2[4],
-                                                 const double c3[4], double UL[4], double UR[4])
+// VanLeer as the reference macro expands (physics.cuh lim_vanleer)
+template <typename T>
+__device__ __forceinline__ T vanleer_t(T a, T P, T Q)
+{
+    T b = P - Q;
+    T r = (a + (T)1e-7) / (b + (T)1e-7);
+    return (r > 0) ? ((r * r + r) * P - Q / (r * r + 1)) : (T)0;
+}
+
+template <typename T, int SCH, int LIM>
+__device__ __forceinline__ void face_states_fast(const T c0[4], const T c1[4], const T c2[4], const T c3[4], T UL[4],
+                                                 T UR[4])
 {
 #pragma unroll
     for (int k = 0; k < 4; k++)
@@ -65,43 +89,44 @@ __device__ __forceinline__ void face_states_fast(const double c0[4], const doubl
         }
         else if (LIM == VANLEER)
         {
-            UL[k] = c1[k] + half_slope<LIM>(c1[k], c0[k], c2[k], c1[k]);
-            UR[k] = c2[k] - half_slope<LIM>(c3[k], c2[k], c2[k], c1[k]);
+            UL[k] = c1[k] + (T)0.5 * vanleer_t<T>(c1[k] - c0[k], c2[k], c1[k]);
+            UR[k] = c2[k] - (T)0.5 * vanleer_t<T>(c3[k] - c2[k], c2[k], c1[k]);
         }
         else
         {
-            const double dm = c1[k] - c0[k], d0 = c2[k] - c1[k], dp = c3[k] - c2[k];
-            UL[k] = fma(0.5, minmod_int(dm, d0), c1[k]);
-            UR[k] = fma(-0.5, minmod_int(dp, d0), c2[k]);
+            const T dm = c1[k] - c0[k], d0 = c2[k] - c1[k], dp = c3[k] - c2[k];
+            UL[k] = fma_t((T)0.5, minmod_t(dm, d0), c1[k]);
+            UR[k] = fma_t((T)-0.5, minmod_t(dp, d0), c2[k]);
         }
     }
 }
 
 // primitive variables and sound speed of one state
+template <typename T>
 struct Prim
 {
-    double r, ir, un, ut, p, a;
+    T r, ir, un, ut, p, a;
 };
 
-// n = index of the face-normal momentum (1 for X, 2 for Y)
-template <int NRM>
-__device__ __forceinline__ Prim prim_fast(const double U[4], const GasConst &K)
+// NRM = index of the face-normal momentum (1 for X, 2 for Y)
+template <typename T, int NRM>
+__device__ __forceinline__ Prim<T> prim_fast(const T U[4], const GasConst<T> &K)
 {
-    Prim s;
+    Prim<T> s;
     s.r = U[0];
-    s.ir = rcp_nr(U[0]);
+    s.ir = rcp_t(U[0]);
     s.un = U[NRM] * s.ir;
     s.ut = U[3 - NRM] * s.ir;
-    s.p = K.gm1 * (U[3] - 0.5 * s.r * (s.un * s.un + s.ut * s.ut));
-    s.a = sqrt(K.g * s.p * s.ir);
+    s.p = K.gm1 * (U[3] - (T)0.5 * s.r * (s.un * s.un + s.ut * s.ut));
+    s.a = sqrt_t(K.g * s.p * s.ir);
     return s;
 }
 
 // physical flux normal to the face; components in state order
-template <int NRM>
-__device__ __forceinline__ void flux_fast(const double U[4], const Prim &s, double F[4])
+template <typename T, int NRM>
+__device__ __forceinline__ void flux_fast(const T U[4], const Prim<T> &s, T F[4])
 {
-    const double m = s.r * s.un;
+    const T m = s.r * s.un;
     F[0] = m;
     F[NRM] = m * s.un + s.p;
     F[3 - NRM] = m * s.ut;
@@ -110,19 +135,19 @@ __device__ __forceinline__ void flux_fast(const double U[4], const Prim &s, doub
 
 // HLL face flux (HLL/Riemann_solver.cpp:131-169 X, :202-235 Y).  For Y,
 // returns false when S_D >= 0 (the reference keeps the X-face flux).
-template <int NRM>
-__device__ __forceinline__ bool hll_fast(const double UL[4], const double UR[4], const GasConst &K, double F[4])
+template <typename T, int NRM>
+__device__ __forceinline__ bool hll_fast(const T UL[4], const T UR[4], const GasConst<T> &K, T F[4])
 {
-    const Prim L = prim_fast<NRM>(UL, K), R = prim_fast<NRM>(UR, K);
-    const double p_star = 0.5 * (L.p + R.p) + 0.125 * (L.un - R.un) * ((L.r + R.r) * (L.a + R.a));
-    const double t = K.c1 * p_star;
-    const double S_L = L.un - L.a * sqrt(fma(t, rcp_nr(L.p), K.c2));
-    const double S_R = R.un + R.a * sqrt(fma(t, rcp_nr(R.p), K.c2));
+    const Prim<T> L = prim_fast<T, NRM>(UL, K), R = prim_fast<T, NRM>(UR, K);
+    const T p_star = (T)0.5 * (L.p + R.p) + (T)0.125 * (L.un - R.un) * ((L.r + R.r) * (L.a + R.a));
+    const T t = K.c1 * p_star;
+    const T S_L = L.un - L.a * sqrt_t(fma_t(t, rcp_t(L.p), K.c2));
+    const T S_R = R.un + R.a * sqrt_t(fma_t(t, rcp_t(R.p), K.c2));
     if (NRM == 2 && S_L >= 0)
         return false;
-    double FL[4], FR[4];
-    flux_fast<NRM>(UL, L, FL);
-    flux_fast<NRM>(UR, R, FR);
+    T FL[4], FR[4];
+    flux_fast<T, NRM>(UL, L, FL);
+    flux_fast<T, NRM>(UR, R, FR);
     if (S_L >= 0)
     {
 #pragma unroll
@@ -137,7 +162,7 @@ __device__ __forceinline__ bool hll_fast(const double UL[4], const double UR[4],
     }
     else
     {
-        const double inv = rcp_nr(S_R - S_L), srsl = S_R * S_L;
+        const T inv = rcp_t(S_R - S_L), srsl = S_R * S_L;
 #pragma unroll
         for (int k = 0; k < 4; k++)
             F[k] = (S_R * FL[k] - S_L * FR[k] + srsl * (UR[k] - UL[k])) * inv;
@@ -145,56 +170,141 @@ __device__ __forceinline__ bool hll_fast(const double UL[4], const double UR[4],
     return true;
 }
 
-// MHM predictor with h2 = 0.5 * dt / h precomputed
-template <int NRM>
-__device__ __forceinline__ void mhm_predict_fast(double UL[4], double UR[4], const GasConst &K, double h2)
+// Steger-Warming flux-vector splitting (StegerWarming/Riemann_solver.cpp:173-234
+// X, :262-325 Y): F = F+(U_L) + F-(U_R) with lambda+- = (lambda +- sqrt(lambda^2 + delta^2))/2
+template <typename T, int NRM, int SIGN>
+__device__ __forceinline__ void sw_split(const T U[4], const GasConst<T> &K, T F[4])
 {
-    double FL[4], FR[4];
-    const Prim L = prim_fast<NRM>(UL, K), R = prim_fast<NRM>(UR, K);
-    flux_fast<NRM>(UL, L, FL);
-    flux_fast<NRM>(UR, R, FR);
+    const Prim<T> s = prim_fast<T, NRM>(U, K);
+    const T d2 = (T)1e-12; // delta = 1e-6 (:193)
+    auto lam = [&](T x) { return (T)0.5 * (x + (T)SIGN * sqrt_t(x * x + d2)); };
+    const T l1 = lam(s.un), l3 = lam(s.un - s.a), l4 = lam(s.un + s.a);
+    const T h = s.p / K.gm1 * s.ir + (T)0.5 * (s.un * s.un + s.ut * s.ut) + s.p * s.ir; // e + |u|^2/2 + p/rho
+    const T w = s.r / ((T)2 * K.g);
+    F[0] = w * ((T)2 * K.gm1 * l1 + l3 + l4);
+    F[NRM] = w * ((T)2 * K.gm1 * s.un * l1 + (s.un - s.a) * l3 + (s.un + s.a) * l4);
+    F[3 - NRM] = w * s.ut * ((T)2 * K.gm1 * l1 + l3 + l4);
+    F[3] = w * (K.gm1 * (s.un * s.un + s.ut * s.ut) * l1 + (h - s.a * s.un) * l3 + (h + s.a * s.un) * l4);
+}
+
+template <typename T, int NRM>
+__device__ __forceinline__ void sw_fast(const T UL[4], const T UR[4], const GasConst<T> &K, T F[4])
+{
+    T Fp[4], Fm[4];
+    sw_split<T, NRM, 1>(UL, K, Fp);
+    sw_split<T, NRM, -1>(UR, K, Fm);
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+        F[k] = Fp[k] + Fm[k];
+}
+
+// Contact-restoring HLLC (Toro, Riemann Solvers and Numerical Methods for
+// Fluid Dynamics, 3rd ed., eqs. 10.37-10.39 and 10.71-10.73), offered under its
+// own key: the reference's HLLC directory holds the HLL solver.  Wave speeds
+// from the PVRS pressure estimate with Toro's q_K = 1 for p* <= p_K; no face
+// leaves its flux slot unchanged (always returns a flux).
+template <typename T, int NRM>
+__device__ __forceinline__ void hllc_toro(const T UL[4], const T UR[4], const GasConst<T> &K, T F[4])
+{
+    const Prim<T> L = prim_fast<T, NRM>(UL, K), R = prim_fast<T, NRM>(UR, K);
+    T p_star = (T)0.5 * (L.p + R.p) + (T)0.125 * (L.un - R.un) * ((L.r + R.r) * (L.a + R.a));
+    p_star = p_star > (T)0 ? p_star : (T)0;
+    const T t = K.c1 * p_star;
+    const T qL = (p_star > L.p) ? sqrt_t(fma_t(t, rcp_t(L.p), K.c2)) : (T)1;
+    const T qR = (p_star > R.p) ? sqrt_t(fma_t(t, rcp_t(R.p), K.c2)) : (T)1;
+    const T S_L = L.un - L.a * qL, S_R = R.un + R.a * qR;
+    T FL[4], FR[4];
+    flux_fast<T, NRM>(UL, L, FL);
+    flux_fast<T, NRM>(UR, R, FR);
+    if (S_L >= 0)
+    {
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            F[k] = FL[k];
+        return;
+    }
+    if (S_R <= 0)
+    {
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            F[k] = FR[k];
+        return;
+    }
+    const T mL = L.r * (S_L - L.un), mR = R.r * (S_R - R.un);
+    const T S_s = (R.p - L.p + L.un * mL - R.un * mR) * rcp_t(mL - mR);
+    const bool left = S_s >= 0;
+    const Prim<T> &s = left ? L : R;
+    const T *U = left ? UL : UR;
+    const T *Fk = left ? FL : FR;
+    const T S = left ? S_L : S_R, m = left ? mL : mR;
+    const T fac = m * rcp_t(S - S_s);
+    T Us[4];
+    Us[0] = fac;
+    Us[NRM] = fac * S_s;
+    Us[3 - NRM] = fac * s.ut;
+    Us[3] = fac * (U[3] * s.ir + (S_s - s.un) * (S_s + s.p * rcp_t(m)));
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+        F[k] = Fk[k] + S * (Us[k] - U[k]);
+}
+
+// MHM predictor with h2 = 0.5 * dt / h precomputed
+template <typename T, int NRM>
+__device__ __forceinline__ void mhm_predict_fast(T UL[4], T UR[4], const GasConst<T> &K, T h2)
+{
+    T FL[4], FR[4];
+    const Prim<T> L = prim_fast<T, NRM>(UL, K), R = prim_fast<T, NRM>(UR, K);
+    flux_fast<T, NRM>(UL, L, FL);
+    flux_fast<T, NRM>(UR, R, FR);
 #pragma unroll
     for (int k = 0; k < 4; k++)
     {
-        const double d = h2 * (FL[k] - FR[k]);
+        const T d = h2 * (FL[k] - FR[k]);
         UL[k] += d;
         UR[k] += d;
     }
 }
 
-template <int SCH, int RIE, int LIM>
-__device__ __forceinline__ void x_face_fast(const double c0[4], const double c1[4], const double c2[4],
-                                            const double c3[4], const GasConst &K, double dt, double h2, double F[4])
+template <typename T, int SCH, int RIE, int LIM>
+__device__ __forceinline__ void x_face_fast(const T c0[4], const T c1[4], const T c2[4], const T c3[4],
+                                            const GasConst<T> &K, T h2, T F[4])
 {
-    double UL[4], UR[4];
-    face_states_fast<SCH, LIM>(c0, c1, c2, c3, UL, UR);
+    T UL[4], UR[4];
+    face_states_fast<T, SCH, LIM>(c0, c1, c2, c3, UL, UR);
     if (SCH == MHM)
-        mhm_predict_fast<1>(UL, UR, K, h2);
-    if (RIE == PVRS)
-        pvrs_x(UL, UR, K.g, F);
-    else if (RIE == SW)
-        sw_x(UL, UR, K.g, F);
+        mhm_predict_fast<T, 1>(UL, UR, K, h2);
+    if constexpr (RIE == PVRS)
+        pvrs_x(UL, UR, (double)K.g, F); // double only (FP32 form rejects PVRS)
+    else if constexpr (RIE == SW)
+        sw_fast<T, 1>(UL, UR, K, F);
+    else if constexpr (RIE == HLLCT)
+        hllc_toro<T, 1>(UL, UR, K, F);
     else
-        hll_fast<1>(UL, UR, K, F);
+        hll_fast<T, 1>(UL, UR, K, F);
 }
 
-template <int SCH, int RIE, int LIM>
-__device__ __forceinline__ int y_face_fast(const double c0[4], const double c1[4], const double c2[4],
-                                           const double c3[4], const GasConst &K, double dt, double h2, double G[4],
-                                           double *stray)
+template <typename T, int SCH, int RIE, int LIM>
+__device__ __forceinline__ int y_face_fast(const T c0[4], const T c1[4], const T c2[4], const T c3[4],
+                                           const GasConst<T> &K, T h2, T G[4], T *stray)
 {
-    double UD[4], UU[4];
-    face_states_fast<SCH, LIM>(c0, c1, c2, c3, UD, UU);
+    T UD[4], UU[4];
+    face_states_fast<T, SCH, LIM>(c0, c1, c2, c3, UD, UU);
     if (SCH == MHM)
-        mhm_predict_fast<2>(UD, UU, K, h2);
-    if (RIE == PVRS)
-        return pvrs_y(UD, UU, K.g, G, stray);
-    if (RIE == SW)
+        mhm_predict_fast<T, 2>(UD, UU, K, h2);
+    if constexpr (RIE == PVRS)
+        return pvrs_y(UD, UU, (double)K.g, G, stray);
+    else if constexpr (RIE == SW)
     {
-        sw_y(UD, UU, K.g, G);
+        sw_fast<T, 2>(UD, UU, K, G);
         return 0;
     }
-    return hll_fast<2>(UD, UU, K, G) ? 0 : 0xF;
+    else if constexpr (RIE == HLLCT)
+    {
+        hllc_toro<T, 2>(UD, UU, K, G);
+        return 0;
+    }
+    else
+        return hll_fast<T, 2>(UD, UU, K, G) ? 0 : 0xF;
 }
 
 } // namespace ibtfo

@@ -11,6 +11,7 @@ SweepLaunch sweep_launcher_godunov_fast(int riemann, int limiter)
     {
     case PVRS: return vl ? &launch_sweep<GODUNOV, PVRS, VANLEER, 1> : &launch_sweep<GODUNOV, PVRS, MINMOD, 1>;
     case SW: return vl ? &launch_sweep<GODUNOV, SW, VANLEER, 1> : &launch_sweep<GODUNOV, SW, MINMOD, 1>;
+    case HLLCT: return vl ? &launch_sweep<GODUNOV, HLLCT, VANLEER, 1> : &launch_sweep<GODUNOV, HLLCT, MINMOD, 1>;
     default: return vl ? &launch_sweep<GODUNOV, HLL, VANLEER, 1> : &launch_sweep<GODUNOV, HLL, MINMOD, 1>;
     }
 }

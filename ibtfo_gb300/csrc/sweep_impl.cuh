@@ -147,10 +147,10 @@ __device__ __forceinline__ void cell_stats(const double v[4], double gam, double
 }
 
 // the same statistics with a shared reciprocal (fp64_fast)
-__device__ __forceinline__ void cell_stats_fast(const double v[4], const GasConst &K, double dxdy, double &amax,
-                                                double &umax, double &vmax, double &mass, int &nans)
+__device__ __forceinline__ void cell_stats_fast(const double v[4], const GasConst<double> &K, double dxdy,
+                                                double &amax, double &umax, double &vmax, double &mass, int &nans)
 {
-    const double ir = rcp_nr(v[0]);
+    const double ir = rcp_t(v[0]);
     const double u = v[1] * ir, w = v[2] * ir;
     const double p = K.gm1 * (v[3] - 0.5 * v[0] * (u * u + w * w));
     const double a = pow_half(K.g * p * ir);
@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_kernel(const SweepArgs a
     __syncthreads();
 
     const double gam = g.gamma;
-    const GasConst K(gam);
+    const GasConst<double> K(gam);
     const double hx2 = 0.5 * dt / g.dx, hy2 = 0.5 * dt / g.dy; // fp64_fast MHM predictor
     constexpr int NXF = (TX + 1) * (TY + 1);
     constexpr int NYF = TX * (TY + 1);
@@ -225,8 +225,8 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_kernel(const SweepArgs a
                 c2[k] = sU[k][r + 1][fc + 2];
                 c3[k] = sU[k][r + 1][fc + 3];
             }
-            if (FAST)
-                x_face_fast<SCH, RIE, LIM>(c0, c1, c2, c3, K, dt, hx2, f);
+            if (FAST || RIE == HLLCT)
+                x_face_fast<double, SCH, RIE, LIM>(c0, c1, c2, c3, K, hx2, f);
             else
                 x_face<SCH, RIE, LIM>(c0, c1, c2, c3, gam, dt, g.dx, f);
 #pragma unroll
@@ -246,7 +246,7 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_kernel(const SweepArgs a
                 c3[k] = sU[k][r + 3][c + 2];
             }
             double stray = 0.0;
-            int keep = FAST ? y_face_fast<SCH, RIE, LIM>(c0, c1, c2, c3, K, dt, hy2, f, &stray)
+            int keep = (FAST || RIE == HLLCT) ? y_face_fast<double, SCH, RIE, LIM>(c0, c1, c2, c3, K, hy2, f, &stray)
                             : y_face<SCH, RIE, LIM>(c0, c1, c2, c3, gam, dt, g.dy, f, &stray);
 #pragma unroll
             for (int k = 0; k < 4; k++)

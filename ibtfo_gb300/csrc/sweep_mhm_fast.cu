@@ -11,6 +11,7 @@ SweepLaunch sweep_launcher_mhm_fast(int riemann, int limiter)
     {
     case PVRS: return vl ? &launch_sweep<MHM, PVRS, VANLEER, 1> : &launch_sweep<MHM, PVRS, MINMOD, 1>;
     case SW: return vl ? &launch_sweep<MHM, SW, VANLEER, 1> : &launch_sweep<MHM, SW, MINMOD, 1>;
+    case HLLCT: return vl ? &launch_sweep<MHM, HLLCT, VANLEER, 1> : &launch_sweep<MHM, HLLCT, MINMOD, 1>;
     default: return vl ? &launch_sweep<MHM, HLL, VANLEER, 1> : &launch_sweep<MHM, HLL, MINMOD, 1>;
     }
 }

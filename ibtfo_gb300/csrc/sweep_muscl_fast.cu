@@ -11,6 +11,7 @@ SweepLaunch sweep_launcher_muscl_fast(int riemann, int limiter)
     {
     case PVRS: return vl ? &launch_sweep<MUSCL, PVRS, VANLEER, 1> : &launch_sweep<MUSCL, PVRS, MINMOD, 1>;
     case SW: return vl ? &launch_sweep<MUSCL, SW, VANLEER, 1> : &launch_sweep<MUSCL, SW, MINMOD, 1>;
+    case HLLCT: return vl ? &launch_sweep<MUSCL, HLLCT, VANLEER, 1> : &launch_sweep<MUSCL, HLLCT, MINMOD, 1>;
     default: return vl ? &launch_sweep<MUSCL, HLL, VANLEER, 1> : &launch_sweep<MUSCL, HLL, MINMOD, 1>;
     }
 }

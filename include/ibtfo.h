@@ -38,7 +38,16 @@ typedef enum ibtfo_status {
 /* selection keys: the reference Makefile slots Scheme / Riemann / Limiter /
  * Boundary (Test/Sod/Makefile:1-7) and the per-case Global_Boundary plug-in */
 enum { IBTFO_SCHEME_MUSCL = 0, IBTFO_SCHEME_MHM = 1, IBTFO_SCHEME_GODUNOV = 2 };
-enum { IBTFO_RIEMANN_HLL = 0, IBTFO_RIEMANN_HLLC = 1, IBTFO_RIEMANN_PVRS = 2, IBTFO_RIEMANN_STEGER_WARMING = 3 };
+/* HLLC is the reference's HLLC directory, whose solver is HLL (including the
+ * Y-face slot reuse); HLLC_TORO is a contact-restoring HLLC with no
+ * reference counterpart */
+enum {
+    IBTFO_RIEMANN_HLL = 0,
+    IBTFO_RIEMANN_HLLC = 1,
+    IBTFO_RIEMANN_PVRS = 2,
+    IBTFO_RIEMANN_STEGER_WARMING = 3,
+    IBTFO_RIEMANN_HLLC_TORO = 4
+};
 enum { IBTFO_LIMITER_MINMOD = 0, IBTFO_LIMITER_VANLEER = 1 };
 enum {
     IBTFO_BOUNDARY_REGULAR = 0,
@@ -51,10 +60,13 @@ enum {
 enum { IBTFO_GLOBAL_WALLS = 0, IBTFO_GLOBAL_PERIODIC = 1 };
 /* arithmetic of the step: FP64 evaluating the reference's expressions in
  * their order (bit-for-bit with the reference except where the library
- * pow(x, 0.5) and sqrt differ in the last bit), or FP64 with shared
+ * pow(x, 0.5) and sqrt differ in the last bit); FP64 with shared
  * reciprocals and fused multiply-adds (rounding-level differences, well
- * inside a 1e-12 relative bar) */
-enum { IBTFO_PRECISION_FP64 = 0, IBTFO_PRECISION_FP64_FAST = 1 };
+ * inside a 1e-12 relative bar); or the precision form: FP32 face
+ * reconstruction, Riemann solves and fluxes with the state held as FP32
+ * (hi, lo) pairs updated by an error-free sum, FP64 for the mass sum, dt and
+ * the ghost-fluid fill (HLL/HLLC and Steger-Warming) */
+enum { IBTFO_PRECISION_FP64 = 0, IBTFO_PRECISION_FP64_FAST = 1, IBTFO_PRECISION_FP32_COMPENSATED = 2 };
 
 /* Case parameters: the numeric .inp keys the reference driver reads
  * (Test/Sod/Sod.cpp:34-48) plus the slot selections. */
@@ -156,9 +168,9 @@ int ibtfo_inp_get(const ibtfo_inp *p, const char *key, double def, double *value
 int ibtfo_inp_get_string(const ibtfo_inp *p, const char *key, char *buf, int size);
 /* numeric keys with the reference drivers' defaults (Test/Sod/Sod.cpp:34-48)
  * and the slot keys Scheme (MUSCL|MHM|Godunov), Riemann (HLL|HLLC|PVRS|
- * StegerWarming), Limiter (minmod|VanLeer), Boundary (Regular|IDWBaseGFM|
+ * StegerWarming|HLLC_Toro), Limiter (minmod|VanLeer), Boundary (Regular|IDWBaseGFM|
  * LinearBaseGFM|RiemannBaseGFM|BCGFM|HBCGFM), Global_Boundary (Walls|
- * Periodic), Precision (FP64|FP64_FAST) */
+ * Periodic), Precision (FP64|FP64_FAST|FP32_COMPENSATED) */
 ibtfo_status ibtfo_config_from_inp(const ibtfo_inp *p, ibtfo_config *cfg);
 
 /* Case plug-ins (the reference's per-case Level_Set_function and Initialize

@@ -1,0 +1,93 @@
+"""Secondary checks against exact solutions (GPU).
+
+* The Sod tube (400x100, t_end 0.2) for every scheme and solver against the
+  exact Riemann solution (tests/exact_riemann.py): L1 density error per cell
+  <= 3e-3 for the second-order schemes and <= 1.2e-2 for Godunov (the
+  reference's own solvers land at 1.7e-3 .. 2.1e-3 and 6.9e-3 .. 9.3e-3).
+* The contact-restoring HLLC keeps a stationary contact discontinuity
+  exactly; HLL smears it (the reason the vortex workload uses HLLC_Toro).
+* The FP32 compensated form on the isentropic vortex: within 1e-5 (L1
+  density) of the FP64 path and as close to the exact solution as FP64.
+"""
+import numpy as np
+import pytest
+
+from exact_riemann import sample
+
+ib = pytest.importorskip("ibtfo_gb300")
+from ibtfo_gb300 import cases  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def simulated_time(p0, p):
+    # now_t advances by the dt computed after each step (Test/Sod/Sod.cpp:176):
+    # the time actually integrated is dt_0 + ... + dt_{n-1}
+    return p["now_t"] - p["dt"] + p0["dt"]
+
+
+@pytest.mark.parametrize("riemann", ["HLL", "HLLC", "PVRS", "StegerWarming", "HLLC_Toro"])
+@pytest.mark.parametrize("scheme", ["MUSCL", "MHM", "Godunov"])
+def test_sod_tube_against_exact_solution(scheme, riemann):
+    w = cases.sod_tube()
+    w.scheme, w.riemann = scheme, riemann
+    g = w.grid
+    phi, u0 = cases.sod_x(g)
+    with ib.Case.from_workload(w, precision="fp64_fast") as c:
+        c.setup_geometry(phi)
+        c.set_state(u0)
+        p0 = c.progress()
+        p = c.run()
+        T = simulated_time(p0, p)
+        u = c.get_state().reshape(g.N, g.M, 4)
+    x, _ = g.coords()
+    xs = x[0, g.ng:-g.ng]
+    ex = sample((1.0, 0.0, 1.0), (0.125, 0.0, 0.1), (xs - 0.5) / T)[:, 0]
+    bar = 1.2e-2 if scheme == "Godunov" else 3e-3
+    for j in (g.ng, g.N // 2, g.N - g.ng - 1):
+        rho = u[j, g.ng:-g.ng, 0]
+        err = float(np.abs(rho - ex).mean())
+        assert err <= bar, (j, err)
+
+
+@pytest.mark.parametrize("riemann,exact", [("HLLC_Toro", True), ("HLL", False)])
+def test_stationary_contact(riemann, exact):
+    g = cases.Grid(128, 16, 2, 0.0, 0.0, 1.0, 0.125)
+    w = cases.Workload("contact", g, 1.4, 0.5, 1.0, "MUSCL", riemann, "minmod", "Regular")
+    phi, u0 = cases.sod_x(g, left=(1.0, 0.0, 0.0, 1.0), right=(0.25, 0.0, 0.0, 1.0))
+    with ib.Case.from_workload(w) as c:
+        c.setup_geometry(phi)
+        c.set_state(u0)
+        c.advance(50)
+        u = c.get_state().reshape(g.N, g.M, 4)
+    rho0 = u0.reshape(g.N, g.M, 4)[g.ng:-g.ng, g.ng:-g.ng, 0]
+    d = float(np.abs(u[g.ng:-g.ng, g.ng:-g.ng, 0] - rho0).max())
+    if exact:
+        assert d <= 1e-12, d
+    else:
+        assert d > 1e-3, d
+
+
+def test_fp32c_isentropic_vortex_hllc():
+    w = cases.vortex_periodic(256)
+    g = w.grid
+    phi, u0 = cases.isentropic_vortex(g)
+    res = {}
+    for prec in ("fp64_fast", "fp32c"):
+        with ib.Case.from_workload(w, precision=prec, t_end=1e300, max_iter=2 ** 31 - 1) as c:
+            c.setup_geometry(phi)
+            c.set_state(u0)
+            p0 = c.progress()
+            c.advance(400)
+            p = c.progress()
+            assert p["nan_cells"] == 0
+            res[prec] = (c.get_state().reshape(g.N, g.M, 4)[g.ng:-g.ng, g.ng:-g.ng, 0], simulated_time(p0, p))
+    (r64, t64), (r32, t32) = res["fp64_fast"], res["fp32c"]
+    assert abs(t32 - t64) <= 1e-6 * t64
+    err = float(np.abs(r32 - r64).sum() / np.abs(r64).sum())
+    assert err <= 1e-5, err
+    _, ex = cases.isentropic_vortex(g, t=t64)
+    rex = ex.reshape(g.N, g.M, 4)[g.ng:-g.ng, g.ng:-g.ng, 0]
+    e64 = float(np.abs(r64 - rex).sum() / np.abs(rex).sum())
+    e32 = float(np.abs(r32 - rex).sum() / np.abs(rex).sum())
+    assert abs(e32 - e64) <= 0.01 * e64, (e32, e64)
