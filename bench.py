@@ -49,6 +49,21 @@ def workload():
 PRECISION = os.environ.get("IBTFO_BENCH_PRECISION", "fp64_fast")
 
 
+def profile_run(args):
+    """Plain stepping of one workload (for profiler captures): set up, warm up,
+    run `--steps` steps, print ms/step.  No CPU leg, no extra legs."""
+    import torch
+    from ibtfo_gb300 import cases
+    w = cases.vortex_periodic(args.size) if args.workload == "vortex" else cases.inclined_channel(args.size,
+                                                                                                  args.size // 2)
+    inputs = vortex_inputs if args.workload == "vortex" else channel_inputs
+    r = gpu_arm(args, 0, 1, 0, precision=args.precision, e2e=False, w=w, inputs=inputs, steps=args.steps)
+    print(json.dumps({"workload": w.name, "precision": args.precision, "steps": args.steps,
+                      "ms_per_step": r["step_ms"] / args.steps, "sweep_ms": r["sweep_ms"] / args.steps,
+                      "Gcell_updates_per_s": w.grid.n_x * w.grid.n_y * args.steps / (r["step_ms"] * 1e-3) / 1e9}))
+    torch.cuda.synchronize()
+
+
 def config_json(w, l2="flushed between timed steps (256 MiB write)"):
     g = w.grid
     return {"workload": w.name, "n_x": g.n_x, "n_y": g.n_y, "domain": [g.lo_x, g.lo_y, g.hi_x, g.hi_y],
@@ -181,7 +196,27 @@ def vortex_inputs(w, case):
     case.set_state(u0)
 
 
-def gpu_arm(args, rank, world, local_rank, precision=None, e2e=True, w=None, inputs=channel_inputs, steps=None):
+def vortex_errors(w, rhos):
+    """Density errors of the FP32 compensated form against the FP64 path (the
+    path pinned to the oracle) after the same steps, and of both against the
+    analytic vortex at the time each integrated: relative L1 and L-inf."""
+    from ibtfo_gb300 import cases
+    g = w.grid
+
+    def rel(a, b):
+        d = np.abs(a - b)
+        return {"l1": float(d.sum() / np.abs(b).sum()), "linf": float(d.max() / np.abs(b).max())}
+
+    (r64, t64), (r32, t32) = rhos["fp64_fast"], rhos["fp32c"]
+    out = {"fp32c_vs_fp64": rel(r32, r64), "t_fp64": t64, "t_fp32c": t32}
+    for name, r, t in (("fp64", r64, t64), ("fp32c", r32, t32)):
+        _, ex = cases.isentropic_vortex(g, t=t)
+        out[f"{name}_vs_analytic"] = rel(r, ex.reshape(g.N, g.M, 4)[g.ng:-g.ng, g.ng:-g.ng, 0])
+    return out
+
+
+def gpu_arm(args, rank, world, local_rank, precision=None, e2e=True, w=None, inputs=channel_inputs, steps=None,
+            snapshot=False):
     import torch
     import ibtfo_gb300 as ib
 
@@ -193,6 +228,7 @@ def gpu_arm(args, rank, world, local_rank, precision=None, e2e=True, w=None, inp
     c = ib.Case.from_workload(w, t_end=1e300, max_iter=2 ** 31 - 1, precision=precision or PRECISION)
     c.set_stream(stream.cuda_stream)
     inputs(w, c)
+    p_start = c.progress()
     K = steps or args.steps
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > 129 MB L2
 
@@ -223,6 +259,12 @@ def gpu_arm(args, rank, world, local_rank, precision=None, e2e=True, w=None, inp
     step_ms = sum(e[0].elapsed_time(e[2]) for e in ev)
     sweep_ms = sum(e[0].elapsed_time(e[1]) for e in ev)
     prog = c.progress()
+    rho = None
+    if snapshot:
+        # interior density after warm-up + K steps, and the time it represents
+        # (now_t advances by the dt computed after each step: dt_0 + ... + dt_{n-1})
+        rho = c.get_state().reshape(g.N, g.M, 4)[g.ng:-g.ng, g.ng:-g.ng, 0].copy()
+        rho_t = prog["now_t"] - prog["dt"] + p_start["dt"]
 
     # end to end through the C ABI with host buffers (pinned)
     e2e_steps = max(1, min(K, 20)) if e2e else 1
@@ -245,6 +287,8 @@ def gpu_arm(args, rank, world, local_rank, precision=None, e2e=True, w=None, inp
     step_ms, sweep_ms, e2e_s = (float(x) for x in t.tolist())
     res = {"step_ms": step_ms, "sweep_ms": sweep_ms, "e2e_s": e2e_s, "e2e_steps": e2e_steps, "cells": cells,
            "launches": launches, "clocks": clk.summary(), "progress": prog, "M": g.M, "N": g.N}
+    if snapshot:
+        res["rho"], res["rho_t"] = rho, rho_t
     c.close()
     return res
 
@@ -256,8 +300,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-workload", dest="workload", choices=("channel", "vortex"), default=None,
+                    help="only step this workload (profiler captures)")
+    ap.add_argument("--size", type=int, default=4096, help="grid size for --profile-workload")
+    ap.add_argument("--precision", default=PRECISION, choices=("fp64", "fp64_fast", "fp32c"))
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.workload:
+        profile_run(args)
+        return 0
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -301,13 +352,18 @@ def main():
     wv = _cases.vortex_periodic(4096)
     kv = max(10, min(args.steps, 100))
     forms = {}
+    rhos = {}
     for prec in ("fp64_fast", "fp32c"):
-        rv = gpu_arm(args, rank, world, local_rank, precision=prec, e2e=False, w=wv, inputs=vortex_inputs, steps=kv)
+        rv = gpu_arm(args, rank, world, local_rank, precision=prec, e2e=False, w=wv, inputs=vortex_inputs, steps=kv,
+                     snapshot=(rank == 0))
         cv = wv.grid.n_x * wv.grid.n_y
         sw_s = rv["sweep_ms"] * 1e-3 / kv
-        forms[prec] = {"value": world * cv * kv / (rv["step_ms"] * 1e-3) / 1e9, "unit": METRIC, "steps": kv,
-                       "sweep_ms": rv["sweep_ms"] / kv,
+        forms[prec] = {"value": world * cv * kv / (rv["step_ms"] * 1e-3) / 1e9, "unit": METRIC,
+                       "steps": args.warmup + kv, "sweep_ms": rv["sweep_ms"] / kv,
                        "roofline_frac": BYTES_PER_CELL * cv / sw_s / 1e9 / measured_peaks()[0]}
+        rhos[prec] = (rv.get("rho"), rv.get("rho_t"))
+    if rank == 0:
+        forms["errors"] = vortex_errors(wv, rhos)
     if world > 1:
         import torch
         torch.distributed.destroy_process_group()

@@ -192,6 +192,14 @@ def vortex_periodic(n=4096, riemann="HLLC_Toro"):
     The vortex's vertical velocity exceeds the sound speed in part of the
     core; the reference's HLLC (its HLL solver, which reuses the X-face flux
     where S_D >= 0) turns the state to NaN there within a few dozen steps, so
-    the workload runs the contact-restoring HLLC ("HLLC_Toro")."""
-    return Workload(f"isentropic_vortex_{n}", Grid(n, n, 2, 0.0, 0.0, 10.0, 10.0), 1.4, 0.5, 10.0,
+    the workload runs the contact-restoring HLLC ("HLLC_Toro").
+
+    CFL 0.25: the reference's update is unsplit (both directions from the
+    same state) while its time step is sized on one direction only
+    (ComputeDt.cpp:49, dt = CFL dx / max wave speed), so on this diagonal
+    stream the summed Courant number is about twice CFL.  At CFL 0.5 the
+    scheme is linearly unstable here: a 1e-12 perturbation of the initial
+    state grows to 1e-3 in 200 steps (FP64, MUSCL and MHM alike); at 0.25 it
+    stays near 1e-8 after 400 steps."""
+    return Workload(f"isentropic_vortex_{n}", Grid(n, n, 2, 0.0, 0.0, 10.0, 10.0), 1.4, 0.25, 10.0,
                     "MHM", riemann, "minmod", "Regular", gbc="periodic", extra={"beta": 5.0})

@@ -79,6 +79,17 @@ void set_last_error(const char *msg) { g_err = msg; }
             return cuda_fail(e_, #call);              \
     } while (0)
 
+static void set_gas_constants(GridDesc &g)
+{
+    g.gm1 = g.gamma - 1;
+    g.c1 = (g.gamma + 1) / (2 * g.gamma);
+    g.c2 = (g.gamma - 1) / (2 * g.gamma);
+    g.gf = (float)g.gamma;
+    g.gm1f = (float)g.gm1;
+    g.c1f = (float)g.c1;
+    g.c2f = (float)g.c2;
+}
+
 struct ibtfo_case
 {
     ibtfo_config cfg;
@@ -191,6 +202,7 @@ ibtfo_status ibtfo_create(const ibtfo_config *cfg, ibtfo_case **out)
     g.gamma = k.gamma;
     g.cfl = k.cfl_number;
     g.f32 = (k.precision == IBTFO_PRECISION_FP32_COMPENSATED) ? 1 : 0;
+    set_gas_constants(g);
     c->nblocks = ((k.n_x + TILE_X - 1) / TILE_X) * ((k.n_y + TILE_Y - 1) / TILE_Y);
     c->sweep = sweep_launcher(k.scheme, k.riemann, k.limiter, k.precision);
 
@@ -734,6 +746,7 @@ int case_set_gas(ibtfo_case *c, double gamma, double cfl)
         cudaStreamSynchronize(c->stream);
         c->g.gamma = c->cfg.gamma = gamma;
         c->g.cfl = c->cfg.cfl_number = cfl;
+        set_gas_constants(c->g);
         drop_graph(c);
     }
     return IBTFO_OK;

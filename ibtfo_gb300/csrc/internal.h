@@ -59,6 +59,10 @@ struct GridDesc
     double Li, Hi;   // coordinate of cell (0,0) centre: x_i = Li + i*dx, y_j = Hi + j*dx
     double gamma, cfl;
     int f32;         // state stored as float (hi, lo) pairs: planes 0-3 hi, 4-7 lo
+    // gas constants precomputed on the host (no per-thread divisions):
+    // gamma - 1, (gamma+1)/(2 gamma), (gamma-1)/(2 gamma), and their FP32 copies
+    double gm1, c1, c2;
+    float gf, gm1f, c1f, c2f;
 };
 
 // One conserved component of one cell of a state buffer, as a double.  FP64

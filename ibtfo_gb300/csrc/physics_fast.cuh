@@ -17,18 +17,12 @@
 
 namespace ibtfo {
 
-// gamma-dependent constants, computed once per thread
+// gamma-dependent constants (precomputed on the host, see GridDesc)
 template <typename T>
 struct GasConst
 {
-    T g, gm1, c1, c2;
-    __device__ __forceinline__ explicit GasConst(double gamma)
-    {
-        g = (T)gamma;
-        gm1 = (T)(gamma - 1);
-        c1 = (T)((gamma + 1) / (2 * gamma)); // HLL wave speed: (g+1)/(2g) * p*/p + (g-1)/(2g)
-        c2 = (T)((gamma - 1) / (2 * gamma));
-    }
+    T g, gm1, c1, c2; // gamma, gamma - 1, (gamma+1)/(2 gamma), (gamma-1)/(2 gamma)
+    __device__ __forceinline__ GasConst(T g_, T gm1_, T c1_, T c2_) : g(g_), gm1(gm1_), c1(c1_), c2(c2_) {}
 };
 
 // 1/x: hardware seed + two Newton steps (within an ulp of the rounded value)

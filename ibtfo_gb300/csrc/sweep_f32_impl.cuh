@@ -42,6 +42,7 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_f32_kernel(const SweepAr
     __shared__ float sF[4][TY + 1][TX + 1];
     __shared__ float sG[4][TY + 1][TX];
     __shared__ unsigned char sKeep[TY + 1][TX];
+    __shared__ float sC[4]; // dt/dx, dt/dy, dt/(2dx), dt/(2dy) of this step (one thread computes them)
 
     const GridDesc &g = a.g;
     DevState *st = a.st;
@@ -49,7 +50,7 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_f32_kernel(const SweepAr
         st->fill_pending = 0;
     if (a.guard && !(st->now_t < a.t_end && st->iter < a.max_iter))
         return;
-    const double dt = st->dt;
+    const double dt = st->dt; // read by thread 0 into sC
     const int cur = st->cur;
     const float *__restrict__ U = reinterpret_cast<const float *>(cur ? a.buf1 : a.buf0);
     float *__restrict__ V = reinterpret_cast<float *>(cur ? a.buf0 : a.buf1);
@@ -59,6 +60,13 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_f32_kernel(const SweepAr
     const int i0 = g.ng + (int)(tile & 0xFFFFu) * TX;
     const int j0 = g.ng + (int)(tile >> 16) * TY;
     const int tid = threadIdx.x;
+    if (tid == 0)
+    {
+        sC[0] = (float)(dt / g.dx);
+        sC[1] = (float)(dt / g.dy);
+        sC[2] = (float)(0.5 * dt / g.dx);
+        sC[3] = (float)(0.5 * dt / g.dy);
+    }
 
     for (int q = tid; q < 4 * WX * WY; q += NT)
     {
@@ -73,8 +81,8 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_f32_kernel(const SweepAr
     }
     __syncthreads();
 
-    const GasConst<float> K(g.gamma);
-    const float hx2 = (float)(0.5 * dt / g.dx), hy2 = (float)(0.5 * dt / g.dy);
+    const GasConst<float> K(g.gf, g.gm1f, g.c1f, g.c2f);
+    const float hx2 = sC[2], hy2 = sC[3];
     constexpr int NXF = (TX + 1) * (TY + 1);
     constexpr int NYF = TX * (TY + 1);
     for (int q = tid; q < NXF + NYF; q += NT)
@@ -118,7 +126,9 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_f32_kernel(const SweepAr
     }
     __syncthreads();
 
-    double amax = 0.0, umax = 0.0, vmax = 0.0, mass = 0.0;
+    // per-cell statistics in FP32; the mass as a compensated (hi, lo) float
+    // pair, converted to FP64 once per warp
+    float famax = 0.0f, fumax = 0.0f, fvmax = 0.0f, mhi = 0.0f, mlo = 0.0f;
     int nans = 0;
     {
         const int c = tid % TX, r = tid / TX;
@@ -127,7 +137,7 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_f32_kernel(const SweepAr
         {
             const long long o = (long long)j * pitch + i;
             const int kp = sKeep[r + 1][c], km = sKeep[r][c];
-            const float lx = (float)(dt / g.dx), ly = (float)(dt / g.dy);
+            const float lx = sC[0], ly = sC[1];
             float hi[4], lo[4];
 #pragma unroll
             for (int k = 0; k < 4; k++)
@@ -141,18 +151,37 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_f32_kernel(const SweepAr
                 V[k * P + o] = hi[k];
                 V[(4 + k) * P + o] = lo[k];
             }
-            // CFL statistics (ComputeDt.cpp:38-45) from the hi parts, mass in FP64
+            // CFL statistics (ComputeDt.cpp:38-45) from the hi parts
             const float ir = rcp_t(hi[0]);
             const float u = hi[1] * ir, w = hi[2] * ir;
             const float p = K.gm1 * (hi[3] - 0.5f * hi[0] * (u * u + w * w));
-            amax = (double)sqrtf(K.g * p * ir); // NaN (ignored by the maximum) where p < 0
-            umax = (double)fabsf(u);
-            vmax = (double)fabsf(w);
-            mass = ((double)hi[0] + (double)lo[0]) * (g.dx * g.dy);
+            famax = sqrtf(K.g * p * ir); // NaN (ignored by the maximum) where p < 0
+            fumax = fabsf(u);
+            fvmax = fabsf(w);
+            mhi = hi[0];
+            mlo = lo[0];
             nans = (isnan(hi[0]) || isnan(hi[1]) || isnan(hi[2]) || isnan(hi[3])) ? 1 : 0;
         }
     }
-    block_reduce_finalize<NT>(amax, umax, vmax, mass, nans, st, a.partial, g, true, false);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        famax = fmaxf(famax, __shfl_xor_sync(0xffffffffu, famax, o));
+        fumax = fmaxf(fumax, __shfl_xor_sync(0xffffffffu, fumax, o));
+        fvmax = fmaxf(fvmax, __shfl_xor_sync(0xffffffffu, fvmax, o));
+        // (mhi, mlo) += the partner's pair, error-free on the hi parts
+        const float oh = __shfl_xor_sync(0xffffffffu, mhi, o), ol = __shfl_xor_sync(0xffffffffu, mlo, o);
+        const float s = mhi + oh, bb = s - mhi;
+        const float err = (mhi - (s - bb)) + (oh - bb);
+        mhi = s;
+        mlo = mlo + ol + err;
+    }
+    // one FP64 value per warp: the lane-0 value carries the warp's sums
+    const bool lead = (threadIdx.x & 31) == 0;
+    const double amax = lead ? (double)famax : 0.0, umax = lead ? (double)fumax : 0.0,
+                 vmax = lead ? (double)fvmax : 0.0;
+    const double mass = lead ? ((double)mhi + (double)mlo) * (g.dx * g.dy) : 0.0;
+    block_reduce_finalize<NT, true>(amax, umax, vmax, mass, nans, st, a.partial, g, true, false);
 }
 
 template <int SCH, int RIE, int LIM>

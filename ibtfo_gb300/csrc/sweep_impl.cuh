@@ -30,7 +30,9 @@ __device__ __forceinline__ void atomic_max_nonneg(unsigned long long *addr, doub
 // then the last block to finish computes the next dt and advances the
 // reference loop accounting.  Deterministic: the mass partials are summed
 // in a fixed order whichever block finishes last.
-template <int NT>
+// WARP_DONE: the caller has already reduced each warp into its lane 0 (the
+// FP32 form does that in FP32 so no per-cell FP64 work remains).
+template <int NT, bool WARP_DONE = false>
 __device__ __forceinline__ void block_reduce_finalize(double amax, double umax, double vmax, double mass, int nans,
                                                       DevState *st, double *partial, const GridDesc &g,
                                                       bool step_accounting, bool set_start)
@@ -39,15 +41,20 @@ __device__ __forceinline__ void block_reduce_finalize(double amax, double umax, 
     __shared__ int rnan[NT / 32];
     __shared__ bool last;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (!WARP_DONE)
+    {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+            umax = fmax(umax, __shfl_xor_sync(0xffffffffu, umax, o));
+            vmax = fmax(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+            mass += __shfl_xor_sync(0xffffffffu, mass, o);
+        }
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1)
-    {
-        amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
-        umax = fmax(umax, __shfl_xor_sync(0xffffffffu, umax, o));
-        vmax = fmax(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
-        mass += __shfl_xor_sync(0xffffffffu, mass, o);
         nans += __shfl_xor_sync(0xffffffffu, nans, o);
-    }
     if (lane == 0)
     {
         red[0][wid] = amax;
@@ -170,6 +177,7 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_kernel(const SweepArgs a
     __shared__ double sF[4][TY + 1][TX + 1]; // X faces (i+1/2, j), i in [i0-1, i0+TX), j in [j0-1, j0+TY)
     __shared__ double sG[4][TY + 1][TX];     // Y faces (i, j+1/2), i in [i0, i0+TX), j in [j0-1, j0+TY)
     __shared__ unsigned char sKeep[TY + 1][TX];
+    __shared__ double sC[4]; // fp64_fast: dt/dx, dt/dy, dt/(2dx), dt/(2dy), computed once per block
 
     const GridDesc &g = a.g;
     DevState *st = a.st;
@@ -191,6 +199,14 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_kernel(const SweepArgs a
     const int i0 = g.ng + (int)(tile & 0xFFFFu) * TX;
     const int j0 = g.ng + (int)(tile >> 16) * TY;
     const int tid = threadIdx.x;
+    constexpr bool FASTPHYS = FAST || RIE == HLLCT; // faces evaluated by physics_fast.cuh
+    if (FASTPHYS && tid == 0)
+    {
+        sC[0] = dt / g.dx;
+        sC[1] = dt / g.dy;
+        sC[2] = 0.5 * dt / g.dx;
+        sC[3] = 0.5 * dt / g.dy;
+    }
 
     // stage the tile and its halo (always inside the padded array: ng >= 2)
     for (int q = tid; q < 4 * WX * WY; q += NT)
@@ -207,8 +223,8 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_kernel(const SweepArgs a
     __syncthreads();
 
     const double gam = g.gamma;
-    const GasConst<double> K(gam);
-    const double hx2 = 0.5 * dt / g.dx, hy2 = 0.5 * dt / g.dy; // fp64_fast MHM predictor
+    const GasConst<double> K(gam, g.gm1, g.c1, g.c2);
+    const double hx2 = FASTPHYS ? sC[2] : 0.0, hy2 = FASTPHYS ? sC[3] : 0.0; // MHM predictor of physics_fast
     constexpr int NXF = (TX + 1) * (TY + 1);
     constexpr int NYF = TX * (TY + 1);
     for (int q = tid; q < NXF + NYF; q += NT)
@@ -225,7 +241,7 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_kernel(const SweepArgs a
                 c2[k] = sU[k][r + 1][fc + 2];
                 c3[k] = sU[k][r + 1][fc + 3];
             }
-            if (FAST || RIE == HLLCT)
+            if (FASTPHYS)
                 x_face_fast<double, SCH, RIE, LIM>(c0, c1, c2, c3, K, hx2, f);
             else
                 x_face<SCH, RIE, LIM>(c0, c1, c2, c3, gam, dt, g.dx, f);
@@ -246,7 +262,7 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_kernel(const SweepArgs a
                 c3[k] = sU[k][r + 3][c + 2];
             }
             double stray = 0.0;
-            int keep = (FAST || RIE == HLLCT) ? y_face_fast<double, SCH, RIE, LIM>(c0, c1, c2, c3, K, hy2, f, &stray)
+            int keep = FASTPHYS ? y_face_fast<double, SCH, RIE, LIM>(c0, c1, c2, c3, K, hy2, f, &stray)
                             : y_face<SCH, RIE, LIM>(c0, c1, c2, c3, gam, dt, g.dy, f, &stray);
 #pragma unroll
             for (int k = 0; k < 4; k++)
@@ -265,7 +281,7 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_kernel(const SweepArgs a
         if (i < g.ng + g.n_x && j < g.ng + g.n_y && a.type[(long long)j * pitch + i] == 0)
         {
             const int kp = sKeep[r + 1][c], km = sKeep[r][c];
-            const double lx = dt / g.dx, ly = dt / g.dy;
+            const double lx = FAST ? sC[0] : 0.0, ly = FAST ? sC[1] : 0.0;
             double v[4];
 #pragma unroll
             for (int k = 0; k < 4; k++)
