@@ -57,6 +57,26 @@ class Progress(C.Structure):
 # every entry point of include/ibtfo.h with its ctypes signature
 _P = C.c_void_p
 _DP = C.POINTER(C.c_double)
+class BatchConfig(C.Structure):
+    _fields_ = [("scheme", C.c_int), ("riemann", C.c_int), ("limiter", C.c_int), ("precision", C.c_int),
+                ("tile_shape", C.c_int), ("ctas_per_sm", C.c_int), ("graph_steps", C.c_int),
+                ("reserved", C.c_int * 5)]
+
+
+class BatchTiling(C.Structure):
+    _fields_ = [("tile_shape", C.c_int), ("ctas_per_sm", C.c_int), ("max_ctas_per_sm", C.c_int), ("grid", C.c_int),
+                ("tiles", C.c_longlong), ("ms_per_step", C.c_double), ("reserved", C.c_int * 4)]
+
+    def as_dict(self):
+        return {"tile_shape": TILE_SHAPES_BY_ID[self.tile_shape], "ctas_per_sm": self.ctas_per_sm,
+                "max_ctas_per_sm": self.max_ctas_per_sm, "grid": self.grid, "tiles": self.tiles,
+                "ms_per_step": self.ms_per_step}
+
+
+TILE_SHAPES = {"32x8": 0, "32x16": 1, "64x8": 2}
+TILE_SHAPES_BY_ID = {v: k for k, v in TILE_SHAPES.items()}
+
+
 SIGNATURES = {
     "ibtfo_abi_version": (C.c_int, []),
     "ibtfo_last_error": (C.c_char_p, []),
@@ -91,6 +111,24 @@ SIGNATURES = {
     "ibtfo_case_init": (C.c_int, [C.c_char_p, _P, C.POINTER(Config), _DP, _DP]),
     "ibtfo_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(_P)]),
     "ibtfo_host_free": (C.c_int, [_P]),
+    "ibtfo_query": (C.c_int, [_P]),
+    "ibtfo_batch_create": (C.c_int, [C.POINTER(BatchConfig), C.POINTER(_P)]),
+    "ibtfo_batch_destroy": (C.c_int, [_P]),
+    "ibtfo_batch_set_stream": (C.c_int, [_P, _P]),
+    "ibtfo_batch_add": (C.c_int, [_P, _P, C.POINTER(C.c_int)]),
+    "ibtfo_batch_remove": (C.c_int, [_P, C.c_int]),
+    "ibtfo_batch_size": (C.c_int, [_P]),
+    "ibtfo_batch_num_slots": (C.c_int, [_P]),
+    "ibtfo_batch_case": (_P, [_P, C.c_int]),
+    "ibtfo_batch_advance": (C.c_int, [_P, C.c_int]),
+    "ibtfo_batch_progress_enqueue": (C.c_int, [_P]),
+    "ibtfo_batch_progress_read": (C.c_int, [_P, C.POINTER(Progress), C.POINTER(C.c_int), C.c_int, C.c_int]),
+    "ibtfo_batch_progress": (C.c_int, [_P, C.POINTER(Progress), C.POINTER(C.c_int), C.c_int]),
+    "ibtfo_batch_synchronize": (C.c_int, [_P]),
+    "ibtfo_batch_set_tiling": (C.c_int, [_P, C.c_int, C.c_int]),
+    "ibtfo_batch_get_tiling": (C.c_int, [_P, C.POINTER(BatchTiling)]),
+    "ibtfo_batch_autotune": (C.c_int, [_P, C.c_int, C.POINTER(BatchTiling), C.POINTER(BatchTiling), C.c_int,
+                                       C.POINTER(C.c_int)]),
 }
 
 _I = C.c_int
@@ -270,6 +308,112 @@ class Case:
 
     def synchronize(self):
         _check(lib().ibtfo_synchronize(self.h))
+
+    def idle(self) -> bool:
+        """True when nothing queued on the case's stream is pending (does not wait)."""
+        code = lib().ibtfo_query(self.h)
+        if code == 4:
+            return False
+        _check(code)
+        return True
+
+
+class Batch:
+    """Many cases stepped together (persistent batched sweep, CUDA graphs).
+
+    Every case must share the batch's scheme, Riemann solver, limiter and
+    precision; `add` takes a Case whose state is set.  A case in a batch is
+    stepped by the batch only; its own get_state / progress stay valid after
+    `synchronize`."""
+
+    def __init__(self, scheme="MUSCL", riemann="HLL", limiter="minmod", precision="fp32c", tile_shape="32x8",
+                 ctas_per_sm=0, graph_steps=16):
+        cfg = BatchConfig(SCHEMES[scheme], RIEMANNS[riemann], LIMITERS[limiter], PRECISIONS[precision],
+                          TILE_SHAPES[tile_shape], ctas_per_sm, graph_steps)
+        h = _P()
+        _check(lib().ibtfo_batch_create(C.byref(cfg), C.byref(h)))
+        self.h = h
+        self.cases = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().ibtfo_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def add(self, case: Case) -> int:
+        slot = C.c_int()
+        _check(lib().ibtfo_batch_add(self.h, case.h, C.byref(slot)))
+        self.cases[slot.value] = case
+        return slot.value
+
+    def remove(self, slot: int):
+        _check(lib().ibtfo_batch_remove(self.h, int(slot)))
+        return self.cases.pop(slot, None)
+
+    def __len__(self):
+        return lib().ibtfo_batch_size(self.h)
+
+    @property
+    def num_slots(self):
+        return lib().ibtfo_batch_num_slots(self.h)
+
+    def set_stream(self, stream_ptr: int | None):
+        _check(lib().ibtfo_batch_set_stream(self.h, C.c_void_p(stream_ptr) if stream_ptr else None))
+
+    def advance(self, nsteps: int):
+        _check(lib().ibtfo_batch_advance(self.h, int(nsteps)))
+
+    def progress(self):
+        """{slot: (progress dict, active)} for every occupied slot (waits)."""
+        n = self.num_slots
+        arr = (Progress * max(n, 1))()
+        act = (C.c_int * max(n, 1))()
+        _check(lib().ibtfo_batch_progress(self.h, arr, act, n))
+        return {k: (arr[k].as_dict(), bool(act[k])) for k in range(n) if k in self.cases}
+
+    def progress_enqueue(self):
+        _check(lib().ibtfo_batch_progress_enqueue(self.h))
+
+    def progress_read(self, wait=True):
+        """Like progress() for the last enqueued snapshot; None if not ready (wait=False)."""
+        n = self.num_slots
+        arr = (Progress * max(n, 1))()
+        act = (C.c_int * max(n, 1))()
+        code = lib().ibtfo_batch_progress_read(self.h, arr, act, n, 1 if wait else 0)
+        if code == 4 and not wait:
+            return None
+        _check(code)
+        return {k: (arr[k].as_dict(), bool(act[k])) for k in range(n) if k in self.cases}
+
+    def synchronize(self):
+        _check(lib().ibtfo_batch_synchronize(self.h))
+
+    def set_tiling(self, tile_shape="32x8", ctas_per_sm=0):
+        _check(lib().ibtfo_batch_set_tiling(self.h, TILE_SHAPES[tile_shape], int(ctas_per_sm)))
+
+    def tiling(self):
+        t = BatchTiling()
+        _check(lib().ibtfo_batch_get_tiling(self.h, C.byref(t)))
+        return t.as_dict()
+
+    def autotune(self, steps=8, max_trials=64):
+        best = BatchTiling()
+        trials = (BatchTiling * max_trials)()
+        n = C.c_int()
+        _check(lib().ibtfo_batch_autotune(self.h, int(steps), C.byref(best), trials, max_trials, C.byref(n)))
+        return best.as_dict(), [trials[i].as_dict() for i in range(min(n.value, max_trials))]
 
 
 class Inp:

@@ -132,6 +132,39 @@ def channel_init(g: Grid, types, gamma=1.4, angle_deg=30.0, center=None, left=(1
     return _solid_fill(u, np.asarray(types).reshape(g.N, g.M)).reshape(-1)
 
 
+def cylinder_phi(g: Grid, xc, yc, r):
+    """Circular body of radius r centred at (xc, yc): phi = distance to the
+    circle, positive in the fluid outside it."""
+    x, y = g.coords()
+    return np.ascontiguousarray(np.hypot(x - xc, y - yc) - r).reshape(-1)
+
+
+def uniform_init(g: Grid, types, state=(1.0, 0.0, 0.0, 1.0), gamma=1.4):
+    """One primitive state (rho, u, v, p) everywhere, solid cells filled as the reference does."""
+    u = np.ascontiguousarray(np.broadcast_to(conserved(*state, gamma), (g.N, g.M, 4))).copy()
+    return _solid_fill(u, np.asarray(types).reshape(g.N, g.M)).reshape(-1)
+
+
+def post_shock(mach, gamma=1.4, pre=(1.0, 0.0, 0.0, 1.0)):
+    """Rankine-Hugoniot state behind a normal shock moving in +x at Mach
+    `mach` into the quiescent state `pre` (rho, u, v, p)."""
+    rho1, _, _, p1 = pre
+    a1 = math.sqrt(gamma * p1 / rho1)
+    m2 = mach * mach
+    rho2 = rho1 * (gamma + 1) * m2 / ((gamma - 1) * m2 + 2)
+    p2 = p1 * (2 * gamma * m2 - (gamma - 1)) / (gamma + 1)
+    u2 = 2 * a1 / (gamma + 1) * (mach - 1 / mach)
+    return (rho2, u2, 0.0, p2)
+
+
+def shock_init(g: Grid, types, mach, x_shock, gamma=1.4, pre=(1.0, 0.0, 0.0, 1.0)):
+    """Normal shock at x = x_shock moving into `pre` (post-shock state behind it)."""
+    x, _ = g.coords()
+    u = np.where((x < x_shock)[..., None], conserved(*post_shock(mach, gamma, pre), gamma), conserved(*pre, gamma))
+    u = np.ascontiguousarray(u)
+    return _solid_fill(u, np.asarray(types).reshape(g.N, g.M)).reshape(-1)
+
+
 def isentropic_vortex(g: Grid, gamma=1.4, beta=5.0, xc=5.0, yc=5.0, u_inf=1.0, v_inf=1.0, t=0.0, periodic=True):
     """Isentropic vortex of strength beta on a uniform (1, u_inf, v_inf, 1)
     stream; at time t the exact solution is the initial field moved by

@@ -216,7 +216,9 @@ __device__ void fill_ring(const FillArgs &a, const View &v, double *dst, long lo
         state_st(dst, k, o, out[k], a.g);
 }
 
-__global__ void __launch_bounds__(256) fill_kernel(const FillArgs a)
+// one 256-thread block of a case's boundary pass: blocks [0, gblocks) fill
+// the ghost list, the rest the domain edges
+__device__ __forceinline__ void fill_block(const FillArgs &a, int vb, int do_ghosts, int do_ring)
 {
     DevState *st = a.st;
     if (!a.init_mode && !st->fill_pending)
@@ -233,20 +235,25 @@ __global__ void __launch_bounds__(256) fill_kernel(const FillArgs a)
     v.n_x = a.g.n_x;
     v.n_y = a.g.n_y;
     double *dst = cur ? a.buf1 : a.buf0;
-    const int gblocks = a.do_ghosts ? (a.nghost + 255) / 256 : 0;
-    if ((int)blockIdx.x < gblocks)
+    const int gblocks = do_ghosts ? (a.nghost + 255) / 256 : 0;
+    if (vb < gblocks)
     {
-        int t = blockIdx.x * 256 + threadIdx.x;
+        int t = vb * 256 + threadIdx.x;
         if (t < a.nghost)
             fill_ghost(a, v, dst, a.ghosts[t]);
         return;
     }
-    if (!a.do_ring)
+    if (!do_ring)
         return;
-    long long q = (long long)(blockIdx.x - gblocks) * 256 + threadIdx.x;
+    long long q = (long long)(vb - gblocks) * 256 + threadIdx.x;
     long long nring = 2LL * a.g.ng * a.g.n_x + 2LL * a.g.ng * a.g.N;
     if (q < nring)
         fill_ring(a, v, dst, q);
+}
+
+__global__ void __launch_bounds__(256) fill_kernel(const FillArgs a)
+{
+    fill_block(a, blockIdx.x, a.do_ghosts, a.do_ring);
 }
 
 void launch_fill(const FillArgs &a, cudaStream_t s)
@@ -260,6 +267,62 @@ void launch_fill(const FillArgs &a, cudaStream_t s)
     count_launch();
 }
 
+// Boundary pass of every case of a batch, phase 0 or 1.  Phase 0: ghost
+// list (ghost-fluid variants) and domain edges; phase 1: the domain edges of
+// periodic ghost-fluid cases, which copy interior cells filled in phase 0.
+// The (slot, block) table lists only blocks with work; persistent CTAs walk it.
+__global__ void __launch_bounds__(256) batch_fill_kernel(const BatchHeader *__restrict__ h, int phase)
+{
+    const int n = h->nfill[phase];
+    const int2 *tab = h->fill[phase];
+    for (int b = blockIdx.x; b < n; b += gridDim.x)
+    {
+        const int2 e = tab[b];
+        const FillArgs &a = h->cases[e.x].f;
+        const bool gfm = a.bc != BC_REGULAR;
+        const bool split = gfm && a.gb == GB_PERIODIC;
+        if (phase == 0)
+            fill_block(a, e.y, gfm ? 1 : 0, split ? 0 : 1);
+        else
+            fill_block(a, e.y, 0, 1);
+    }
+}
+
+void launch_batch_fill(const BatchHeader *h, int phase, int grid, cudaStream_t s)
+{
+    batch_fill_kernel<<<grid, 256, 0, s>>>(h, phase);
+    count_launch();
+}
+
+// per-slot progress for the host (one thread per slot)
+__global__ void batch_progress_kernel(const BatchHeader *__restrict__ h, BatchProgress *out)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= h->nslots)
+        return;
+    const BatchCase &c = h->cases[k];
+    BatchProgress p{};
+    if (c.s.st)
+    {
+        const DevState *st = c.s.st;
+        p.now_t = st->now_t;
+        p.dt = st->dt;
+        p.mass = st->mass;
+        p.mass_start = st->mass_start;
+        p.iter = st->iter;
+        p.status = st->status;
+        p.nan_cells = st->nan_cells;
+        p.active = (st->now_t < c.s.t_end && st->iter < c.s.max_iter) ? 1 : 0;
+    }
+    out[k] = p;
+}
+
+void launch_batch_progress(const BatchHeader *h, int nslots_max, BatchProgress *out, cudaStream_t s)
+{
+    batch_progress_kernel<<<(nslots_max + 127) / 128, 128, 0, s>>>(h, out);
+    count_launch();
+}
+
 // ---------------------------------------------------------------- reduction
 
 // ComputeDt (Src/Base/Common/ComputeDt.cpp:4-51) and CaculateMass
@@ -269,8 +332,7 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) reduce_kernel(const ReduceArgs
     const GridDesc &g = a.g;
     const int i = g.ng + blockIdx.x * TILE_X + (threadIdx.x % TILE_X);
     const int j = g.ng + blockIdx.y * TILE_Y + (threadIdx.x / TILE_X);
-    double amax = 0, umax = 0, vmax = 0, mass = 0;
-    int nans = 0;
+    CellStats cs;
     if (i < g.ng + g.n_x && j < g.ng + g.n_y)
     {
         long long o = (long long)j * g.pitch + i;
@@ -279,10 +341,11 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) reduce_kernel(const ReduceArgs
             double v[4];
             for (int k = 0; k < 4; k++)
                 v[k] = state_ld(a.u, k, o, g);
-            cell_stats(v, g.gamma, g.dx, g.dy, amax, umax, vmax, mass, nans);
+            cell_stats(v, g.gamma, g.dx, g.dy, cs);
         }
     }
-    block_reduce_finalize<TILE_X * TILE_Y>(amax, umax, vmax, mass, nans, a.st, a.partial, g, false, a.set_start);
+    block_reduce_finalize<TILE_X * TILE_Y>(cs, a.st, a.partial, g, false, a.set_start, gridDim.x * gridDim.y,
+                                           blockIdx.y * gridDim.x + blockIdx.x);
 }
 
 void launch_reduce(const ReduceArgs &a, int, cudaStream_t s)

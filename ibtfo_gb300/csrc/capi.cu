@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -79,7 +80,7 @@ void set_last_error(const char *msg) { g_err = msg; }
             return cuda_fail(e_, #call);              \
     } while (0)
 
-static void set_gas_constants(GridDesc &g)
+static void set_derived_constants(GridDesc &g)
 {
     g.gm1 = g.gamma - 1;
     g.c1 = (g.gamma + 1) / (2 * g.gamma);
@@ -88,6 +89,15 @@ static void set_gas_constants(GridDesc &g)
     g.gm1f = (float)g.gm1;
     g.c1f = (float)g.c1;
     g.c2f = (float)g.c2;
+    g.igm1 = 1.0 / g.gm1;
+    g.ig2 = 1.0 / (2 * g.gamma);
+    g.igm1f = (float)g.igm1;
+    g.ig2f = (float)g.ig2;
+    g.idx = 1.0 / g.dx;
+    g.idy = 1.0 / g.dy;
+    g.dxdy = g.dx * g.dy;
+    g.idxf = (float)g.idx;
+    g.idyf = (float)g.idy;
 }
 
 struct ibtfo_case
@@ -114,6 +124,26 @@ struct ibtfo_case
     cudaGraphExec_t graph = nullptr;
     int graph_steps = 0;
 };
+
+// Case buffers come from the device's stream-ordered pool; freed memory stays
+// in the pool (no release threshold) so that cases created and destroyed
+// while others run reuse it without device-wide synchronisation.
+static void retain_pool_memory(int device)
+{
+    static std::mutex mu;
+    static std::vector<int> done;
+    std::lock_guard<std::mutex> lk(mu);
+    for (int d : done)
+        if (d == device)
+            return;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess)
+    {
+        uint64_t thr = ~0ull;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    done.push_back(device);
+}
 
 static int nsch_of(int bc)
 {
@@ -143,21 +173,19 @@ ibtfo_status ibtfo_destroy(ibtfo_case *c)
         cudaStreamSynchronize(c->stream);
     if (c->graph)
         cudaGraphExecDestroy(c->graph);
-    cudaFree(c->buf[0]);
-    cudaFree(c->buf[1]);
-    cudaFree(c->ic);
-    cudaFree(c->staging);
-    cudaFree(c->phi);
-    cudaFree(c->nx);
-    cudaFree(c->ny);
-    cudaFree(c->type);
-    cudaFree(c->ghosts);
-    cudaFree(c->st);
-    cudaFree(c->partial);
-    cudaFree(c->ring_ic);
-    cudaFree(c->tiles);
+    // stream-ordered frees: the memory returns to the device pool without a
+    // device-wide synchronisation (other cases keep running)
+    cudaStream_t fs = c->own ? c->own : c->stream;
+    void *bufs[] = {c->buf[0], c->buf[1], c->ic, c->staging, c->phi, c->nx, c->ny, c->type, c->ghosts,
+                    c->st, c->partial, c->ring_ic, c->tiles};
+    for (void *p : bufs)
+        if (p)
+            cudaFreeAsync(p, fs);
     if (c->own)
+    {
+        cudaStreamSynchronize(c->own);
         cudaStreamDestroy(c->own);
+    }
     delete c;
     return IBTFO_OK;
 }
@@ -202,18 +230,19 @@ ibtfo_status ibtfo_create(const ibtfo_config *cfg, ibtfo_case **out)
     g.gamma = k.gamma;
     g.cfl = k.cfl_number;
     g.f32 = (k.precision == IBTFO_PRECISION_FP32_COMPENSATED) ? 1 : 0;
-    set_gas_constants(g);
+    set_derived_constants(g);
     c->nblocks = ((k.n_x + TILE_X - 1) / TILE_X) * ((k.n_y + TILE_Y - 1) / TILE_Y);
     c->sweep = sweep_launcher(k.scheme, k.riemann, k.limiter, k.precision);
 
     const size_t cells = (size_t)g.M * g.N;
     const size_t plane_bytes = sizeof(double) * (size_t)g.plane;
-    cudaError_t e = cudaSuccess;
+    retain_pool_memory(c->device);
+    cudaError_t e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
     auto A = [&](void **p, size_t bytes) {
         if (e == cudaSuccess)
-            e = cudaMalloc(p, bytes);
+            e = cudaMallocAsync(p, bytes, c->own);
         if (e == cudaSuccess)
-            e = cudaMemset(*p, 0, bytes);
+            e = cudaMemsetAsync(*p, 0, bytes, c->own);
     };
     A((void **)&c->buf[0], 4 * plane_bytes);
     A((void **)&c->buf[1], 4 * plane_bytes);
@@ -228,7 +257,7 @@ ibtfo_status ibtfo_create(const ibtfo_config *cfg, ibtfo_case **out)
     A((void **)&c->partial, sizeof(double) * (size_t)c->nblocks);
     A((void **)&c->ring_ic, sizeof(double) * 2 * 2 * g.ng * 4);
     if (e == cudaSuccess)
-        e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
+        e = cudaStreamSynchronize(c->own);
     if (e != cudaSuccess)
     {
         ibtfo_status s = (e == cudaErrorMemoryAllocation) ? fail(IBTFO_ENOMEM, "device allocation failed")
@@ -271,7 +300,7 @@ ibtfo_status ibtfo_setup_geometry(ibtfo_case *c, const double *phi)
                          cudaMemcpyHostToDevice, c->stream));
     if (c->ghosts)
     {
-        cudaFree(c->ghosts);
+        cudaFreeAsync(c->ghosts, c->stream);
         c->ghosts = nullptr;
         c->nghost = 0;
     }
@@ -513,6 +542,18 @@ ibtfo_status ibtfo_get_progress(ibtfo_case *c, ibtfo_progress *p)
     return IBTFO_OK;
 }
 
+ibtfo_status ibtfo_query(ibtfo_case *c)
+{
+    if (!c)
+        return fail(IBTFO_EINVAL, "null case");
+    cudaSetDevice(c->device);
+    cudaError_t e = cudaStreamQuery(c->stream);
+    if (e == cudaErrorNotReady)
+        return IBTFO_ETIMEOUT;
+    CK(e);
+    return IBTFO_OK;
+}
+
 ibtfo_status ibtfo_synchronize(ibtfo_case *c)
 {
     if (!c)
@@ -746,7 +787,7 @@ int case_set_gas(ibtfo_case *c, double gamma, double cfl)
         cudaStreamSynchronize(c->stream);
         c->g.gamma = c->cfg.gamma = gamma;
         c->g.cfl = c->cfg.cfl_number = cfl;
-        set_gas_constants(c->g);
+        set_derived_constants(c->g);
         drop_graph(c);
     }
     return IBTFO_OK;
@@ -754,6 +795,22 @@ int case_set_gas(ibtfo_case *c, double gamma, double cfl)
 
 double case_cfl(const ibtfo_case *c) { return c->g.cfl; }
 double case_gamma(const ibtfo_case *c) { return c->g.gamma; }
+
+int case_batch_view(ibtfo_case *c, SweepArgs *sa, FillArgs *fa, int *scheme, int *riemann, int *limiter,
+                    int *precision, int *has_state)
+{
+    *sa = sweep_args(c, 1);
+    *fa = fill_args(c);
+    *scheme = c->cfg.scheme;
+    *riemann = c->cfg.riemann;
+    *limiter = c->cfg.limiter;
+    *precision = c->cfg.precision;
+    *has_state = c->state ? 1 : 0;
+    return 0;
+}
+
+cudaStream_t case_stream(const ibtfo_case *c) { return c->stream; }
+int case_device(const ibtfo_case *c) { return c->device; }
 
 int case_set_dt(ibtfo_case *c, double dt)
 {

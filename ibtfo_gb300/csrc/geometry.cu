@@ -246,17 +246,18 @@ __global__ void scheme_index_kernel(GridDesc g, int bc, const double *__restrict
 
 static inline unsigned nblk(long long n, int b) { return (unsigned)((n + b - 1) / b); }
 
-// one flag per sweep tile: does it hold an interior fluid cell?
-__global__ void tile_flags_kernel(GridDesc g, const uint8_t *__restrict__ type, int ntx, int nty, uint8_t *flags)
+// one flag per tx x ty sweep tile: does it hold an interior fluid cell?
+__global__ void tile_flags_kernel(GridDesc g, const uint8_t *__restrict__ type, int tx, int ty, int ntx, int nty,
+                                  uint8_t *flags)
 {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ntx * nty)
         return;
     int bx = t % ntx, by = t / ntx;
-    int i0 = g.ng + bx * TILE_X, j0 = g.ng + by * TILE_Y;
+    int i0 = g.ng + bx * tx, j0 = g.ng + by * ty;
     uint8_t f = 0;
-    for (int j = j0; j < j0 + TILE_Y && j < g.ng + g.n_y && !f; j++)
-        for (int i = i0; i < i0 + TILE_X && i < g.ng + g.n_x; i++)
+    for (int j = j0; j < j0 + ty && j < g.ng + g.n_y && !f; j++)
+        for (int i = i0; i < i0 + tx && i < g.ng + g.n_x; i++)
             if (type[(long long)j * g.pitch + i] == 0)
             {
                 f = 1;
@@ -265,34 +266,46 @@ __global__ void tile_flags_kernel(GridDesc g, const uint8_t *__restrict__ type, 
     flags[t] = f;
 }
 
-int active_tiles(const GridDesc &g, const uint8_t *d_type, unsigned **d_tiles, int *ntiles, cudaStream_t s)
+int active_tile_list(const GridDesc &g, const uint8_t *d_type, int tx, int ty, std::vector<unsigned> &list,
+                     cudaStream_t s)
 {
-    const int ntx = (g.n_x + TILE_X - 1) / TILE_X, nty = (g.n_y + TILE_Y - 1) / TILE_Y;
+    const int ntx = (g.n_x + tx - 1) / tx, nty = (g.n_y + ty - 1) / ty;
     const int n = ntx * nty;
     uint8_t *d_flags = nullptr;
-    if (cudaMalloc(&d_flags, n) != cudaSuccess)
+    if (cudaMallocAsync(&d_flags, n, s) != cudaSuccess)
         return 2;
-    tile_flags_kernel<<<nblk(n, 256), 256, 0, s>>>(g, d_type, ntx, nty, d_flags);
+    tile_flags_kernel<<<nblk(n, 256), 256, 0, s>>>(g, d_type, tx, ty, ntx, nty, d_flags);
     count_launch();
     std::vector<uint8_t> flags(n);
     cudaError_t e = cudaMemcpyAsync(flags.data(), d_flags, n, cudaMemcpyDeviceToHost, s);
+    cudaFreeAsync(d_flags, s);
     if (e == cudaSuccess)
         e = cudaStreamSynchronize(s);
-    cudaFree(d_flags);
     if (e != cudaSuccess)
         return 5;
-    std::vector<unsigned> list;
+    list.clear();
     for (int t = 0; t < n; t++)
         if (flags[t])
             list.push_back((unsigned)(t % ntx) | ((unsigned)(t / ntx) << 16));
     if (list.empty())
         list.push_back(0u); // a tile without fluid still runs the loop accounting
+    return 0;
+}
+
+int active_tiles(const GridDesc &g, const uint8_t *d_type, unsigned **d_tiles, int *ntiles, cudaStream_t s)
+{
+    std::vector<unsigned> list;
+    int rc = active_tile_list(g, d_type, TILE_X, TILE_Y, list, s);
+    if (rc)
+        return rc;
     if (*d_tiles)
-        cudaFree(*d_tiles);
+        cudaFreeAsync(*d_tiles, s);
     *d_tiles = nullptr;
-    if (cudaMalloc(d_tiles, sizeof(unsigned) * list.size()) != cudaSuccess)
+    if (cudaMallocAsync(d_tiles, sizeof(unsigned) * list.size(), s) != cudaSuccess)
         return 2;
-    if (cudaMemcpy(*d_tiles, list.data(), sizeof(unsigned) * list.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+    if (cudaMemcpyAsync(*d_tiles, list.data(), sizeof(unsigned) * list.size(), cudaMemcpyHostToDevice, s) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
         return 5;
     *ntiles = (int)list.size();
     return 0;
@@ -310,7 +323,7 @@ int setup_geometry(const GridDesc &g, int bc, const double *d_phi, double *d_nx,
     if (bc == BC_REGULAR)
         return 0;
     int *d_counts = nullptr;
-    if (cudaMalloc(&d_counts, sizeof(int) * (size_t)g.n_y) != cudaSuccess)
+    if (cudaMallocAsync(&d_counts, sizeof(int) * (size_t)g.n_y, s) != cudaSuccess)
         return 2;
     const int rows_per_block = 8;
     ghost_count_kernel<<<nblk(g.n_y, rows_per_block), 32 * rows_per_block, 0, s>>>(g, d_type, d_counts);
@@ -319,7 +332,7 @@ int setup_geometry(const GridDesc &g, int bc, const double *d_phi, double *d_nx,
     if (cudaMemcpyAsync(counts.data(), d_counts, sizeof(int) * g.n_y, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)
     {
-        cudaFree(d_counts);
+        cudaFreeAsync(d_counts, s);
         return 5;
     }
     long long tot = 0;
@@ -331,13 +344,13 @@ int setup_geometry(const GridDesc &g, int bc, const double *d_phi, double *d_nx,
     *nghost = (int)tot;
     if (tot == 0)
     {
-        cudaFree(d_counts);
+        cudaFreeAsync(d_counts, s);
         return 0;
     }
     GhostRec *gl = nullptr;
-    if (cudaMalloc(&gl, sizeof(GhostRec) * (size_t)tot) != cudaSuccess)
+    if (cudaMallocAsync(&gl, sizeof(GhostRec) * (size_t)tot, s) != cudaSuccess)
     {
-        cudaFree(d_counts);
+        cudaFreeAsync(d_counts, s);
         return 2;
     }
     cudaMemcpyAsync(d_counts, offs.data(), sizeof(int) * g.n_y, cudaMemcpyHostToDevice, s);
@@ -345,10 +358,10 @@ int setup_geometry(const GridDesc &g, int bc, const double *d_phi, double *d_nx,
     scheme_index_kernel<<<nblk(tot, 128), 128, 0, s>>>(g, bc, d_phi, d_nx, d_ny, d_type, gl, (int)tot);
     count_launch(2);
     cudaError_t e = cudaStreamSynchronize(s);
-    cudaFree(d_counts);
+    cudaFreeAsync(d_counts, s);
     if (e != cudaSuccess)
     {
-        cudaFree(gl);
+        cudaFreeAsync(gl, s);
         return 5;
     }
     *d_ghosts = gl;

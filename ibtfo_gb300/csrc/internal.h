@@ -4,6 +4,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <vector>
 
 namespace ibtfo {
 
@@ -61,8 +62,11 @@ struct GridDesc
     int f32;         // state stored as float (hi, lo) pairs: planes 0-3 hi, 4-7 lo
     // gas constants precomputed on the host (no per-thread divisions):
     // gamma - 1, (gamma+1)/(2 gamma), (gamma-1)/(2 gamma), and their FP32 copies
-    double gm1, c1, c2;
-    float gf, gm1f, c1f, c2f;
+    double gm1, c1, c2, igm1, ig2; // ..., 1/(gamma - 1), 1/(2 gamma)
+    float gf, gm1f, c1f, c2f, igm1f, ig2f;
+    // 1/dx, 1/dy, dx*dy and FP32 copies of the reciprocals
+    double idx, idy, dxdy;
+    float idxf, idyf;
 };
 
 // One conserved component of one cell of a state buffer, as a double.  FP64
@@ -142,8 +146,66 @@ void launch_reduce(const ReduceArgs &a, int nblocks_max, cudaStream_t s);
 void launch_aos_to_soa(const double *aos, double *soa, const GridDesc &g, cudaStream_t s);
 void launch_soa_to_aos(const double *soa, double *aos, const GridDesc &g, cudaStream_t s);
 
+// ---------------------------------------------------------------- batches
+//
+// A batch steps many cases (each with its own grid, geometry, dt and loop
+// accounting) with one persistent sweep kernel over a shared tile table and
+// one fill kernel per boundary phase.  The kernels take the address of a
+// BatchHeader whose device copy the host rewrites (stream-ordered) when
+// cases join or leave, so a captured graph of steps stays valid.
+
+// one case of a batch
+struct BatchCase
+{
+    SweepArgs s;  // buffers, cell types, device state, this case's mass partials, t_end, max_iter
+    FillArgs f;   // ghost list and domain-edge pass
+    int ntiles;   // tiles of this case in the table (the case's block count)
+    int slot;
+};
+
+// tile table entry: x = tile (bx | by << 16), y = index of the tile within
+// its case, z = batch slot
+typedef uint4 BatchTile;
+
+struct BatchHeader
+{
+    const BatchCase *cases;   // indexed by slot
+    const BatchTile *tiles;
+    const int2 *fill[2];      // (slot, block of the case's fill pass) per boundary phase
+    int ntiles;
+    int nfill[2];
+    int nslots;
+};
+
+// progress of one slot, gathered for the host after a chunk of steps
+struct BatchProgress
+{
+    double now_t, dt, mass, mass_start;
+    int iter, status, nan_cells, active;
+};
+
+// tile shapes of the batched sweep (cells per CTA; 256 threads)
+enum BatchShape { SHAPE_32x8 = 0, SHAPE_32x16 = 1, SHAPE_64x8 = 2, SHAPE_COUNT = 3 };
+constexpr int shape_tx(int shape) { return shape == SHAPE_64x8 ? 64 : 32; }
+constexpr int shape_ty(int shape) { return shape == SHAPE_32x16 ? 16 : 8; }
+constexpr int BATCH_THREADS = 256;
+
+struct BatchKernel
+{
+    void (*launch)(const BatchHeader *h, int grid, cudaStream_t s);
+    int (*prepare)(); // sets the shared-memory limit, returns resident CTAs per SM (0 on failure)
+};
+// precision: 1 = fp64_fast, 2 = FP32 compensated (strict FP64 runs one case per launch)
+BatchKernel batch_kernel(int scheme, int riemann, int limiter, int precision, int shape);
+void launch_batch_fill(const BatchHeader *h, int phase, int grid, cudaStream_t s);
+void launch_batch_progress(const BatchHeader *h, int nslots_max, BatchProgress *out, cudaStream_t s);
+
 // geometry set-up (geometry.cu)
 int active_tiles(const GridDesc &g, const uint8_t *d_type, unsigned **d_tiles, int *ntiles, cudaStream_t s);
+// host list of the tx x ty tiles holding at least one fluid cell (bx | by << 16);
+// 0, or 2 (allocation) / 5 (CUDA error)
+int active_tile_list(const GridDesc &g, const uint8_t *d_type, int tx, int ty, std::vector<unsigned> &list,
+                     cudaStream_t s);
 int setup_geometry(const GridDesc &g, int bc, const double *d_phi, double *d_nx, double *d_ny, uint8_t *d_type,
                    GhostRec **d_ghosts, int *nghost, cudaStream_t s);
 
@@ -161,6 +223,11 @@ int case_sweep_unguarded(ibtfo_case *c);
 int case_fill(ibtfo_case *c, int ghosts, int ring);
 int case_reduce_current(ibtfo_case *c);
 double case_cfl(const ibtfo_case *c);
+// batch view of a case: its sweep/fill arguments and the arguments of the batch kernel variant
+int case_batch_view(ibtfo_case *c, SweepArgs *s, FillArgs *f, int *scheme, int *riemann, int *limiter,
+                    int *precision, int *has_state);
+cudaStream_t case_stream(const ibtfo_case *c);
+int case_device(const ibtfo_case *c);
 double case_gamma(const ibtfo_case *c);
 void set_last_error(const char *msg);
 

@@ -22,7 +22,11 @@ template <typename T>
 struct GasConst
 {
     T g, gm1, c1, c2; // gamma, gamma - 1, (gamma+1)/(2 gamma), (gamma-1)/(2 gamma)
-    __device__ __forceinline__ GasConst(T g_, T gm1_, T c1_, T c2_) : g(g_), gm1(gm1_), c1(c1_), c2(c2_) {}
+    T igm1, ig2;      // 1/(gamma - 1), 1/(2 gamma)
+    __device__ __forceinline__ GasConst(T g_, T gm1_, T c1_, T c2_, T igm1_, T ig2_)
+        : g(g_), gm1(gm1_), c1(c1_), c2(c2_), igm1(igm1_), ig2(ig2_)
+    {
+    }
 };
 
 // 1/x: hardware seed + two Newton steps (within an ulp of the rounded value)
@@ -35,9 +39,23 @@ __device__ __forceinline__ double rcp_t(double x)
     e = fma(-x, y, 1.0);
     return fma(y, e, y);
 }
-__device__ __forceinline__ float rcp_t(float x) { return __frcp_rn(x); }
+// FP32 form: hardware reciprocal seed + one Newton step (within ~1 ulp; no
+// correctly-rounded slow path), and the hardware square root approximation
+// (relative error ~2^-23); the FP32 form makes no bitwise claim
+__device__ __forceinline__ float rcp_t(float x)
+{
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    const float e = fmaf(-x, y, 1.0f);
+    return fmaf(y, e, y);
+}
 __device__ __forceinline__ double sqrt_t(double x) { return sqrt(x); }
-__device__ __forceinline__ float sqrt_t(float x) { return sqrtf(x); }
+__device__ __forceinline__ float sqrt_t(float x)
+{
+    float y;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
 __device__ __forceinline__ double fma_t(double a, double b, double c) { return fma(a, b, c); }
 __device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
 
@@ -173,8 +191,8 @@ __device__ __forceinline__ void sw_split(const T U[4], const GasConst<T> &K, T F
     const T d2 = (T)1e-12; // delta = 1e-6 (:193)
     auto lam = [&](T x) { return (T)0.5 * (x + (T)SIGN * sqrt_t(x * x + d2)); };
     const T l1 = lam(s.un), l3 = lam(s.un - s.a), l4 = lam(s.un + s.a);
-    const T h = s.p / K.gm1 * s.ir + (T)0.5 * (s.un * s.un + s.ut * s.ut) + s.p * s.ir; // e + |u|^2/2 + p/rho
-    const T w = s.r / ((T)2 * K.g);
+    const T h = s.p * K.igm1 * s.ir + (T)0.5 * (s.un * s.un + s.ut * s.ut) + s.p * s.ir; // e + |u|^2/2 + p/rho
+    const T w = s.r * K.ig2;
     F[0] = w * ((T)2 * K.gm1 * l1 + l3 + l4);
     F[NRM] = w * ((T)2 * K.gm1 * s.un * l1 + (s.un - s.a) * l3 + (s.un + s.a) * l4);
     F[3 - NRM] = w * s.ut * ((T)2 * K.gm1 * l1 + l3 + l4);

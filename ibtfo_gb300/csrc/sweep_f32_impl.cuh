@@ -8,11 +8,11 @@
 // adds the FP32 increment to the (hi, lo) pair with an error-free sum
 // (TwoSum, then renormalisation), so the stored state keeps about 48
 // significant bits across steps instead of accumulating one FP32 rounding
-// per step.  The mass sum and the CFL time step are formed in FP64.
+// per step.  The mass sum and the CFL time step are formed in FP64 once per
+// block, from FP32 (compensated for the mass) block reductions.
 //
 // Memory per cell update: 32 B read (hi, lo x 4) + 32 B write + 1 B type,
-// the same bytes as the FP64 path but a quarter of the FP64 instructions run
-// on the FP32 pipes, so this form can approach the HBM bound.
+// the same bytes as the FP64 path, with the arithmetic on the FP32 pipes.
 #pragma once
 
 #include "internal.h"
@@ -33,39 +33,50 @@ __device__ __forceinline__ void two_float_sub(float &hi, float &lo, float d)
     hi = h3;
 }
 
-template <int SCH, int RIE, int LIM>
-__global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_f32_kernel(const SweepArgs a)
+// (h, l) += (oh, ol), error-free on the hi parts (TwoSum)
+__device__ __forceinline__ void two_float_acc(float &h, float &l, float oh, float ol)
 {
-    constexpr int TX = TILE_X, TY = TILE_Y, NT = TX * TY;
-    constexpr int WX = TX + 4, WY = TY + 4;
-    __shared__ float sU[4][WY][WX];
-    __shared__ float sF[4][TY + 1][TX + 1];
-    __shared__ float sG[4][TY + 1][TX];
-    __shared__ unsigned char sKeep[TY + 1][TX];
-    __shared__ float sC[4]; // dt/dx, dt/dy, dt/(2dx), dt/(2dy) of this step (one thread computes them)
+    const float s = h + oh, bb = s - h;
+    const float err = (h - (s - bb)) + (oh - bb);
+    h = s;
+    l = l + ol + err;
+}
 
-    const GridDesc &g = a.g;
-    DevState *st = a.st;
-    if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0)
-        st->fill_pending = 0;
-    if (a.guard && !(st->now_t < a.t_end && st->iter < a.max_iter))
-        return;
-    const double dt = st->dt; // read by thread 0 into sC
-    const int cur = st->cur;
-    const float *__restrict__ U = reinterpret_cast<const float *>(cur ? a.buf1 : a.buf0);
-    float *__restrict__ V = reinterpret_cast<float *>(cur ? a.buf0 : a.buf1);
+// per-thread statistics in FP32; the mass as a compensated (hi, lo) pair
+struct CellStats32
+{
+    float amax = 0.0f, umax = 0.0f, vmax = 0.0f, mhi = 0.0f, mlo = 0.0f;
+    int nans = 0;
+};
+
+template <int TX, int TY>
+struct SweepSmem32
+{
+    float sU[4][TY + 4][TX + 4];
+    float sF[4][TY + 1][TX + 1];
+    float sG[4][TY + 1][TX];
+    float sC[4]; // dt/dx, dt/dy, dt/(2dx), dt/(2dy) of this step (one thread computes them)
+    unsigned char sKeep[TY + 1][TX];
+};
+
+// Advance the tile whose first interior cell is (i0, j0) from U into V (float
+// planes: 0-3 hi, 4-7 lo) and accumulate the statistics of the updated cells.
+template <int SCH, int RIE, int LIM, int TX, int TY, int NT>
+__device__ __forceinline__ void sweep_tile32(SweepSmem32<TX, TY> &s, const GridDesc &g, const float *__restrict__ U,
+                                             float *__restrict__ V, const uint8_t *__restrict__ type, int i0, int j0,
+                                             double dt, CellStats32 &cs)
+{
+    constexpr int WX = TX + 4, WY = TY + 4;
     const long long P = g.plane;
     const int pitch = g.pitch;
-    const unsigned tile = a.tiles[blockIdx.x];
-    const int i0 = g.ng + (int)(tile & 0xFFFFu) * TX;
-    const int j0 = g.ng + (int)(tile >> 16) * TY;
     const int tid = threadIdx.x;
     if (tid == 0)
     {
-        sC[0] = (float)(dt / g.dx);
-        sC[1] = (float)(dt / g.dy);
-        sC[2] = (float)(0.5 * dt / g.dx);
-        sC[3] = (float)(0.5 * dt / g.dy);
+        const float dtf = (float)dt;
+        s.sC[0] = dtf * g.idxf;
+        s.sC[1] = dtf * g.idyf;
+        s.sC[2] = 0.5f * s.sC[0];
+        s.sC[3] = 0.5f * s.sC[1];
     }
 
     for (int q = tid; q < 4 * WX * WY; q += NT)
@@ -77,12 +88,12 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_f32_kernel(const SweepAr
         float v = 0.0f;
         if (gi < g.M && gj < g.N)
             v = U[k * P + (long long)gj * pitch + gi];
-        sU[k][ly][lx] = v;
+        s.sU[k][ly][lx] = v;
     }
     __syncthreads();
 
-    const GasConst<float> K(g.gf, g.gm1f, g.c1f, g.c2f);
-    const float hx2 = sC[2], hy2 = sC[3];
+    const GasConst<float> K(g.gf, g.gm1f, g.c1f, g.c2f, g.igm1f, g.ig2f);
+    const float hx2 = s.sC[2], hy2 = s.sC[3];
     constexpr int NXF = (TX + 1) * (TY + 1);
     constexpr int NYF = TX * (TY + 1);
     for (int q = tid; q < NXF + NYF; q += NT)
@@ -94,15 +105,15 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_f32_kernel(const SweepAr
 #pragma unroll
             for (int k = 0; k < 4; k++)
             {
-                c0[k] = sU[k][r + 1][fc];
-                c1[k] = sU[k][r + 1][fc + 1];
-                c2[k] = sU[k][r + 1][fc + 2];
-                c3[k] = sU[k][r + 1][fc + 3];
+                c0[k] = s.sU[k][r + 1][fc];
+                c1[k] = s.sU[k][r + 1][fc + 1];
+                c2[k] = s.sU[k][r + 1][fc + 2];
+                c3[k] = s.sU[k][r + 1][fc + 3];
             }
             x_face_fast<float, SCH, RIE, LIM>(c0, c1, c2, c3, K, hx2, f);
 #pragma unroll
             for (int k = 0; k < 4; k++)
-                sF[k][r][fc] = f[k];
+                s.sF[k][r][fc] = f[k];
         }
         else
         {
@@ -111,41 +122,38 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_f32_kernel(const SweepAr
 #pragma unroll
             for (int k = 0; k < 4; k++)
             {
-                c0[k] = sU[k][r][c + 2];
-                c1[k] = sU[k][r + 1][c + 2];
-                c2[k] = sU[k][r + 2][c + 2];
-                c3[k] = sU[k][r + 3][c + 2];
+                c0[k] = s.sU[k][r][c + 2];
+                c1[k] = s.sU[k][r + 1][c + 2];
+                c2[k] = s.sU[k][r + 2][c + 2];
+                c3[k] = s.sU[k][r + 3][c + 2];
             }
             float stray = 0.0f;
             int keep = y_face_fast<float, SCH, RIE, LIM>(c0, c1, c2, c3, K, hy2, f, &stray);
 #pragma unroll
             for (int k = 0; k < 4; k++)
-                sG[k][r][c] = f[k];
-            sKeep[r][c] = (unsigned char)keep;
+                s.sG[k][r][c] = f[k];
+            s.sKeep[r][c] = (unsigned char)keep;
         }
     }
     __syncthreads();
 
-    // per-cell statistics in FP32; the mass as a compensated (hi, lo) float
-    // pair, converted to FP64 once per warp
-    float famax = 0.0f, fumax = 0.0f, fvmax = 0.0f, mhi = 0.0f, mlo = 0.0f;
-    int nans = 0;
+    for (int cell = tid; cell < TX * TY; cell += NT)
     {
-        const int c = tid % TX, r = tid / TX;
+        const int c = cell % TX, r = cell / TX;
         const int i = i0 + c, j = j0 + r;
-        if (i < g.ng + g.n_x && j < g.ng + g.n_y && a.type[(long long)j * pitch + i] == 0)
+        if (i < g.ng + g.n_x && j < g.ng + g.n_y && type[(long long)j * pitch + i] == 0)
         {
             const long long o = (long long)j * pitch + i;
-            const int kp = sKeep[r + 1][c], km = sKeep[r][c];
-            const float lx = sC[0], ly = sC[1];
+            const int kp = s.sKeep[r + 1][c], km = s.sKeep[r][c];
+            const float lx = s.sC[0], ly = s.sC[1];
             float hi[4], lo[4];
 #pragma unroll
             for (int k = 0; k < 4; k++)
             {
-                const float gp = ((kp >> k) & 1) ? sF[k][r + 1][c + 1] : sG[k][r + 1][c];
-                const float gm = ((km >> k) & 1) ? sF[k][r][c + 1] : sG[k][r][c];
-                const float d = fmaf(lx, sF[k][r + 1][c + 1] - sF[k][r + 1][c], ly * (gp - gm));
-                hi[k] = sU[k][r + 2][c + 2];
+                const float gp = ((kp >> k) & 1) ? s.sF[k][r + 1][c + 1] : s.sG[k][r + 1][c];
+                const float gm = ((km >> k) & 1) ? s.sF[k][r][c + 1] : s.sG[k][r][c];
+                const float d = fmaf(lx, s.sF[k][r + 1][c + 1] - s.sF[k][r + 1][c], ly * (gp - gm));
+                hi[k] = s.sU[k][r + 2][c + 2];
                 lo[k] = U[(4 + k) * P + o];
                 two_float_sub(hi[k], lo[k], d);
                 V[k * P + o] = hi[k];
@@ -155,39 +163,97 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_f32_kernel(const SweepAr
             const float ir = rcp_t(hi[0]);
             const float u = hi[1] * ir, w = hi[2] * ir;
             const float p = K.gm1 * (hi[3] - 0.5f * hi[0] * (u * u + w * w));
-            famax = sqrtf(K.g * p * ir); // NaN (ignored by the maximum) where p < 0
-            fumax = fabsf(u);
-            fvmax = fabsf(w);
-            mhi = hi[0];
-            mlo = lo[0];
-            nans = (isnan(hi[0]) || isnan(hi[1]) || isnan(hi[2]) || isnan(hi[3])) ? 1 : 0;
+            cs.amax = fmaxf(cs.amax, sqrt_t(K.g * p * ir)); // NaN (ignored by the maximum) where p < 0
+            cs.umax = fmaxf(cs.umax, fabsf(u));
+            cs.vmax = fmaxf(cs.vmax, fabsf(w));
+            two_float_acc(cs.mhi, cs.mlo, hi[0], lo[0]);
+            cs.nans += (isnan(hi[0]) || isnan(hi[1]) || isnan(hi[2]) || isnan(hi[3])) ? 1 : 0;
         }
     }
+}
+
+// Block reduction in FP32 (compensated for the mass); thread 0 converts the
+// block's values to FP64 once (an FP64 instruction costs 64 FP32 ones on
+// this part), then block_commit_finalize.
+template <int NT>
+__device__ __forceinline__ void block_reduce_finalize32(CellStats32 cs, DevState *st, double *partial,
+                                                        const GridDesc &g, unsigned nblocks, unsigned bid)
+{
+    __shared__ float red[5][NT / 32];
+    __shared__ int rnan[NT / 32];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1)
     {
-        famax = fmaxf(famax, __shfl_xor_sync(0xffffffffu, famax, o));
-        fumax = fmaxf(fumax, __shfl_xor_sync(0xffffffffu, fumax, o));
-        fvmax = fmaxf(fvmax, __shfl_xor_sync(0xffffffffu, fvmax, o));
-        // (mhi, mlo) += the partner's pair, error-free on the hi parts
-        const float oh = __shfl_xor_sync(0xffffffffu, mhi, o), ol = __shfl_xor_sync(0xffffffffu, mlo, o);
-        const float s = mhi + oh, bb = s - mhi;
-        const float err = (mhi - (s - bb)) + (oh - bb);
-        mhi = s;
-        mlo = mlo + ol + err;
+        cs.amax = fmaxf(cs.amax, __shfl_xor_sync(0xffffffffu, cs.amax, o));
+        cs.umax = fmaxf(cs.umax, __shfl_xor_sync(0xffffffffu, cs.umax, o));
+        cs.vmax = fmaxf(cs.vmax, __shfl_xor_sync(0xffffffffu, cs.vmax, o));
+        const float oh = __shfl_xor_sync(0xffffffffu, cs.mhi, o), ol = __shfl_xor_sync(0xffffffffu, cs.mlo, o);
+        two_float_acc(cs.mhi, cs.mlo, oh, ol);
+        cs.nans += __shfl_xor_sync(0xffffffffu, cs.nans, o);
     }
-    // one FP64 value per warp: the lane-0 value carries the warp's sums
-    const bool lead = (threadIdx.x & 31) == 0;
-    const double amax = lead ? (double)famax : 0.0, umax = lead ? (double)fumax : 0.0,
-                 vmax = lead ? (double)fvmax : 0.0;
-    const double mass = lead ? ((double)mhi + (double)mlo) * (g.dx * g.dy) : 0.0;
-    block_reduce_finalize<NT, true>(amax, umax, vmax, mass, nans, st, a.partial, g, true, false);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0)
+    {
+        red[0][wid] = cs.amax;
+        red[1][wid] = cs.umax;
+        red[2][wid] = cs.vmax;
+        red[3][wid] = cs.mhi;
+        red[4][wid] = cs.mlo;
+        rnan[wid] = cs.nans;
+    }
+    __syncthreads();
+    double amax = 0.0, umax = 0.0, vmax = 0.0, mass = 0.0;
+    int n = 0;
+    if (threadIdx.x == 0)
+    {
+        float fa = red[0][0], fu = red[1][0], fv = red[2][0], h = red[3][0], l = red[4][0];
+        n = rnan[0];
+        for (int w = 1; w < NT / 32; w++)
+        {
+            fa = fmaxf(fa, red[0][w]);
+            fu = fmaxf(fu, red[1][w]);
+            fv = fmaxf(fv, red[2][w]);
+            two_float_acc(h, l, red[3][w], red[4][w]);
+            n += rnan[w];
+        }
+        amax = (double)fa;
+        umax = (double)fu;
+        vmax = (double)fv;
+        mass = ((double)h + (double)l) * g.dxdy;
+    }
+    block_commit_finalize<NT>(amax, umax, vmax, mass, n, st, partial, g, true, false, nblocks, bid);
+}
+
+// one case: one CTA per active tile
+template <int SCH, int RIE, int LIM>
+__global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_f32_kernel(const SweepArgs a)
+{
+    constexpr int NT = TILE_X * TILE_Y;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    auto &s = *reinterpret_cast<SweepSmem32<TILE_X, TILE_Y> *>(smem_raw);
+
+    const GridDesc &g = a.g;
+    DevState *st = a.st;
+    if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0)
+        st->fill_pending = 0;
+    if (a.guard && !(st->now_t < a.t_end && st->iter < a.max_iter))
+        return;
+    const double dt = st->dt;
+    const int cur = st->cur;
+    const float *U = reinterpret_cast<const float *>(cur ? a.buf1 : a.buf0);
+    float *V = reinterpret_cast<float *>(cur ? a.buf0 : a.buf1);
+    const unsigned tile = a.tiles[blockIdx.x];
+    const int i0 = g.ng + (int)(tile & 0xFFFFu) * TILE_X;
+    const int j0 = g.ng + (int)(tile >> 16) * TILE_Y;
+    CellStats32 cs;
+    sweep_tile32<SCH, RIE, LIM, TILE_X, TILE_Y, NT>(s, g, U, V, a.type, i0, j0, dt, cs);
+    block_reduce_finalize32<NT>(cs, st, a.partial, g, gridDim.x * gridDim.y, blockIdx.y * gridDim.x + blockIdx.x);
 }
 
 template <int SCH, int RIE, int LIM>
 void launch_sweep_f32(const SweepArgs &a, dim3 grid, dim3 block, cudaStream_t s)
 {
-    sweep_f32_kernel<SCH, RIE, LIM><<<grid, block, 0, s>>>(a);
+    sweep_f32_kernel<SCH, RIE, LIM><<<grid, block, sizeof(SweepSmem32<TILE_X, TILE_Y>), s>>>(a);
 }
 
 } // namespace ibtfo

@@ -1,5 +1,5 @@
-// The fused per-step sweep: one CTA advances a TILE_X x TILE_Y block of
-// interior cells by one time step.
+// The fused per-step sweep: one CTA advances a TX x TY tile of interior
+// cells by one time step.
 //
 // It restates, in one pass over shared memory, the reference Advance
 // (MUSCL_Scheme.cpp:6-152 / MHM_Scheme.cpp:5-203 / Godunov_Scheme.cpp:6-140):
@@ -12,6 +12,10 @@
 // (MUSCL/EQDefine.H:35-36) and skips the store in some branches; the
 // kernel keeps both face fluxes in shared memory and takes the X-face flux
 // of the same cell where the reference would have left it in place.
+//
+// The tile body (sweep_tile64) is shared by two frames: sweep_kernel (one
+// case, one CTA per active tile) and the persistent batched kernel of
+// batch.cu (many cases, CTAs loop over one tile table).
 #pragma once
 
 #include "internal.h"
@@ -26,58 +30,20 @@ __device__ __forceinline__ void atomic_max_nonneg(unsigned long long *addr, doub
     atomicMax(addr, (unsigned long long)__double_as_longlong(v));
 }
 
-// Block-wide reduction of (max a, max |u|, max |v|, sum mass, nan count),
-// then the last block to finish computes the next dt and advances the
-// reference loop accounting.  Deterministic: the mass partials are summed
-// in a fixed order whichever block finishes last.
-// WARP_DONE: the caller has already reduced each warp into its lane 0 (the
-// FP32 form does that in FP32 so no per-cell FP64 work remains).
-template <int NT, bool WARP_DONE = false>
-__device__ __forceinline__ void block_reduce_finalize(double amax, double umax, double vmax, double mass, int nans,
-                                                      DevState *st, double *partial, const GridDesc &g,
-                                                      bool step_accounting, bool set_start)
+// Commit one block's (max a, max |u|, max |v|, mass, nan count), held by
+// thread 0, to the step's device state; the last of the case's `nblocks`
+// blocks to finish computes the next dt and advances the reference loop
+// accounting.  Deterministic: the mass partials are summed in a fixed order
+// (by block index `bid`) whichever block finishes last.  Called by every
+// thread of the block.
+template <int NT>
+__device__ __forceinline__ void block_commit_finalize(double a, double u, double v, double m, int n, DevState *st,
+                                                      double *partial, const GridDesc &g, bool step_accounting,
+                                                      bool set_start, unsigned nblocks, unsigned bid)
 {
-    __shared__ double red[4][NT / 32];
-    __shared__ int rnan[NT / 32];
     __shared__ bool last;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (!WARP_DONE)
-    {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
-        {
-            amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
-            umax = fmax(umax, __shfl_xor_sync(0xffffffffu, umax, o));
-            vmax = fmax(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
-            mass += __shfl_xor_sync(0xffffffffu, mass, o);
-        }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
-        nans += __shfl_xor_sync(0xffffffffu, nans, o);
-    if (lane == 0)
-    {
-        red[0][wid] = amax;
-        red[1][wid] = umax;
-        red[2][wid] = vmax;
-        red[3][wid] = mass;
-        rnan[wid] = nans;
-    }
-    __syncthreads();
-    const unsigned nblocks = gridDim.x * gridDim.y;
-    const unsigned bid = blockIdx.y * gridDim.x + blockIdx.x;
     if (threadIdx.x == 0)
     {
-        double a = red[0][0], u = red[1][0], v = red[2][0], m = red[3][0];
-        int n = rnan[0];
-        for (int w = 1; w < NT / 32; w++)
-        {
-            a = fmax(a, red[0][w]);
-            u = fmax(u, red[1][w]);
-            v = fmax(v, red[2][w]);
-            m += red[3][w];
-            n += rnan[w];
-        }
         if (a > 0) atomic_max_nonneg(&st->amax_bits, a);
         if (u > 0) atomic_max_nonneg(&st->umax_bits, u);
         if (v > 0) atomic_max_nonneg(&st->vmax_bits, v);
@@ -134,78 +100,124 @@ __device__ __forceinline__ void block_reduce_finalize(double amax, double umax, 
         vs->ticket = 0u;
         __threadfence();
     }
+    __syncthreads(); // msum and `last` are reused by the next tile of a persistent CTA
+}
+
+// Per-thread CFL maxima, mass and NaN count of the cells a thread updated
+struct CellStats
+{
+    double amax = 0.0, umax = 0.0, vmax = 0.0, mass = 0.0;
+    int nans = 0;
+};
+
+// Block-wide FP64 reduction of the per-thread statistics, then
+// block_commit_finalize.
+template <int NT>
+__device__ __forceinline__ void block_reduce_finalize(CellStats cs, DevState *st, double *partial, const GridDesc &g,
+                                                      bool step_accounting, bool set_start, unsigned nblocks,
+                                                      unsigned bid)
+{
+    __shared__ double red[4][NT / 32];
+    __shared__ int rnan[NT / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        cs.amax = fmax(cs.amax, __shfl_xor_sync(0xffffffffu, cs.amax, o));
+        cs.umax = fmax(cs.umax, __shfl_xor_sync(0xffffffffu, cs.umax, o));
+        cs.vmax = fmax(cs.vmax, __shfl_xor_sync(0xffffffffu, cs.vmax, o));
+        cs.mass += __shfl_xor_sync(0xffffffffu, cs.mass, o);
+        cs.nans += __shfl_xor_sync(0xffffffffu, cs.nans, o);
+    }
+    if (lane == 0)
+    {
+        red[0][wid] = cs.amax;
+        red[1][wid] = cs.umax;
+        red[2][wid] = cs.vmax;
+        red[3][wid] = cs.mass;
+        rnan[wid] = cs.nans;
+    }
+    __syncthreads();
+    double a = 0.0, u = 0.0, v = 0.0, m = 0.0;
+    int n = 0;
+    if (threadIdx.x == 0)
+    {
+        a = red[0][0], u = red[1][0], v = red[2][0], m = red[3][0];
+        n = rnan[0];
+        for (int w = 1; w < NT / 32; w++)
+        {
+            a = fmax(a, red[0][w]);
+            u = fmax(u, red[1][w]);
+            v = fmax(v, red[2][w]);
+            m += red[3][w];
+            n += rnan[w];
+        }
+    }
+    block_commit_finalize<NT>(a, u, v, m, n, st, partial, g, step_accounting, set_start, nblocks, bid);
 }
 
 // CFL and mass contributions of one fluid cell of the new state
 // (ComputeDt.cpp:38-45, CaculateMass.cpp:36)
-__device__ __forceinline__ void cell_stats(const double v[4], double gam, double dx, double dy, double &amax,
-                                           double &umax, double &vmax, double &mass, int &nans)
+__device__ __forceinline__ void cell_stats(const double v[4], double gam, double dx, double dy, CellStats &cs)
 {
     double rho = v[0];
     double u = v[1] / v[0];
     double w = v[2] / v[0];
     double p = (gam - 1) * (v[3] - 0.5 * rho * (u * u + w * w));
     double a = pow_half(gam * p / rho);
-    amax = fmax(amax, a);
-    umax = fmax(umax, fabs(u));
-    vmax = fmax(vmax, fabs(w));
-    mass += v[0] * dx * dy;
-    nans += (isnan(v[0]) || isnan(v[1]) || isnan(v[2]) || isnan(v[3])) ? 1 : 0;
+    cs.amax = fmax(cs.amax, a);
+    cs.umax = fmax(cs.umax, fabs(u));
+    cs.vmax = fmax(cs.vmax, fabs(w));
+    cs.mass += v[0] * dx * dy;
+    cs.nans += (isnan(v[0]) || isnan(v[1]) || isnan(v[2]) || isnan(v[3])) ? 1 : 0;
 }
 
 // the same statistics with a shared reciprocal (fp64_fast)
 __device__ __forceinline__ void cell_stats_fast(const double v[4], const GasConst<double> &K, double dxdy,
-                                                double &amax, double &umax, double &vmax, double &mass, int &nans)
+                                                CellStats &cs)
 {
     const double ir = rcp_t(v[0]);
     const double u = v[1] * ir, w = v[2] * ir;
     const double p = K.gm1 * (v[3] - 0.5 * v[0] * (u * u + w * w));
     const double a = pow_half(K.g * p * ir);
-    amax = fmax(amax, a);
-    umax = fmax(umax, fabs(u));
-    vmax = fmax(vmax, fabs(w));
-    mass += v[0] * dxdy;
-    nans += (isnan(v[0]) || isnan(v[1]) || isnan(v[2]) || isnan(v[3])) ? 1 : 0;
+    cs.amax = fmax(cs.amax, a);
+    cs.umax = fmax(cs.umax, fabs(u));
+    cs.vmax = fmax(cs.vmax, fabs(w));
+    cs.mass += v[0] * dxdy;
+    cs.nans += (isnan(v[0]) || isnan(v[1]) || isnan(v[2]) || isnan(v[3])) ? 1 : 0;
 }
 
-template <int SCH, int RIE, int LIM, int FAST>
-__global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_kernel(const SweepArgs a)
+// shared memory of one FP64 tile: the tile plus two halo cells each side,
+// X faces (i+1/2, j) for i in [i0-1, i0+TX), j in [j0-1, j0+TY), Y faces
+// (i, j+1/2) for i in [i0, i0+TX), j in [j0-1, j0+TY)
+template <int TX, int TY>
+struct SweepSmem64
 {
-    constexpr int TX = TILE_X, TY = TILE_Y, NT = TX * TY;
-    constexpr int WX = TX + 4, WY = TY + 4; // tile plus two halo cells each side
-    __shared__ double sU[4][WY][WX];
-    __shared__ double sF[4][TY + 1][TX + 1]; // X faces (i+1/2, j), i in [i0-1, i0+TX), j in [j0-1, j0+TY)
-    __shared__ double sG[4][TY + 1][TX];     // Y faces (i, j+1/2), i in [i0, i0+TX), j in [j0-1, j0+TY)
-    __shared__ unsigned char sKeep[TY + 1][TX];
-    __shared__ double sC[4]; // fp64_fast: dt/dx, dt/dy, dt/(2dx), dt/(2dy), computed once per block
+    double sU[4][TY + 4][TX + 4];
+    double sF[4][TY + 1][TX + 1];
+    double sG[4][TY + 1][TX];
+    double sC[4]; // fp64_fast: dt/dx, dt/dy, dt/(2dx), dt/(2dy), computed once per tile
+    unsigned char sKeep[TY + 1][TX];
+};
 
-    const GridDesc &g = a.g;
-    DevState *st = a.st;
-    if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0)
-        st->fill_pending = 0;
-    // reference loop condition, Test/Sod/Sod.cpp:123
-    if (a.guard && !(st->now_t < a.t_end && st->iter < a.max_iter))
-        return;
-    const double dt = st->dt;
-    const int cur = st->cur;
-    const double *__restrict__ U = cur ? a.buf1 : a.buf0;
-    double *__restrict__ V = cur ? a.buf0 : a.buf1;
+// Advance the tile whose first interior cell is (i0, j0) from U into V and
+// accumulate the statistics of the updated cells.  All NT threads call it.
+template <int SCH, int RIE, int LIM, int FAST, int TX, int TY, int NT>
+__device__ __forceinline__ void sweep_tile64(SweepSmem64<TX, TY> &s, const GridDesc &g, const double *__restrict__ U,
+                                             double *__restrict__ V, const uint8_t *__restrict__ type, int i0, int j0,
+                                             double dt, CellStats &cs)
+{
+    constexpr int WX = TX + 4, WY = TY + 4;
     const long long P = g.plane;
     const int pitch = g.pitch;
-    // tiles without fluid cells are skipped: nothing in them is updated or
-    // counted by the reference (updates, ComputeDt and CaculateMass all test
-    // the cell type), so the launch covers the active tiles only
-    const unsigned tile = a.tiles[blockIdx.x];
-    const int i0 = g.ng + (int)(tile & 0xFFFFu) * TX;
-    const int j0 = g.ng + (int)(tile >> 16) * TY;
     const int tid = threadIdx.x;
     constexpr bool FASTPHYS = FAST || RIE == HLLCT; // faces evaluated by physics_fast.cuh
     if (FASTPHYS && tid == 0)
     {
-        sC[0] = dt / g.dx;
-        sC[1] = dt / g.dy;
-        sC[2] = 0.5 * dt / g.dx;
-        sC[3] = 0.5 * dt / g.dy;
+        s.sC[0] = dt * g.idx;
+        s.sC[1] = dt * g.idy;
+        s.sC[2] = 0.5 * s.sC[0];
+        s.sC[3] = 0.5 * s.sC[1];
     }
 
     // stage the tile and its halo (always inside the padded array: ng >= 2)
@@ -218,13 +230,13 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_kernel(const SweepArgs a
         double v = 0.0;
         if (gi < g.M && gj < g.N)
             v = U[k * P + (long long)gj * pitch + gi];
-        sU[k][ly][lx] = v;
+        s.sU[k][ly][lx] = v;
     }
     __syncthreads();
 
     const double gam = g.gamma;
-    const GasConst<double> K(gam, g.gm1, g.c1, g.c2);
-    const double hx2 = FASTPHYS ? sC[2] : 0.0, hy2 = FASTPHYS ? sC[3] : 0.0; // MHM predictor of physics_fast
+    const GasConst<double> K(gam, g.gm1, g.c1, g.c2, g.igm1, g.ig2);
+    const double hx2 = FASTPHYS ? s.sC[2] : 0.0, hy2 = FASTPHYS ? s.sC[3] : 0.0; // MHM predictor of physics_fast
     constexpr int NXF = (TX + 1) * (TY + 1);
     constexpr int NYF = TX * (TY + 1);
     for (int q = tid; q < NXF + NYF; q += NT)
@@ -236,10 +248,10 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_kernel(const SweepArgs a
 #pragma unroll
             for (int k = 0; k < 4; k++)
             {
-                c0[k] = sU[k][r + 1][fc];
-                c1[k] = sU[k][r + 1][fc + 1];
-                c2[k] = sU[k][r + 1][fc + 2];
-                c3[k] = sU[k][r + 1][fc + 3];
+                c0[k] = s.sU[k][r + 1][fc];
+                c1[k] = s.sU[k][r + 1][fc + 1];
+                c2[k] = s.sU[k][r + 1][fc + 2];
+                c3[k] = s.sU[k][r + 1][fc + 3];
             }
             if (FASTPHYS)
                 x_face_fast<double, SCH, RIE, LIM>(c0, c1, c2, c3, K, hx2, f);
@@ -247,7 +259,7 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_kernel(const SweepArgs a
                 x_face<SCH, RIE, LIM>(c0, c1, c2, c3, gam, dt, g.dx, f);
 #pragma unroll
             for (int k = 0; k < 4; k++)
-                sF[k][r][fc] = f[k];
+                s.sF[k][r][fc] = f[k];
         }
         else
         {
@@ -256,63 +268,92 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_kernel(const SweepArgs a
 #pragma unroll
             for (int k = 0; k < 4; k++)
             {
-                c0[k] = sU[k][r][c + 2];
-                c1[k] = sU[k][r + 1][c + 2];
-                c2[k] = sU[k][r + 2][c + 2];
-                c3[k] = sU[k][r + 3][c + 2];
+                c0[k] = s.sU[k][r][c + 2];
+                c1[k] = s.sU[k][r + 1][c + 2];
+                c2[k] = s.sU[k][r + 2][c + 2];
+                c3[k] = s.sU[k][r + 3][c + 2];
             }
             double stray = 0.0;
             int keep = FASTPHYS ? y_face_fast<double, SCH, RIE, LIM>(c0, c1, c2, c3, K, hy2, f, &stray)
-                            : y_face<SCH, RIE, LIM>(c0, c1, c2, c3, gam, dt, g.dy, f, &stray);
+                                : y_face<SCH, RIE, LIM>(c0, c1, c2, c3, gam, dt, g.dy, f, &stray);
 #pragma unroll
             for (int k = 0; k < 4; k++)
-                sG[k][r][c] = f[k];
-            sKeep[r][c] = (unsigned char)keep;
+                s.sG[k][r][c] = f[k];
+            s.sKeep[r][c] = (unsigned char)keep;
         }
     }
     __syncthreads();
 
     // update (X then Y, MUSCL_Scheme.cpp:74-88 and :136-150) on fluid cells
-    double amax = 0.0, umax = 0.0, vmax = 0.0, mass = 0.0;
-    int nans = 0;
+    for (int cell = tid; cell < TX * TY; cell += NT)
     {
-        const int c = tid % TX, r = tid / TX;
+        const int c = cell % TX, r = cell / TX;
         const int i = i0 + c, j = j0 + r;
-        if (i < g.ng + g.n_x && j < g.ng + g.n_y && a.type[(long long)j * pitch + i] == 0)
+        if (i < g.ng + g.n_x && j < g.ng + g.n_y && type[(long long)j * pitch + i] == 0)
         {
-            const int kp = sKeep[r + 1][c], km = sKeep[r][c];
-            const double lx = FAST ? sC[0] : 0.0, ly = FAST ? sC[1] : 0.0;
+            const int kp = s.sKeep[r + 1][c], km = s.sKeep[r][c];
+            const double lx = FAST ? s.sC[0] : 0.0, ly = FAST ? s.sC[1] : 0.0;
             double v[4];
 #pragma unroll
             for (int k = 0; k < 4; k++)
             {
-                double gp = ((kp >> k) & 1) ? sF[k][r + 1][c + 1] : sG[k][r + 1][c];
-                double gm = ((km >> k) & 1) ? sF[k][r][c + 1] : sG[k][r][c];
+                double gp = ((kp >> k) & 1) ? s.sF[k][r + 1][c + 1] : s.sG[k][r + 1][c];
+                double gm = ((km >> k) & 1) ? s.sF[k][r][c + 1] : s.sG[k][r][c];
                 if (FAST)
                 {
-                    double x = sU[k][r + 2][c + 2] - lx * (sF[k][r + 1][c + 1] - sF[k][r + 1][c]);
+                    double x = s.sU[k][r + 2][c + 2] - lx * (s.sF[k][r + 1][c + 1] - s.sF[k][r + 1][c]);
                     v[k] = x - ly * (gp - gm);
                 }
                 else
                 {
-                    double x = sU[k][r + 2][c + 2] - dt * (sF[k][r + 1][c + 1] - sF[k][r + 1][c]) / g.dx;
+                    double x = s.sU[k][r + 2][c + 2] - dt * (s.sF[k][r + 1][c + 1] - s.sF[k][r + 1][c]) / g.dx;
                     v[k] = x - dt * (gp - gm) / g.dy;
                 }
                 V[k * P + (long long)j * pitch + i] = v[k];
             }
             if (FAST)
-                cell_stats_fast(v, K, g.dx * g.dy, amax, umax, vmax, mass, nans);
+                cell_stats_fast(v, K, g.dxdy, cs);
             else
-                cell_stats(v, gam, g.dx, g.dy, amax, umax, vmax, mass, nans);
+                cell_stats(v, gam, g.dx, g.dy, cs);
         }
     }
-    block_reduce_finalize<NT>(amax, umax, vmax, mass, nans, st, a.partial, g, true, false);
+}
+
+// one case: one CTA per active tile
+template <int SCH, int RIE, int LIM, int FAST>
+__global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_kernel(const SweepArgs a)
+{
+    constexpr int NT = TILE_X * TILE_Y;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    auto &s = *reinterpret_cast<SweepSmem64<TILE_X, TILE_Y> *>(smem_raw);
+
+    const GridDesc &g = a.g;
+    DevState *st = a.st;
+    if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0)
+        st->fill_pending = 0;
+    // reference loop condition, Test/Sod/Sod.cpp:123
+    if (a.guard && !(st->now_t < a.t_end && st->iter < a.max_iter))
+        return;
+    const double dt = st->dt;
+    const int cur = st->cur;
+    const double *U = cur ? a.buf1 : a.buf0;
+    double *V = cur ? a.buf0 : a.buf1;
+    // tiles without fluid cells are skipped: nothing in them is updated or
+    // counted by the reference (updates, ComputeDt and CaculateMass all test
+    // the cell type), so the launch covers the active tiles only
+    const unsigned tile = a.tiles[blockIdx.x];
+    const int i0 = g.ng + (int)(tile & 0xFFFFu) * TILE_X;
+    const int j0 = g.ng + (int)(tile >> 16) * TILE_Y;
+    CellStats cs;
+    sweep_tile64<SCH, RIE, LIM, FAST, TILE_X, TILE_Y, NT>(s, g, U, V, a.type, i0, j0, dt, cs);
+    block_reduce_finalize<NT>(cs, st, a.partial, g, true, false, gridDim.x * gridDim.y,
+                              blockIdx.y * gridDim.x + blockIdx.x);
 }
 
 template <int SCH, int RIE, int LIM, int FAST>
 void launch_sweep(const SweepArgs &a, dim3 grid, dim3 block, cudaStream_t s)
 {
-    sweep_kernel<SCH, RIE, LIM, FAST><<<grid, block, 0, s>>>(a);
+    sweep_kernel<SCH, RIE, LIM, FAST><<<grid, block, sizeof(SweepSmem64<TILE_X, TILE_Y>), s>>>(a);
 }
 
 } // namespace ibtfo

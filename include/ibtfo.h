@@ -206,6 +206,77 @@ ibtfo_status ibtfo_dt_mass_noalloc(const double *d_u, long long plane, int pitch
                                    int n_x, int n_y, int num_ghost_cell, double lo_x, double lo_y, double hi_x,
                                    double hi_y, double gamma, double cfl_number, double *d_out, void *stream);
 
+/* ---------------------------------------------------------------- batches
+ *
+ * No counterpart in the reference: its drivers (Test/Sod/Sod.cpp:108-181)
+ * advance one case per process.  A batch steps many cases of uneven grid
+ * sizes together: one persistent sweep kernel over a shared tile table, one
+ * boundary pass over all cases, each step captured in a CUDA graph.  Every
+ * case keeps its own dt, loop time and loop condition (t_end, max_iter);
+ * cases whose loop has ended are skipped.  A case advances in a batch bit for
+ * bit as it does alone (same kernels), and with the 32 x 8 tile shape its
+ * mass sum is bitwise identical too.
+ *
+ * Cases join with ibtfo_batch_add (after ibtfo_set_state) and leave with
+ * ibtfo_batch_remove; in between, the batch alone steps them (do not call
+ * ibtfo_advance/ibtfo_step on a case in a batch; ibtfo_get_state and
+ * ibtfo_get_progress remain valid after ibtfo_batch_synchronize).  All
+ * cases of a batch share the kernel variant (scheme, Riemann solver,
+ * limiter, precision); grid size, geometry, boundary method, domain
+ * boundaries, gamma, CFL, t_end and max_iter are per case.  Batches run the
+ * fp64_fast and FP32 compensated precisions. */
+typedef struct ibtfo_batch ibtfo_batch;
+
+enum { IBTFO_TILE_32x8 = 0, IBTFO_TILE_32x16 = 1, IBTFO_TILE_64x8 = 2 };
+
+typedef struct ibtfo_batch_config {
+    int scheme, riemann, limiter, precision; /* the kernel variant of every case */
+    int tile_shape;   /* IBTFO_TILE_*: interior cells per CTA (256 threads) */
+    int ctas_per_sm;  /* resident CTAs per SM of the persistent sweep (0: the occupancy limit) */
+    int graph_steps;  /* steps per captured graph (0: 16) */
+    int reserved[5];
+} ibtfo_batch_config;
+
+typedef struct ibtfo_batch_tiling {
+    int tile_shape, ctas_per_sm, max_ctas_per_sm, grid; /* grid = SMs x ctas_per_sm */
+    long long tiles;    /* tiles in the table */
+    double ms_per_step; /* autotuner timing (0 elsewhere) */
+    int reserved[4];
+} ibtfo_batch_tiling;
+
+ibtfo_status ibtfo_batch_create(const ibtfo_batch_config *cfg, ibtfo_batch **out);
+ibtfo_status ibtfo_batch_destroy(ibtfo_batch *b); /* does not destroy the cases */
+ibtfo_status ibtfo_batch_set_stream(ibtfo_batch *b, void *stream);
+/* add a case (state set, same kernel variant); *slot receives its slot */
+ibtfo_status ibtfo_batch_add(ibtfo_batch *b, ibtfo_case *c, int *slot);
+/* take a case out; returns without waiting: the case's own stream (its
+ * transfers, ibtfo_destroy) is ordered after the steps already queued */
+ibtfo_status ibtfo_batch_remove(ibtfo_batch *b, int slot);
+int ibtfo_batch_size(const ibtfo_batch *b);      /* cases in the batch */
+int ibtfo_batch_num_slots(const ibtfo_batch *b); /* highest used slot + 1 */
+ibtfo_case *ibtfo_batch_case(const ibtfo_batch *b, int slot);
+/* queue nsteps steps of every case (graph launches of graph_steps, then
+ * single steps); returns without waiting */
+ibtfo_status ibtfo_batch_advance(ibtfo_batch *b, int nsteps);
+/* progress of every slot: enqueue a snapshot after the queued steps, then
+ * read it (wait != 0 blocks; wait == 0 returns IBTFO_ETIMEOUT while the
+ * snapshot is not ready).  active[k] = the case's loop condition still holds. */
+ibtfo_status ibtfo_batch_progress_enqueue(ibtfo_batch *b);
+ibtfo_status ibtfo_batch_progress_read(ibtfo_batch *b, ibtfo_progress *out, int *active, int n, int wait);
+ibtfo_status ibtfo_batch_progress(ibtfo_batch *b, ibtfo_progress *out, int *active, int n);
+ibtfo_status ibtfo_batch_synchronize(ibtfo_batch *b);
+ibtfo_status ibtfo_batch_set_tiling(ibtfo_batch *b, int tile_shape, int ctas_per_sm);
+ibtfo_status ibtfo_batch_get_tiling(const ibtfo_batch *b, ibtfo_batch_tiling *t);
+/* time every tile shape x resident-CTA count on `steps` real steps of the
+ * current cases and keep the fastest (the state is the same under every
+ * tiling, so the trial steps are ordinary steps) */
+ibtfo_status ibtfo_batch_autotune(ibtfo_batch *b, int steps, ibtfo_batch_tiling *best, ibtfo_batch_tiling *trials,
+                                  int max_trials, int *n_trials);
+
+/* IBTFO_OK when every operation queued on the case's stream has finished,
+ * IBTFO_ETIMEOUT while some are pending (does not wait) */
+ibtfo_status ibtfo_query(ibtfo_case *c);
+
 /* Page-locked host memory for fast transfers (cudaHostAlloc / cudaFreeHost). */
 ibtfo_status ibtfo_host_alloc(size_t bytes, void **p);
 ibtfo_status ibtfo_host_free(void *p);
