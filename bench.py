@@ -293,6 +293,73 @@ def gpu_arm(args, rank, world, local_rank, precision=None, e2e=True, w=None, inp
     return res
 
 
+def served_request(ib, r, arrival, density_out=None):
+    from ibtfo_gb300 import cases
+    post = cases.post_shock(r.mach)
+    return ib.request(r.id, r.n_x, r.n_y, (0.0, 0.0), (r.width, r.height), r.t_end,
+                      bodies=[ib.circle(r.xc, r.yc, r.radius)], x_split=r.x_shock, left=post,
+                      right=(1.0, 0.0, 0.0, 1.0), arrival=arrival, density_out=density_out)
+
+
+def serve_leg(n_requests=24, rates=(None, 2.0), precision="fp32c", plain_precision="fp64_fast"):
+    """The served batch stream (first `n_requests` of the seeded stream):
+    cases/s and p50/p99 latency of the server at each arrival rate (None: all
+    requests at t = 0, the server's capacity), the same requests run plainly
+    one after another in `plain_precision`, and each served density against
+    the plain one (relative L1)."""
+    import ibtfo_gb300 as ib
+    from ibtfo_gb300 import cases
+    base = cases.served_stream(n_requests, 1.0, seed=42)
+    cells = sum(r.n_x * r.n_y for r in base)
+    bufs = {r.id: ib.PinnedBuffer(r.n_x * r.n_y) for r in base}
+    out = {"workload": f"shock over a cylinder, first {n_requests} requests of the seed-42 stream "
+                       f"(grids {min(r.n_x * r.n_y for r in base)}..{max(r.n_x * r.n_y for r in base)} cells, "
+                       f"{cells} cells in all), MUSCL + HLLC + minmod, IDWBaseGFM, CFL 0.45, 1.5 crossings",
+           "served_precision": precision, "plain_precision": plain_precision, "rates": []}
+    cell_updates = 0
+    for rate in rates:
+        arrivals = [0.0] * n_requests if rate is None else \
+            [r.arrival for r in cases.served_stream(n_requests, rate, seed=42)]
+        with ib.Server(precision=precision, chunk_steps=32, tile_shape="auto") as srv:
+            for r, a in zip(base, arrivals):
+                srv.submit(served_request(ib, r, a, density_out=bufs[r.id]))
+            srv.start()
+            srv.run(max_seconds=1200)
+            res = srv.poll(max_results=n_requests + 8)
+            st = srv.stats()
+        lat = sorted(x["finished"] - x["arrival"] for x in res)
+        span = max(x["finished"] for x in res)
+        cell_updates = sum(r.n_x * r.n_y * x["iter"] for r, x in zip(base, sorted(res, key=lambda q: q["id"])))
+        out["rates"].append({
+            "rate_per_s": rate if rate is not None else "all at t=0", "cases": len(res),
+            "failed": sum(1 for x in res if x["status"] != 0), "seconds": span, "cases_per_s": len(res) / span,
+            "Gcell_updates_per_s": cell_updates / span / 1e9,
+            "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
+            "peak_active": st["peak_active"], "peak_bytes": st["peak_bytes"],
+            "tiling": {"shape": ib.TILE_SHAPES_BY_ID.get(st["tile_shape"]), "ctas_per_sm": st["ctas_per_sm"]}})
+    served_rho = {k: b.array.copy() for k, b in bufs.items()}
+    for b in bufs.values():
+        b.close()
+    # the same requests run plainly, one after another
+    errs = []
+    t0 = time.perf_counter()
+    for r in base:
+        with ib.Case(r.n_x, r.n_y, lo=(0.0, 0.0), hi=(r.width, r.height), cfl=0.45, t_end=r.t_end,
+                     max_iter=2 ** 31 - 1, scheme="MUSCL", riemann="HLLC", boundary="IDWBaseGFM",
+                     precision=plain_precision) as c:
+            c.setup_bodies([ib.circle(r.xc, r.yc, r.radius)])
+            c.init_x_split(r.x_shock, cases.post_shock(r.mach), (1.0, 0.0, 0.0, 1.0))
+            c.run()
+            rho = c.density().reshape(-1)
+        errs.append(float(np.abs(served_rho[r.id] - rho).sum() / np.abs(rho).sum()))
+    plain_s = time.perf_counter() - t0
+    out["plain"] = {"seconds": plain_s, "cases_per_s": n_requests / plain_s,
+                    "Gcell_updates_per_s": cell_updates / plain_s / 1e9}
+    out["served_vs_plain_cases_per_s"] = out["rates"][0]["cases_per_s"] / out["plain"]["cases_per_s"]
+    out["density_l1_vs_plain"] = {"max": max(errs), "median": float(np.median(errs))}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -304,10 +371,17 @@ def main():
                     help="only step this workload (profiler captures)")
     ap.add_argument("--size", type=int, default=4096, help="grid size for --profile-workload")
     ap.add_argument("--precision", default=PRECISION, choices=("fp64", "fp64_fast", "fp32c"))
+    ap.add_argument("--serve-requests", type=int, default=24, help="requests of the served-stream leg (0: skip)")
+    ap.add_argument("--serve-only", action="store_true", help="run only the served-stream leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.workload:
         profile_run(args)
+        return 0
+    if args.serve_only:
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        print(json.dumps({"serve": serve_leg(args.serve_requests)}), flush=True)
         return 0
 
     world = int(os.environ.get("WORLD_SIZE", "1"))

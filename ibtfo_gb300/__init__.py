@@ -73,6 +73,57 @@ class BatchTiling(C.Structure):
                 "ms_per_step": self.ms_per_step}
 
 
+class Body(C.Structure):
+    _fields_ = [("kind", C.c_int), ("reserved", C.c_int), ("xc", C.c_double), ("yc", C.c_double),
+                ("a", C.c_double), ("b", C.c_double), ("theta", C.c_double)]
+
+
+def circle(xc, yc, r):
+    return Body(0, 0, xc, yc, r, r, 0.0)
+
+
+def ellipse(xc, yc, a, b, theta):
+    return Body(1, 0, xc, yc, a, b, theta)
+
+
+MAX_BODIES = 8
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("scheme", C.c_int), ("riemann", C.c_int), ("limiter", C.c_int), ("precision", C.c_int),
+                ("memory_budget", C.c_longlong), ("max_active", C.c_int), ("chunk_steps", C.c_int),
+                ("tile_shape", C.c_int), ("ctas_per_sm", C.c_int), ("reserved", C.c_int * 6)]
+
+
+class Request(C.Structure):
+    _fields_ = [("id", C.c_longlong), ("arrival", C.c_double), ("n_x", C.c_int), ("n_y", C.c_int),
+                ("lo_x", C.c_double), ("lo_y", C.c_double), ("hi_x", C.c_double), ("hi_y", C.c_double),
+                ("gamma", C.c_double), ("cfl_number", C.c_double), ("t_end", C.c_double), ("max_iter", C.c_int),
+                ("boundary", C.c_int), ("global_boundary", C.c_int), ("n_bodies", C.c_int),
+                ("bodies", Body * MAX_BODIES), ("x_split", C.c_double), ("left", C.c_double * 4),
+                ("right", C.c_double * 4), ("density_out", C.c_void_p), ("reserved", C.c_int * 8)]
+
+
+class Result(C.Structure):
+    _fields_ = [("id", C.c_longlong), ("status", C.c_int), ("iter", C.c_int), ("nan_cells", C.c_int),
+                ("reserved", C.c_int), ("now_t", C.c_double), ("mass", C.c_double), ("mass_start", C.c_double),
+                ("arrival", C.c_double), ("admitted", C.c_double), ("finished", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_longlong), ("admitted", C.c_longlong), ("completed", C.c_longlong),
+                ("failed", C.c_longlong), ("pending", C.c_int), ("active", C.c_int), ("retiring", C.c_int),
+                ("peak_active", C.c_int), ("bytes_in_use", C.c_longlong), ("peak_bytes", C.c_longlong),
+                ("memory_budget", C.c_longlong), ("chunks", C.c_longlong), ("steps", C.c_longlong),
+                ("tile_shape", C.c_int), ("ctas_per_sm", C.c_int), ("reserved", C.c_int * 6)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
 TILE_SHAPES = {"32x8": 0, "32x16": 1, "64x8": 2}
 TILE_SHAPES_BY_ID = {v: k for k, v in TILE_SHAPES.items()}
 
@@ -112,6 +163,21 @@ SIGNATURES = {
     "ibtfo_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(_P)]),
     "ibtfo_host_free": (C.c_int, [_P]),
     "ibtfo_query": (C.c_int, [_P]),
+    "ibtfo_setup_bodies": (C.c_int, [_P, C.POINTER(Body), C.c_int]),
+    "ibtfo_init_x_split": (C.c_int, [_P, C.c_double, _DP, _DP]),
+    "ibtfo_post_shock_state": (C.c_int, [C.c_double, C.c_double, _DP, _DP]),
+    "ibtfo_release_geometry": (C.c_int, [_P]),
+    "ibtfo_get_density": (C.c_int, [_P, _DP, C.c_int]),
+    "ibtfo_case_bytes": (C.c_int, [C.POINTER(Config), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
+    "ibtfo_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(_P)]),
+    "ibtfo_server_destroy": (C.c_int, [_P]),
+    "ibtfo_server_submit": (C.c_int, [_P, C.POINTER(Request)]),
+    "ibtfo_server_start": (C.c_int, [_P]),
+    "ibtfo_server_clock": (C.c_double, [_P]),
+    "ibtfo_server_pump": (C.c_int, [_P, C.POINTER(C.c_int)]),
+    "ibtfo_server_run": (C.c_int, [_P, C.c_double]),
+    "ibtfo_server_poll": (C.c_int, [_P, C.POINTER(Result), C.c_int]),
+    "ibtfo_server_stats_get": (C.c_int, [_P, C.POINTER(ServerStats)]),
     "ibtfo_batch_create": (C.c_int, [C.POINTER(BatchConfig), C.POINTER(_P)]),
     "ibtfo_batch_destroy": (C.c_int, [_P]),
     "ibtfo_batch_set_stream": (C.c_int, [_P, _P]),
@@ -309,6 +375,25 @@ class Case:
     def synchronize(self):
         _check(lib().ibtfo_synchronize(self.h))
 
+    def setup_bodies(self, bodies):
+        """Geometry from analytic bodies (circle()/ellipse()), phi built on the GPU."""
+        arr = (Body * max(len(bodies), 1))(*bodies)
+        _check(lib().ibtfo_setup_bodies(self.h, arr, len(bodies)))
+
+    def init_x_split(self, x_split, left, right):
+        """Initial primitive states left of / right of x = x_split, built on the GPU."""
+        L = np.ascontiguousarray(left, dtype=np.float64)
+        R = np.ascontiguousarray(right, dtype=np.float64)
+        _check(lib().ibtfo_init_x_split(self.h, float(x_split), _dp(L), _dp(R)))
+
+    def release_geometry(self):
+        _check(lib().ibtfo_release_geometry(self.h))
+
+    def density(self):
+        out = np.empty(self.n_x * self.n_y)
+        _check(lib().ibtfo_get_density(self.h, _dp(out), 1))
+        return out.reshape(self.n_y, self.n_x)
+
     def idle(self) -> bool:
         """True when nothing queued on the case's stream is pending (does not wait)."""
         code = lib().ibtfo_query(self.h)
@@ -414,6 +499,98 @@ class Batch:
         n = C.c_int()
         _check(lib().ibtfo_batch_autotune(self.h, int(steps), C.byref(best), trials, max_trials, C.byref(n)))
         return best.as_dict(), [trials[i].as_dict() for i in range(min(n.value, max_trials))]
+
+
+def post_shock_state(mach, gamma=1.4, pre=(1.0, 0.0, 0.0, 1.0)):
+    pre = np.ascontiguousarray(pre, dtype=np.float64)
+    out = np.empty(4)
+    _check(lib().ibtfo_post_shock_state(float(mach), float(gamma), _dp(pre), _dp(out)))
+    return tuple(out)
+
+
+def case_bytes(cfg: "Config"):
+    r, s = C.c_longlong(), C.c_longlong()
+    _check(lib().ibtfo_case_bytes(C.byref(cfg), C.byref(r), C.byref(s)))
+    return r.value, s.value
+
+
+def request(id, n_x, n_y, lo, hi, t_end, bodies=(), x_split=0.0, left=(1.0, 0.0, 0.0, 1.0),
+            right=(1.0, 0.0, 0.0, 1.0), arrival=0.0, gamma=1.4, cfl=0.45, boundary="IDWBaseGFM", gbc="walls",
+            max_iter=0, density_out=None):
+    """A Request; density_out: optional PinnedBuffer (or integer address) of n_x*n_y doubles."""
+    if len(bodies) > MAX_BODIES:
+        raise ValueError(f"at most {MAX_BODIES} bodies")
+    r = Request()
+    r.id, r.arrival, r.n_x, r.n_y = int(id), float(arrival), int(n_x), int(n_y)
+    r.lo_x, r.lo_y, r.hi_x, r.hi_y = float(lo[0]), float(lo[1]), float(hi[0]), float(hi[1])
+    r.gamma, r.cfl_number, r.t_end, r.max_iter = float(gamma), float(cfl), float(t_end), int(max_iter)
+    r.boundary, r.global_boundary = BOUNDARIES[boundary], GLOBAL_BCS[gbc]
+    r.n_bodies = len(bodies)
+    for k, b in enumerate(bodies):
+        r.bodies[k] = b
+    r.x_split = float(x_split)
+    r.left[:] = [float(v) for v in left]
+    r.right[:] = [float(v) for v in right]
+    if density_out is not None:
+        r.density_out = density_out.ptr if hasattr(density_out, "ptr") else int(density_out)
+    return r
+
+
+class Server:
+    """Continuous-batching request loop (native; see ibtfo_server_* in ibtfo.h)."""
+
+    def __init__(self, scheme="MUSCL", riemann="HLLC", limiter="minmod", precision="fp32c", memory_budget=0,
+                 max_active=0, chunk_steps=32, tile_shape="32x8", ctas_per_sm=0):
+        cfg = ServerConfig(SCHEMES[scheme], RIEMANNS[riemann], LIMITERS[limiter], PRECISIONS[precision],
+                           int(memory_budget), int(max_active), int(chunk_steps),
+                           -1 if tile_shape == "auto" else TILE_SHAPES[tile_shape], int(ctas_per_sm))
+        h = _P()
+        _check(lib().ibtfo_server_create(C.byref(cfg), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().ibtfo_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def submit(self, req: "Request"):
+        _check(lib().ibtfo_server_submit(self.h, C.byref(req)))
+
+    def start(self):
+        _check(lib().ibtfo_server_start(self.h))
+
+    def clock(self):
+        return lib().ibtfo_server_clock(self.h)
+
+    def pump(self):
+        busy = C.c_int()
+        _check(lib().ibtfo_server_pump(self.h, C.byref(busy)))
+        return bool(busy.value)
+
+    def run(self, max_seconds=0.0):
+        _check(lib().ibtfo_server_run(self.h, float(max_seconds)))
+
+    def poll(self, max_results=4096):
+        out = (Result * max_results)()
+        n = lib().ibtfo_server_poll(self.h, out, max_results)
+        return [out[i].as_dict() for i in range(n)]
+
+    def stats(self):
+        st = ServerStats()
+        _check(lib().ibtfo_server_stats_get(self.h, C.byref(st)))
+        return st.as_dict()
 
 
 class Inp:

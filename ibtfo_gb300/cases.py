@@ -136,7 +136,8 @@ def cylinder_phi(g: Grid, xc, yc, r):
     """Circular body of radius r centred at (xc, yc): phi = distance to the
     circle, positive in the fluid outside it."""
     x, y = g.coords()
-    return np.ascontiguousarray(np.hypot(x - xc, y - yc) - r).reshape(-1)
+    dx, dy = x - xc, y - yc
+    return np.ascontiguousarray(np.sqrt(dx * dx + dy * dy) - r).reshape(-1)
 
 
 def uniform_init(g: Grid, types, state=(1.0, 0.0, 0.0, 1.0), gamma=1.4):
@@ -236,3 +237,59 @@ def vortex_periodic(n=4096, riemann="HLLC_Toro"):
     stays near 1e-8 after 400 steps."""
     return Workload(f"isentropic_vortex_{n}", Grid(n, n, 2, 0.0, 0.0, 10.0, 10.0), 1.4, 0.25, 10.0,
                     "MHM", riemann, "minmod", "Regular", gbc="periodic", extra={"beta": 5.0})
+
+
+# served batch stream --------------------------------------------------------
+
+
+@dataclass
+class ServedRequest:
+    id: int
+    arrival: float        # seconds after the stream starts
+    n_x: int
+    n_y: int
+    width: float
+    height: float
+    mach: float
+    xc: float
+    yc: float
+    radius: float
+    x_shock: float
+    t_end: float
+
+
+def served_stream(n_requests, rate, seed=42, min_cells=128 * 128, max_cells=2048 * 2048, crossings=1.5,
+                  gamma=1.4):
+    """Shock over an immersed cylinder, one request each, arriving as a
+    Poisson stream of `rate` requests/s: cell count log-uniform in
+    [min_cells, max_cells], aspect ratio n_x/n_y uniform in [1, 4], width 1
+    and height n_y/n_x (square cells, as the reference's coordinates assume,
+    Psy_coord.cpp:22), shock Mach uniform in [1.5, 4] starting at x = 0.1,
+    cylinder radius uniform in [0.05, 0.2] of the height at a seeded position
+    (x in [0.3, 0.7] of the width, y in [0.3, 0.7] of the height), run to
+    t_end = `crossings` domain-crossing times of the shock."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    a1 = math.sqrt(gamma)  # sound speed of the quiescent (1, 0, 0, 1) gas
+    for k in range(n_requests):
+        t += rng.exponential(1.0 / rate)
+        cells = math.exp(rng.uniform(math.log(min_cells), math.log(max_cells)))
+        aspect = rng.uniform(1.0, 4.0)
+        n_x = max(16, int(round(math.sqrt(cells * aspect))))
+        n_y = max(16, int(round(cells / n_x)))
+        mach = rng.uniform(1.5, 4.0)
+        r_frac = rng.uniform(0.05, 0.2)
+        fx, fy = rng.uniform(0.3, 0.7), rng.uniform(0.3, 0.7)
+        W, H = 1.0, n_y / n_x
+        out.append(ServedRequest(k, t, n_x, n_y, W, H, mach, fx * W, fy * H, r_frac * H, 0.1 * W,
+                                 crossings * W / (mach * a1)))
+    return out
+
+
+def served_steps_estimate(r: ServedRequest, cfl=0.45, gamma=1.4):
+    """Steps to t_end with the post-shock maximum wave speed (u2 + a2)."""
+    rho2, u2, _, p2 = post_shock(r.mach, gamma)
+    lam = u2 + math.sqrt(gamma * p2 / rho2)
+    return int(math.ceil(r.t_end / (cfl * (r.width / r.n_x) / lam)))
+

@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <initializer_list>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -145,6 +146,20 @@ static void retain_pool_memory(int device)
     done.push_back(device);
 }
 
+extern "C" {
+static ibtfo_status geometry_from_phi(ibtfo_case *c);
+static ibtfo_status finish_initial_state(ibtfo_case *c);
+}
+
+// the array-of-structures staging buffer of host transfers, allocated on first use
+static cudaError_t ensure_staging(ibtfo_case *c)
+{
+    if (c->staging)
+        return cudaSuccess;
+    const size_t cells = (size_t)c->g.M * c->g.N;
+    return cudaMallocAsync(&c->staging, sizeof(double) * 4 * cells, c->stream);
+}
+
 static int nsch_of(int bc)
 {
     switch (bc)
@@ -234,7 +249,6 @@ ibtfo_status ibtfo_create(const ibtfo_config *cfg, ibtfo_case **out)
     c->nblocks = ((k.n_x + TILE_X - 1) / TILE_X) * ((k.n_y + TILE_Y - 1) / TILE_Y);
     c->sweep = sweep_launcher(k.scheme, k.riemann, k.limiter, k.precision);
 
-    const size_t cells = (size_t)g.M * g.N;
     const size_t plane_bytes = sizeof(double) * (size_t)g.plane;
     retain_pool_memory(c->device);
     cudaError_t e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
@@ -248,7 +262,6 @@ ibtfo_status ibtfo_create(const ibtfo_config *cfg, ibtfo_case **out)
     A((void **)&c->buf[1], 4 * plane_bytes);
     if (k.boundary == IBTFO_BOUNDARY_REGULAR)
         A((void **)&c->ic, 4 * plane_bytes);
-    A((void **)&c->staging, sizeof(double) * 4 * cells);
     A((void **)&c->phi, plane_bytes);
     A((void **)&c->nx, plane_bytes);
     A((void **)&c->ny, plane_bytes);
@@ -296,8 +309,17 @@ ibtfo_status ibtfo_setup_geometry(ibtfo_case *c, const double *phi)
         return fail(IBTFO_EINVAL, "null argument");
     cudaSetDevice(c->device);
     const GridDesc &g = c->g;
+    if (!c->phi)
+        return fail(IBTFO_ESTATE, "the geometry arrays were released (ibtfo_release_geometry)");
     CK(cudaMemcpy2DAsync(c->phi, sizeof(double) * g.pitch, phi, sizeof(double) * g.M, sizeof(double) * g.M, g.N,
                          cudaMemcpyHostToDevice, c->stream));
+    return geometry_from_phi(c);
+}
+
+// normals, cell types, ghost list and tiles from the level set in c->phi
+static ibtfo_status geometry_from_phi(ibtfo_case *c)
+{
+    const GridDesc &g = c->g;
     if (c->ghosts)
     {
         cudaFreeAsync(c->ghosts, c->stream);
@@ -329,6 +351,8 @@ ibtfo_status ibtfo_get_geometry(ibtfo_case *c, double *xy)
         return fail(IBTFO_EINVAL, "null argument");
     if (!c->geometry)
         return fail(IBTFO_ESTATE, "ibtfo_setup_geometry has not run");
+    if (!c->phi)
+        return fail(IBTFO_ESTATE, "the geometry arrays were released (ibtfo_release_geometry)");
     cudaSetDevice(c->device);
     const GridDesc &g = c->g;
     std::vector<double> phi((size_t)g.plane), nx((size_t)g.plane), ny((size_t)g.plane);
@@ -462,13 +486,9 @@ ibtfo_status ibtfo_set_state(ibtfo_case *c, const double *u0)
     cudaSetDevice(c->device);
     const GridDesc &g = c->g;
     const size_t cells = (size_t)g.M * g.N;
+    CK(ensure_staging(c));
     CK(cudaMemcpyAsync(c->staging, u0, sizeof(double) * 4 * cells, cudaMemcpyHostToDevice, c->stream));
     launch_aos_to_soa(c->staging, c->buf[0], g, c->stream);
-    CK(cudaMemcpyAsync(c->buf[1], c->buf[0], sizeof(double) * 4 * (size_t)g.plane, cudaMemcpyDeviceToDevice,
-                       c->stream));
-    if (c->ic)
-        CK(cudaMemcpyAsync(c->ic, c->buf[0], sizeof(double) * 4 * (size_t)g.plane, cudaMemcpyDeviceToDevice,
-                           c->stream));
     // initial values at the corner-column sources (columns ng and N_x+ng-1, ghost rows)
     std::vector<double> ring(2 * 2 * g.ng * 4);
     for (int side = 0; side < 2; side++)
@@ -480,6 +500,20 @@ ibtfo_status ibtfo_set_state(ibtfo_case *c, const double *u0)
                 ring[(side * 2 * g.ng + rr) * 4 + k] = u0[((size_t)g.M * j + i) * 4 + k];
         }
     CK(cudaMemcpyAsync(c->ring_ic, ring.data(), sizeof(double) * ring.size(), cudaMemcpyHostToDevice, c->stream));
+    return finish_initial_state(c);
+}
+
+// buffer 0 holds the initial state and ring_ic its corner-column sources:
+// mirror it into buffer 1 (and the Regular initial copy), run the initial
+// Boundary call and the initial ComputeDt / CaculateMass (InclineSod.cpp:105-120)
+static ibtfo_status finish_initial_state(ibtfo_case *c)
+{
+    const GridDesc &g = c->g;
+    CK(cudaMemcpyAsync(c->buf[1], c->buf[0], sizeof(double) * 4 * (size_t)g.plane, cudaMemcpyDeviceToDevice,
+                       c->stream));
+    if (c->ic)
+        CK(cudaMemcpyAsync(c->ic, c->buf[0], sizeof(double) * 4 * (size_t)g.plane, cudaMemcpyDeviceToDevice,
+                           c->stream));
     DevState s{};
     const bool gfm = c->cfg.boundary != IBTFO_BOUNDARY_REGULAR;
     s.cur = gfm ? 1 : 0; // the initial Boundary call writes the ghost cells into buffer 1
@@ -517,6 +551,7 @@ ibtfo_status ibtfo_put_state(ibtfo_case *c, const double *u)
     DevState s;
     CK(cudaMemcpyAsync(&s, c->st, sizeof(DevState), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    CK(ensure_staging(c));
     CK(cudaMemcpyAsync(c->staging, u, sizeof(double) * 4 * (size_t)g.M * g.N, cudaMemcpyHostToDevice, c->stream));
     launch_aos_to_soa(c->staging, c->buf[s.cur], g, c->stream);
     CK(cudaGetLastError());
@@ -539,6 +574,127 @@ ibtfo_status ibtfo_get_progress(ibtfo_case *c, ibtfo_progress *p)
     p->dt = s.dt;
     p->mass = s.mass;
     p->mass_start = s.mass_start;
+    return IBTFO_OK;
+}
+
+ibtfo_status ibtfo_setup_bodies(ibtfo_case *c, const ibtfo_body *bodies, int n)
+{
+    if (!c || n < 0 || (n > 0 && !bodies))
+        return fail(IBTFO_EINVAL, "null case, or bodies missing");
+    if (!c->phi)
+        return fail(IBTFO_ESTATE, "the geometry arrays were released (ibtfo_release_geometry)");
+    for (int k = 0; k < n; k++)
+    {
+        const ibtfo_body &b = bodies[k];
+        if ((b.kind != IBTFO_BODY_CIRCLE && b.kind != IBTFO_BODY_ELLIPSE) || !(b.a > 0) ||
+            (b.kind == IBTFO_BODY_ELLIPSE && !(b.b > 0)))
+            return fail(IBTFO_EINVAL, "body " + std::to_string(k) + ": unknown kind or non-positive semi-axis");
+    }
+    cudaSetDevice(c->device);
+    ibtfo_body *d = nullptr;
+    if (n > 0)
+    {
+        CK(cudaMallocAsync(&d, sizeof(ibtfo_body) * n, c->stream));
+        CK(cudaMemcpyAsync(d, bodies, sizeof(ibtfo_body) * n, cudaMemcpyHostToDevice, c->stream));
+    }
+    launch_bodies_phi(c->g, d, n, c->phi, c->stream);
+    if (d)
+        cudaFreeAsync(d, c->stream);
+    CK(cudaGetLastError());
+    return geometry_from_phi(c);
+}
+
+ibtfo_status ibtfo_init_x_split(ibtfo_case *c, double x_split, const double left[4], const double right[4])
+{
+    if (!c || !left || !right)
+        return fail(IBTFO_EINVAL, "null argument");
+    if (!c->geometry)
+        return fail(IBTFO_ESTATE, "the geometry must be set up before the initial state");
+    cudaSetDevice(c->device);
+    const double g1 = c->g.gamma - 1;
+    double L[4], R[4];
+    const double *P[2] = {left, right};
+    double *Q[2] = {L, R};
+    for (int k = 0; k < 2; k++) // conserved (rho, rho u, rho v, E) as Test/Sod/Initialize.cpp:45-48
+    {
+        const double rho = P[k][0], u = P[k][1], v = P[k][2], p = P[k][3];
+        Q[k][0] = rho;
+        Q[k][1] = rho * u;
+        Q[k][2] = rho * v;
+        Q[k][3] = p / g1 + 0.5 * rho * (u * u + v * v);
+    }
+    launch_x_split_init(c->g, c->type, x_split, L, R, c->buf[0], c->ring_ic, c->stream);
+    CK(cudaGetLastError());
+    return finish_initial_state(c);
+}
+
+ibtfo_status ibtfo_post_shock_state(double mach, double gamma, const double pre[4], double post[4])
+{
+    if (!pre || !post || !(mach >= 1.0) || !(gamma > 1.0) || !(pre[0] > 0) || !(pre[3] > 0))
+        return fail(IBTFO_EINVAL, "need mach >= 1, gamma > 1, positive pre-shock density and pressure");
+    // normal shock moving in +x into the state `pre` (Rankine-Hugoniot jump conditions)
+    const double a1 = std::sqrt(gamma * pre[3] / pre[0]), m2 = mach * mach;
+    post[0] = pre[0] * (gamma + 1) * m2 / ((gamma - 1) * m2 + 2);
+    post[1] = pre[1] + 2 * a1 / (gamma + 1) * (mach - 1 / mach);
+    post[2] = pre[2];
+    post[3] = pre[3] * (2 * gamma * m2 - (gamma - 1)) / (gamma + 1);
+    return IBTFO_OK;
+}
+
+ibtfo_status ibtfo_release_geometry(ibtfo_case *c)
+{
+    if (!c)
+        return fail(IBTFO_EINVAL, "null case");
+    cudaSetDevice(c->device);
+    for (double **p : {&c->phi, &c->nx, &c->ny})
+    {
+        if (*p)
+            cudaFreeAsync(*p, c->stream);
+        *p = nullptr;
+    }
+    CK(cudaGetLastError());
+    return IBTFO_OK;
+}
+
+ibtfo_status ibtfo_get_density(ibtfo_case *c, double *out, int wait)
+{
+    if (!c || !out)
+        return fail(IBTFO_EINVAL, "null argument");
+    if (!c->state)
+        return fail(IBTFO_ESTATE, "no state");
+    cudaSetDevice(c->device);
+    const GridDesc &g = c->g;
+    const size_t n = (size_t)g.n_x * g.n_y;
+    double *d = nullptr;
+    CK(cudaMallocAsync(&d, sizeof(double) * n, c->stream));
+    launch_density(g, c->buf[0], c->buf[1], c->st, d, c->stream);
+    CK(cudaMemcpyAsync(out, d, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    cudaFreeAsync(d, c->stream);
+    if (wait)
+        CK(cudaStreamSynchronize(c->stream));
+    CK(cudaGetLastError());
+    return IBTFO_OK;
+}
+
+ibtfo_status ibtfo_case_bytes(const ibtfo_config *k, long long *resident, long long *setup)
+{
+    if (!k || !resident || !setup)
+        return fail(IBTFO_EINVAL, "null argument");
+    if (k->n_x < 2 || k->n_y < 2 || k->num_ghost_cell < 2)
+        return fail(IBTFO_EINVAL, "bad grid");
+    const long long M = k->n_x + 2LL * k->num_ghost_cell, N = k->n_y + 2LL * k->num_ghost_cell;
+    const long long pitch = (M + 31) / 32 * 32, plane = pitch * N;
+    const long long nblocks = ((k->n_x + TILE_X - 1) / TILE_X) * (long long)((k->n_y + TILE_Y - 1) / TILE_Y);
+    long long r = 2 * 4 * 8 * plane;                      // two state buffers
+    if (k->boundary == IBTFO_BOUNDARY_REGULAR)
+        r += 4 * 8 * plane;                               // Regular: initial state
+    r += plane + (long long)sizeof(DevState) + 8 * nblocks + 4 * nblocks + 2 * 2 * k->num_ghost_cell * 4 * 8;
+    // ghost records: at most every interior cell next to the outline, bounded
+    // here by two layers around the domain perimeter per unit of perimeter
+    if (k->boundary != IBTFO_BOUNDARY_REGULAR)
+        r += (long long)sizeof(GhostRec) * 4 * (M + N) * k->num_ghost_cell;
+    *resident = r;
+    *setup = r + 3 * 8 * plane; // plus phi, n_x, n_y until ibtfo_release_geometry
     return IBTFO_OK;
 }
 
@@ -591,6 +747,7 @@ ibtfo_status ibtfo_get_state(ibtfo_case *c, double *u_old, double *u_new)
     const GridDesc &g = c->g;
     const size_t cells = (size_t)g.M * g.N;
     DevState s;
+    CK(ensure_staging(c));
     CK(cudaMemcpyAsync(&s, c->st, sizeof(DevState), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     if (u_old)

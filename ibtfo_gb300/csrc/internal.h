@@ -200,6 +200,16 @@ BatchKernel batch_kernel(int scheme, int riemann, int limiter, int precision, in
 void launch_batch_fill(const BatchHeader *h, int phase, int grid, cudaStream_t s);
 void launch_batch_progress(const BatchHeader *h, int nslots_max, BatchProgress *out, cudaStream_t s);
 
+// device-side case set-up (bodies.cu); ibtfo_body is declared in ibtfo.h
+}
+struct ibtfo_body;
+namespace ibtfo {
+void launch_bodies_phi(const GridDesc &g, const ibtfo_body *d_bodies, int n, double *phi, cudaStream_t s);
+void launch_x_split_init(const GridDesc &g, const uint8_t *type, double x_split, const double L[4],
+                         const double R[4], double *buf, double *ring_ic, cudaStream_t s);
+void launch_density(const GridDesc &g, const double *b0, const double *b1, const DevState *st, double *out,
+                    cudaStream_t s);
+
 // geometry set-up (geometry.cu)
 int active_tiles(const GridDesc &g, const uint8_t *d_type, unsigned **d_tiles, int *ntiles, cudaStream_t s);
 // host list of the tx x ty tiles holding at least one fluid cell (bx | by << 16);

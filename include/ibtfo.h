@@ -128,6 +128,45 @@ ibtfo_status ibtfo_set_state(ibtfo_case *c, const double *u0);
  * Waits for queued work. */
 ibtfo_status ibtfo_get_state(ibtfo_case *c, double *u_old, double *u_new);
 
+/* ---------------------------------------------------------------- device-side set-up
+ *
+ * No counterparts in the reference, which builds phi and the initial state
+ * on the host (Test/InclineSod/Level_Set_function.cpp:8-52,
+ * Test/PNGGeo/Level_Set.cpp:31-142 and each test's Initialize.cpp).  These build
+ * them on the GPU, so a case of millions of cells is set up without a host
+ * array or a host-to-device copy. */
+enum { IBTFO_BODY_CIRCLE = 0, IBTFO_BODY_ELLIPSE = 1 };
+typedef struct ibtfo_body {
+    int kind;          /* IBTFO_BODY_* */
+    int reserved;
+    double xc, yc;     /* centre */
+    double a, b;       /* circle: radius a; ellipse: semi-axes a (along theta) and b */
+    double theta;      /* ellipse orientation, radians */
+} ibtfo_body;
+
+/* ibtfo_setup_geometry with phi = the signed distance to the union of the
+ * bodies (positive in the fluid outside them; exact within 16 cells of an
+ * outline, a lower bound of the right sign farther out).  n = 0: no body. */
+ibtfo_status ibtfo_setup_bodies(ibtfo_case *c, const ibtfo_body *bodies, int n);
+/* ibtfo_set_state with primitive states (rho, u, v, p) `left` for
+ * x < x_split and `right` elsewhere; solid cells hold rho = -1, E = -1 as the
+ * reference's Initialize writes them. */
+ibtfo_status ibtfo_init_x_split(ibtfo_case *c, double x_split, const double left[4], const double right[4]);
+/* Primitive state behind a normal shock moving in +x at Mach `mach` into the
+ * primitive state `pre` (Rankine-Hugoniot). */
+ibtfo_status ibtfo_post_shock_state(double mach, double gamma, const double pre[4], double post[4]);
+/* Free phi and the normals once the geometry is set up (ibtfo_get_geometry
+ * and ibtfo_setup_geometry then return IBTFO_ESTATE). */
+ibtfo_status ibtfo_release_geometry(ibtfo_case *c);
+/* Interior density of the current state, n_y rows of n_x doubles; wait = 0
+ * queues the copy on the case's stream and returns (use pinned memory). */
+ibtfo_status ibtfo_get_density(ibtfo_case *c, double *out, int wait);
+/* Device bytes a case of this configuration holds: `resident` while it runs
+ * (after ibtfo_release_geometry, without the host-transfer staging that
+ * ibtfo_set_state / ibtfo_get_state allocate on first use), `setup` at the
+ * peak of its set-up. */
+ibtfo_status ibtfo_case_bytes(const ibtfo_config *cfg, long long *resident, long long *setup);
+
 /* Replaces U_OLD (the current state, M*N*4 doubles) without touching the
  * loop accounting, dt or U_NEW: the host-buffer round trip of a caller that
  * keeps its own copy of the state between steps. */
@@ -272,6 +311,80 @@ ibtfo_status ibtfo_batch_get_tiling(const ibtfo_batch *b, ibtfo_batch_tiling *t)
  * tiling, so the trial steps are ordinary steps) */
 ibtfo_status ibtfo_batch_autotune(ibtfo_batch *b, int steps, ibtfo_batch_tiling *best, ibtfo_batch_tiling *trials,
                                   int max_trials, int *n_trials);
+
+/* ---------------------------------------------------------------- serving
+ *
+ * No counterpart in the reference.  A server accepts solves as requests,
+ * admits them in arrival order while its device-memory budget and
+ * active-case limit allow, steps all admitted cases together in one batch
+ * (continuous batching: requests that arrive while others run join between
+ * chunks of steps), and retires each case when its own loop ends.  Each
+ * request is one case set up on the GPU: bodies (ibtfo_setup_bodies) and a
+ * two-state initial condition split at x = x_split (ibtfo_init_x_split; a
+ * shock with ibtfo_post_shock_state).  Results carry the final loop scalars,
+ * the times of arrival, admission and completion on the server clock, and,
+ * when requested, the final density. */
+typedef struct ibtfo_server ibtfo_server;
+
+#define IBTFO_MAX_BODIES 8
+
+typedef struct ibtfo_server_config {
+    int scheme, riemann, limiter, precision; /* kernel variant of every case */
+    long long memory_budget; /* device bytes for cases (0: 80% of the free memory at creation) */
+    int max_active;          /* cases stepped at once (0: no limit) */
+    int chunk_steps;         /* steps per scheduling round (0: 32) */
+    int tile_shape;          /* IBTFO_TILE_*, or -1: autotune once 4 cases are active */
+    int ctas_per_sm;         /* 0: the occupancy limit */
+    int reserved[6];
+} ibtfo_server_config;
+
+typedef struct ibtfo_request {
+    long long id;
+    double arrival;          /* seconds on the server clock; admitted no earlier */
+    int n_x, n_y;
+    double lo_x, lo_y, hi_x, hi_y;
+    double gamma, cfl_number, t_end;
+    int max_iter;            /* 0: no limit */
+    int boundary, global_boundary;
+    int n_bodies;
+    ibtfo_body bodies[IBTFO_MAX_BODIES];
+    double x_split;
+    double left[4], right[4]; /* primitive (rho, u, v, p) */
+    double *density_out;     /* optional, n_x*n_y doubles (pinned for an asynchronous copy) */
+    int reserved[8];
+} ibtfo_request;
+
+typedef struct ibtfo_result {
+    long long id;
+    int status;              /* IBTFO_OK, or the error that failed the request */
+    int iter, nan_cells, reserved;
+    double now_t, mass, mass_start;
+    double arrival, admitted, finished; /* server clock, seconds */
+} ibtfo_result;
+
+typedef struct ibtfo_server_stats {
+    long long submitted, admitted, completed, failed;
+    int pending, active, retiring, peak_active;
+    long long bytes_in_use, peak_bytes, memory_budget;
+    long long chunks, steps;
+    int tile_shape, ctas_per_sm;
+    int reserved[6];
+} ibtfo_server_stats;
+
+ibtfo_status ibtfo_server_create(const ibtfo_server_config *cfg, ibtfo_server **out);
+ibtfo_status ibtfo_server_destroy(ibtfo_server *s);
+/* thread-safe; requests are kept in arrival order */
+ibtfo_status ibtfo_server_submit(ibtfo_server *s, const ibtfo_request *r);
+/* sets the server clock to zero (the first pump does it otherwise) */
+ibtfo_status ibtfo_server_start(ibtfo_server *s);
+double ibtfo_server_clock(const ibtfo_server *s);
+/* one scheduling round; *busy = 1 while requests are pending, active or retiring */
+ibtfo_status ibtfo_server_pump(ibtfo_server *s, int *busy);
+/* pump until no work is left (IBTFO_ETIMEOUT after max_seconds > 0) */
+ibtfo_status ibtfo_server_run(ibtfo_server *s, double max_seconds);
+/* move up to `max` completed results into `out`; returns how many (thread-safe) */
+int ibtfo_server_poll(ibtfo_server *s, ibtfo_result *out, int max);
+ibtfo_status ibtfo_server_stats_get(ibtfo_server *s, ibtfo_server_stats *out);
 
 /* IBTFO_OK when every operation queued on the case's stream has finished,
  * IBTFO_ETIMEOUT while some are pending (does not wait) */

@@ -60,3 +60,42 @@ def test_null_pointers_rejected():
     assert L.ibtfo_create(None, None) == 1
     assert L.ibtfo_advance(None, 1) == 1
     assert L.ibtfo_get_state(None, None, None) == 1
+
+
+STRUCTS = {
+    "ibtfo_config": "Config", "ibtfo_progress": "Progress", "ibtfo_batch_config": "BatchConfig",
+    "ibtfo_batch_tiling": "BatchTiling", "ibtfo_body": "Body", "ibtfo_server_config": "ServerConfig",
+    "ibtfo_request": "Request", "ibtfo_result": "Result", "ibtfo_server_stats": "ServerStats",
+}
+
+
+def test_ctypes_layouts_match_the_header(tmp_path):
+    """Size and every field offset of each public struct, as gcc lays out
+    include/ibtfo.h, equal the ctypes mirrors in the Python binding."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "ibtfo.h"', "int main(void) {"]
+    for cname, pyname in STRUCTS.items():
+        py = getattr(ib, pyname)
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {}
+    for ln in out:
+        if ln:
+            s, f, v = ln.split()
+            got[(s, f)] = int(v)
+    for cname, pyname in STRUCTS.items():
+        py = getattr(ib, pyname)
+        assert got[(cname, "size")] == C.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert got[(cname, f)] == getattr(py, f).offset, (cname, f)
