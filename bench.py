@@ -301,12 +301,20 @@ def served_request(ib, r, arrival, density_out=None):
                       right=(1.0, 0.0, 0.0, 1.0), arrival=arrival, density_out=density_out)
 
 
+SERVE_RIEMANN = "HLLC_Toro"
+
+
 def serve_leg(n_requests=24, rates=(None, 2.0), precision="fp32c", plain_precision="fp64_fast"):
     """The served batch stream (first `n_requests` of the seeded stream):
     cases/s and p50/p99 latency of the server at each arrival rate (None: all
     requests at t = 0, the server's capacity), the same requests run plainly
     one after another in `plain_precision`, and each served density against
-    the plain one (relative L1)."""
+    the plain one (relative L1 and L-inf).
+
+    The solver is the contact-restoring HLLC with its positivity safeguards:
+    the reference's HLLC (its HLL solver) and Steger-Warming turn these cases
+    to NaN from about Mach 2 on (a face pressure below zero in the expansion
+    behind the cylinder, which the oracle reproduces)."""
     import ibtfo_gb300 as ib
     from ibtfo_gb300 import cases
     base = cases.served_stream(n_requests, 1.0, seed=42)
@@ -314,13 +322,14 @@ def serve_leg(n_requests=24, rates=(None, 2.0), precision="fp32c", plain_precisi
     bufs = {r.id: ib.PinnedBuffer(r.n_x * r.n_y) for r in base}
     out = {"workload": f"shock over a cylinder, first {n_requests} requests of the seed-42 stream "
                        f"(grids {min(r.n_x * r.n_y for r in base)}..{max(r.n_x * r.n_y for r in base)} cells, "
-                       f"{cells} cells in all), MUSCL + HLLC + minmod, IDWBaseGFM, CFL 0.45, 1.5 crossings",
+                       f"{cells} cells in all), MUSCL + {SERVE_RIEMANN} + minmod, IDWBaseGFM, CFL 0.45, "
+                       f"1.5 crossings",
            "served_precision": precision, "plain_precision": plain_precision, "rates": []}
     cell_updates = 0
     for rate in rates:
         arrivals = [0.0] * n_requests if rate is None else \
             [r.arrival for r in cases.served_stream(n_requests, rate, seed=42)]
-        with ib.Server(precision=precision, chunk_steps=32, tile_shape="auto") as srv:
+        with ib.Server(riemann=SERVE_RIEMANN, precision=precision, chunk_steps=32, tile_shape="auto") as srv:
             for r, a in zip(base, arrivals):
                 srv.submit(served_request(ib, r, a, density_out=bufs[r.id]))
             srv.start()
@@ -341,22 +350,26 @@ def serve_leg(n_requests=24, rates=(None, 2.0), precision="fp32c", plain_precisi
     for b in bufs.values():
         b.close()
     # the same requests run plainly, one after another
-    errs = []
+    errs, linf = [], []
     t0 = time.perf_counter()
     for r in base:
         with ib.Case(r.n_x, r.n_y, lo=(0.0, 0.0), hi=(r.width, r.height), cfl=0.45, t_end=r.t_end,
-                     max_iter=2 ** 31 - 1, scheme="MUSCL", riemann="HLLC", boundary="IDWBaseGFM",
+                     max_iter=2 ** 31 - 1, scheme="MUSCL", riemann=SERVE_RIEMANN, boundary="IDWBaseGFM",
                      precision=plain_precision) as c:
             c.setup_bodies([ib.circle(r.xc, r.yc, r.radius)])
             c.init_x_split(r.x_shock, cases.post_shock(r.mach), (1.0, 0.0, 0.0, 1.0))
             c.run()
             rho = c.density().reshape(-1)
         errs.append(float(np.abs(served_rho[r.id] - rho).sum() / np.abs(rho).sum()))
+        linf.append(float(np.abs(served_rho[r.id] - rho).max() / np.abs(rho).max()))
     plain_s = time.perf_counter() - t0
     out["plain"] = {"seconds": plain_s, "cases_per_s": n_requests / plain_s,
                     "Gcell_updates_per_s": cell_updates / plain_s / 1e9}
     out["served_vs_plain_cases_per_s"] = out["rates"][0]["cases_per_s"] / out["plain"]["cases_per_s"]
-    out["density_l1_vs_plain"] = {"max": max(errs), "median": float(np.median(errs))}
+    out["density_l1_vs_plain"] = {"max": max(errs), "median": float(np.median(errs)),
+                                  "within_1e-5": sum(1 for e in errs if e <= 1e-5), "of": len(errs)}
+    out["density_linf_vs_plain"] = {"max": max(linf), "median": float(np.median(linf))}
+    out["nan_results"] = sum(1 for x in res if x["nan_cells"])
     return out
 
 

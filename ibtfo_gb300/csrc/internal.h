@@ -24,7 +24,8 @@ struct DevState
     int iter;          // completed steps
     int cur;           // buffer holding the current state
     int fill_pending;  // a step completed and its boundary pass has not run yet
-    int nan_cells;     // fluid cells with a NaN component, summed over steps
+    int nan_cells;     // fluid cells with a NaN component after the latest step (or reduction)
+    int nan_step;      // running count of the launch in progress
     unsigned int ticket;       // blocks finished in the current reduction launch
     int status;                // bit flags, see STATUS_*
     double last_amax, last_umax, last_vmax; // maxima behind the latest dt

@@ -212,7 +212,8 @@ __device__ __forceinline__ void sw_fast(const T UL[4], const T UR[4], const GasC
 
 // Contact-restoring HLLC (Toro, Riemann Solvers and Numerical Methods for
 // Fluid Dynamics, 3rd ed., eqs. 10.37-10.39 and 10.71-10.73), offered under its
-// own key: the reference's HLLC directory holds the HLL solver.  Wave speeds
+// own key: the reference's HLLC directory holds the HLL solver (see also the
+// HLLC_Toro safeguards below).  Wave speeds
 // from the PVRS pressure estimate with Toro's q_K = 1 for p* <= p_K; no face
 // leaves its flux slot unchanged (always returns a flux).
 template <typename T, int NRM>
@@ -277,6 +278,77 @@ __device__ __forceinline__ void mhm_predict_fast(T UL[4], T UR[4], const GasCons
     }
 }
 
+// ---------------------------------------------------------------- HLLC_Toro safeguards
+//
+// MUSCL on conserved variables keeps each variable between its neighbours
+// but not the pressure: in the fast, low-pressure expansion behind a body hit
+// by a strong shock (a cylinder at Mach >= 2.5) a reconstructed face state can
+// have p < 0, and the conservative update can leave a cell with p < 0, where
+// the kinetic energy is tens of times the internal energy.  The reference's
+// solvers turn such cases to NaN (its HLL takes the square root of a negative
+// p*, reproduced by the oracle).  Under the HLLC_Toro key two safeguards keep
+// the pressure positive.  Their thresholds are fractions of E, the same in
+// FP64 and FP32 so that both precisions run one algorithm; they sit well above
+// FP32 rounding of E - E_kin (about 1e-7 E), so whatever way an expression
+// rounds, the solver never meets a non-positive pressure.
+
+// internal energy E - rho (u^2 + v^2) / 2, evaluated as prim_fast does
+template <typename T>
+__device__ __forceinline__ T internal_energy(const T U[4])
+{
+    const T ir = rcp_t(U[0]);
+    const T u = U[1] * ir, v = U[2] * ir;
+    return U[3] - (T)0.5 * U[0] * (u * u + v * v);
+}
+
+// positive density and an internal energy above 1e-6 E (NaN fails)
+template <typename T>
+__device__ __forceinline__ bool physical(const T U[4])
+{
+    return U[0] > (T)0 && internal_energy(U) > (T)1e-6 * fabs(U[3]);
+}
+
+// a face whose reconstructed (or predicted) pair is not physical takes the
+// first-order pair, the two cell averages; faces next to solid cells are
+// left alone (their fluxes are not used)
+template <typename T>
+__device__ __forceinline__ void positivity_fallback(const T c1[4], const T c2[4], T UL[4], T UR[4])
+{
+    if (!physical(c1) || !physical(c2) || (physical(UL) && physical(UR)))
+        return;
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+    {
+        UL[k] = c1[k];
+        UR[k] = c2[k];
+    }
+}
+
+// after the update of a fluid cell: where the internal energy falls below
+// 1e-5 E, E becomes E_kin + 1e-5 E (the energy added is at most 1e-5 E, in
+// the few cells where the conservative update lost positivity).  Returns
+// whether the floor applied and the energy to store.
+template <typename T>
+__device__ __forceinline__ bool pressure_floor_energy(const T U[4], T &E)
+{
+    if (!(U[0] > (T)0))
+        return false; // density not positive: nothing sensible to floor
+    const T f = (T)1e-5 * fabs(U[3]);
+    const T e = internal_energy(U);
+    if (e >= f)
+        return false;
+    E = (U[3] - e) + f;
+    return true;
+}
+
+template <typename T>
+__device__ __forceinline__ void pressure_floor(T U[4])
+{
+    T e;
+    if (pressure_floor_energy(U, e))
+        U[3] = e;
+}
+
 template <typename T, int SCH, int RIE, int LIM>
 __device__ __forceinline__ void x_face_fast(const T c0[4], const T c1[4], const T c2[4], const T c3[4],
                                             const GasConst<T> &K, T h2, T F[4])
@@ -285,6 +357,9 @@ __device__ __forceinline__ void x_face_fast(const T c0[4], const T c1[4], const 
     face_states_fast<T, SCH, LIM>(c0, c1, c2, c3, UL, UR);
     if (SCH == MHM)
         mhm_predict_fast<T, 1>(UL, UR, K, h2);
+    if constexpr (RIE == HLLCT)
+        if (SCH != GODUNOV)
+            positivity_fallback(c1, c2, UL, UR);
     if constexpr (RIE == PVRS)
         pvrs_x(UL, UR, (double)K.g, F); // double only (FP32 form rejects PVRS)
     else if constexpr (RIE == SW)
@@ -303,6 +378,9 @@ __device__ __forceinline__ int y_face_fast(const T c0[4], const T c1[4], const T
     face_states_fast<T, SCH, LIM>(c0, c1, c2, c3, UD, UU);
     if (SCH == MHM)
         mhm_predict_fast<T, 2>(UD, UU, K, h2);
+    if constexpr (RIE == HLLCT)
+        if (SCH != GODUNOV)
+            positivity_fallback(c1, c2, UD, UU);
     if constexpr (RIE == PVRS)
         return pvrs_y(UD, UU, (double)K.g, G, stray);
     else if constexpr (RIE == SW)

@@ -156,6 +156,19 @@ __device__ __forceinline__ void sweep_tile32(SweepSmem32<TX, TY> &s, const GridD
                 hi[k] = s.sU[k][r + 2][c + 2];
                 lo[k] = U[(4 + k) * P + o];
                 two_float_sub(hi[k], lo[k], d);
+            }
+            if constexpr (RIE == HLLCT)
+            {
+                float e;
+                if (pressure_floor_energy(hi, e))
+                {
+                    hi[3] = e;
+                    lo[3] = 0.0f;
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+            {
                 V[k * P + o] = hi[k];
                 V[(4 + k) * P + o] = lo[k];
             }

@@ -47,7 +47,7 @@ __device__ __forceinline__ void block_commit_finalize(double a, double u, double
         if (a > 0) atomic_max_nonneg(&st->amax_bits, a);
         if (u > 0) atomic_max_nonneg(&st->umax_bits, u);
         if (v > 0) atomic_max_nonneg(&st->vmax_bits, v);
-        if (n) atomicAdd(&st->nan_cells, n);
+        if (n) atomicAdd(&st->nan_step, n);
         partial[bid] = m;
         __threadfence();
         unsigned t = atomicAdd(&st->ticket, 1u);
@@ -92,8 +92,10 @@ __device__ __forceinline__ void block_commit_finalize(double a, double u, double
             vs->cur = vs->cur ^ 1;
             vs->fill_pending = 1;
         }
+        vs->nan_cells = vs->nan_step;
+        vs->nan_step = 0;
         if (vs->nan_cells)
-            vs->status |= STATUS_NAN;
+            vs->status |= STATUS_NAN; // sticky: some step held a NaN
         vs->amax_bits = 0ull;
         vs->umax_bits = 0ull;
         vs->vmax_bits = 0ull;
@@ -309,8 +311,12 @@ __device__ __forceinline__ void sweep_tile64(SweepSmem64<TX, TY> &s, const GridD
                     double x = s.sU[k][r + 2][c + 2] - dt * (s.sF[k][r + 1][c + 1] - s.sF[k][r + 1][c]) / g.dx;
                     v[k] = x - dt * (gp - gm) / g.dy;
                 }
-                V[k * P + (long long)j * pitch + i] = v[k];
             }
+            if constexpr (RIE == HLLCT)
+                pressure_floor(v);
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                V[k * P + (long long)j * pitch + i] = v[k];
             if (FAST)
                 cell_stats_fast(v, K, g.dxdy, cs);
             else

@@ -40,7 +40,11 @@ typedef enum ibtfo_status {
 enum { IBTFO_SCHEME_MUSCL = 0, IBTFO_SCHEME_MHM = 1, IBTFO_SCHEME_GODUNOV = 2 };
 /* HLLC is the reference's HLLC directory, whose solver is HLL (including the
  * Y-face slot reuse); HLLC_TORO is a contact-restoring HLLC with no
- * reference counterpart */
+ * reference counterpart, with two positivity safeguards: a face whose
+ * reconstructed state has rho <= 0 or an internal energy below 1e-6 of E
+ * takes the first-order pair (the two cell averages), and an updated fluid
+ * cell whose internal energy falls below 1e-5 of E has E raised to
+ * E_kin + 1e-5 E */
 enum {
     IBTFO_RIEMANN_HLL = 0,
     IBTFO_RIEMANN_HLLC = 1,
@@ -83,8 +87,8 @@ typedef struct ibtfo_config {
 /* The reference time-loop scalars after the last completed step. */
 typedef struct ibtfo_progress {
     int iter;       /* completed steps */
-    int status;     /* bit 0: a fluid cell holds NaN */
-    int nan_cells;  /* fluid cells with a NaN component, summed over steps */
+    int status;     /* bit 0: a fluid cell held NaN after some step (sticky) */
+    int nan_cells;  /* fluid cells with a NaN component after the latest step */
     int reserved;
     double now_t;   /* loop time, advanced by the dt computed after each step (Sod.cpp:176) */
     double dt;      /* dt the next step applies (ComputeDt of the current state) */
