@@ -304,7 +304,8 @@ def served_request(ib, r, arrival, density_out=None):
 SERVE_RIEMANN = "HLLC_Toro"
 
 
-def serve_leg(n_requests=24, rates=(None, 2.0), precision="fp32c", plain_precision="fp64_fast"):
+def serve_leg(n_requests=24, rates=(None, 2.0), precision="fp32c", plain_precision="fp64_fast",
+              max_cells=2048 * 2048):
     """The served batch stream (first `n_requests` of the seeded stream):
     cases/s and p50/p99 latency of the server at each arrival rate (None: all
     requests at t = 0, the server's capacity), the same requests run plainly
@@ -317,10 +318,11 @@ def serve_leg(n_requests=24, rates=(None, 2.0), precision="fp32c", plain_precisi
     behind the cylinder, which the oracle reproduces)."""
     import ibtfo_gb300 as ib
     from ibtfo_gb300 import cases
-    base = cases.served_stream(n_requests, 1.0, seed=42)
+    base = cases.served_stream(n_requests, 1.0, seed=42, max_cells=max_cells)
     cells = sum(r.n_x * r.n_y for r in base)
     bufs = {r.id: ib.PinnedBuffer(r.n_x * r.n_y) for r in base}
     out = {"workload": f"shock over a cylinder, first {n_requests} requests of the seed-42 stream "
+                       f"(cells per request log-uniform up to {max_cells}) "
                        f"(grids {min(r.n_x * r.n_y for r in base)}..{max(r.n_x * r.n_y for r in base)} cells, "
                        f"{cells} cells in all), MUSCL + {SERVE_RIEMANN} + minmod, IDWBaseGFM, CFL 0.45, "
                        f"1.5 crossings",
@@ -328,7 +330,7 @@ def serve_leg(n_requests=24, rates=(None, 2.0), precision="fp32c", plain_precisi
     cell_updates = 0
     for rate in rates:
         arrivals = [0.0] * n_requests if rate is None else \
-            [r.arrival for r in cases.served_stream(n_requests, rate, seed=42)]
+            [r.arrival for r in cases.served_stream(n_requests, rate, seed=42, max_cells=max_cells)]
         with ib.Server(riemann=SERVE_RIEMANN, precision=precision, chunk_steps=32, tile_shape="auto") as srv:
             for r, a in zip(base, arrivals):
                 srv.submit(served_request(ib, r, a, density_out=bufs[r.id]))
@@ -385,6 +387,8 @@ def main():
     ap.add_argument("--size", type=int, default=4096, help="grid size for --profile-workload")
     ap.add_argument("--precision", default=PRECISION, choices=("fp64", "fp64_fast", "fp32c"))
     ap.add_argument("--serve-requests", type=int, default=24, help="requests of the served-stream leg (0: skip)")
+    ap.add_argument("--serve-max-cells", type=int, default=None,
+                    help="largest request grid (default: 2048^2 with --serve-only, 1024^2 in the full run)")
     ap.add_argument("--serve-only", action="store_true", help="run only the served-stream leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -394,7 +398,8 @@ def main():
     if args.serve_only:
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        print(json.dumps({"serve": serve_leg(args.serve_requests)}), flush=True)
+        print(json.dumps({"serve": serve_leg(args.serve_requests, max_cells=args.serve_max_cells or 2048 * 2048)}),
+              flush=True)
         return 0
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -456,6 +461,11 @@ def main():
         torch.distributed.destroy_process_group()
     if rank != 0:
         return 0
+    # the served stream (rank 0; replicas would serve their own streams)
+    serve = None
+    if args.serve_requests > 0:
+        serve = serve_leg(args.serve_requests, rates=(None, 8.0),
+                          max_cells=args.serve_max_cells or 1024 * 1024)
     K = args.steps
     step_s = r["step_ms"] * 1e-3
     value = world * cells * K / step_s / 1e9
@@ -477,6 +487,7 @@ def main():
             "gpu_launches": r["launches"], "clocks": r["clocks"],
             "other_precision": {"precision": other, "value": world * cells * K / (r2["step_ms"] * 1e-3) / 1e9,
                                 "unit": METRIC, "sweep_ms": r2["sweep_ms"] / K},
+            "serve": serve,
             "forms": {"workload": wv.name, "scheme": wv.scheme, "riemann": wv.riemann, "boundary": "periodic",
                       **forms},
             "final": {"iter": r["progress"]["iter"], "nan_cells": r["progress"]["nan_cells"]}}
