@@ -215,6 +215,22 @@ def vortex_errors(w, rhos):
     return out
 
 
+def max_over_ranks(values, world, device):
+    """Element-wise maximum of per-rank timings over all ranks (the slowest
+    replica sets the whole job's time); identity for one rank."""
+    import torch
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return [float(x) for x in t.tolist()]
+
+
+def job_rate(world, cells, steps, seconds):
+    """Whole-job cell updates per second (Gcell-updates/s): every replica
+    advanced `cells` cells `steps` times within `seconds`."""
+    return world * cells * steps / seconds / 1e9
+
+
 def gpu_arm(args, rank, world, local_rank, precision=None, e2e=True, w=None, inputs=channel_inputs, steps=None,
             snapshot=False):
     import torch
@@ -281,10 +297,7 @@ def gpu_arm(args, rank, world, local_rank, precision=None, e2e=True, w=None, inp
     e2e_s = time.perf_counter() - t0
     pin.close()
 
-    t = torch.tensor([step_ms, sweep_ms, e2e_s], dtype=torch.float64, device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    step_ms, sweep_ms, e2e_s = (float(x) for x in t.tolist())
+    step_ms, sweep_ms, e2e_s = max_over_ranks([step_ms, sweep_ms, e2e_s], world, "cuda")
     res = {"step_ms": step_ms, "sweep_ms": sweep_ms, "e2e_s": e2e_s, "e2e_steps": e2e_steps, "cells": cells,
            "launches": launches, "clocks": clk.summary(), "progress": prog, "M": g.M, "N": g.N}
     if snapshot:
@@ -450,7 +463,7 @@ def main():
                      snapshot=(rank == 0))
         cv = wv.grid.n_x * wv.grid.n_y
         sw_s = rv["sweep_ms"] * 1e-3 / kv
-        forms[prec] = {"value": world * cv * kv / (rv["step_ms"] * 1e-3) / 1e9, "unit": METRIC,
+        forms[prec] = {"value": job_rate(world, cv, kv, rv["step_ms"] * 1e-3), "unit": METRIC,
                        "steps": args.warmup + kv, "sweep_ms": rv["sweep_ms"] / kv,
                        "roofline_frac": BYTES_PER_CELL * cv / sw_s / 1e9 / measured_peaks()[0]}
         rhos[prec] = (rv.get("rho"), rv.get("rho_t"))
@@ -468,13 +481,13 @@ def main():
                           max_cells=args.serve_max_cells or 1024 * 1024)
     K = args.steps
     step_s = r["step_ms"] * 1e-3
-    value = world * cells * K / step_s / 1e9
+    value = job_rate(world, cells, K, step_s)
     sweep_s = r["sweep_ms"] * 1e-3 / K
     peak, peak_kind = measured_peaks()
     achieved = BYTES_PER_CELL * cells / sweep_s / 1e9
     traffic = profiled_traffic()
     state_bytes = r["M"] * r["N"] * 32
-    e2e_val = world * cells * r["e2e_steps"] / r["e2e_s"] / 1e9
+    e2e_val = job_rate(world, cells, r["e2e_steps"], r["e2e_s"])
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K, "warmup": args.warmup,
             "ms_per_step": r["step_ms"] / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic", "config": config_json(w),
@@ -485,7 +498,7 @@ def main():
             "e2e": {"value": e2e_val, "unit": METRIC, "h2d_bytes_per_step": state_bytes,
                     "d2h_bytes_per_step": state_bytes + 48, "steps": r["e2e_steps"]},
             "gpu_launches": r["launches"], "clocks": r["clocks"],
-            "other_precision": {"precision": other, "value": world * cells * K / (r2["step_ms"] * 1e-3) / 1e9,
+            "other_precision": {"precision": other, "value": job_rate(world, cells, K, r2["step_ms"] * 1e-3),
                                 "unit": METRIC, "sweep_ms": r2["sweep_ms"] / K},
             "serve": serve,
             "forms": {"workload": wv.name, "scheme": wv.scheme, "riemann": wv.riemann, "boundary": "periodic",
