@@ -24,7 +24,8 @@ LIB_PATH = os.path.join(HERE, "libibtfo_gb300.so")
 SCHEMES = {"MUSCL": 0, "MHM": 1, "Godunov": 2}
 RIEMANNS = {"HLL": 0, "HLLC": 1, "PVRS": 2, "StegerWarming": 3, "HLLC_Toro": 4}
 LIMITERS = {"minmod": 0, "VanLeer": 1}
-BOUNDARIES = {"Regular": 0, "IDWBaseGFM": 1, "LinearBaseGFM": 2, "RiemannBaseGFM": 3, "BCGFM": 4, "HBCGFM": 5}
+BOUNDARIES = {"Regular": 0, "IDWBaseGFM": 1, "LinearBaseGFM": 2, "RiemannBaseGFM": 3, "BCGFM": 4, "HBCGFM": 5,
+              "CCM": 6}
 GLOBAL_BCS = {"walls": 0, "periodic": 1}
 PRECISIONS = {"fp64": 0, "fp64_fast": 1, "fp32c": 2}
 
@@ -140,6 +141,7 @@ SIGNATURES = {
     "ibtfo_num_sch": (C.c_int, [_P]),
     "ibtfo_get_scheme_index": (C.c_int, [_P, _DP]),
     "ibtfo_num_ghost_cells": (C.c_int, [_P]),
+    "ibtfo_get_cut_cells": (C.c_int, [_P, _DP, _DP, _DP]),
     "ibtfo_set_state": (C.c_int, [_P, _DP]),
     "ibtfo_get_state": (C.c_int, [_P, _DP, _DP]),
     "ibtfo_put_state": (C.c_int, [_P, _DP]),
@@ -312,6 +314,12 @@ class Case:
     @property
     def num_ghost_cells(self):
         return lib().ibtfo_num_ghost_cells(self.h)
+
+    def cut_cells(self):
+        """(alpha, ax, ay), each (N, M), of a cut-cell case."""
+        a, x, y = (np.empty(self.M * self.N) for _ in range(3))
+        _check(lib().ibtfo_get_cut_cells(self.h, _dp(a), _dp(x), _dp(y)))
+        return a.reshape(self.N, self.M), x.reshape(self.N, self.M), y.reshape(self.N, self.M)
 
     def cell_types(self):
         return self.get_geometry().reshape(-1, 6)[:, 5].copy()

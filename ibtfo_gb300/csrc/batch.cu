@@ -447,6 +447,8 @@ ibtfo_status ibtfo_batch_add(ibtfo_batch *b, ibtfo_case *c, int *slot)
     case_batch_view(c, &sa, &fa, &sch, &rie, &lim, &prec, &has);
     if (!has)
         return bfail(IBTFO_ESTATE, "no state: call ibtfo_set_state before adding the case");
+    if (fa.bc == BC_CCM)
+        return bfail(IBTFO_EINVAL, "cut-cell cases run one per launch (their mixing step is not batched)");
     const int r0 = (rie == IBTFO_RIEMANN_HLLC) ? IBTFO_RIEMANN_HLL : rie;
     const int r1 = (b->cfg.riemann == IBTFO_RIEMANN_HLLC) ? IBTFO_RIEMANN_HLL : b->cfg.riemann;
     if (sch != b->cfg.scheme || r0 != r1 || lim != b->cfg.limiter || prec != b->cfg.precision)

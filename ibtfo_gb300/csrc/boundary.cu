@@ -9,7 +9,7 @@
 // Global_Boundary then reads U_NEW (Test/Sod/Global_Boudary.cpp:23-75).
 // Here the two buffers ping-pong: after a sweep, `next` holds the new fluid
 // values and `prev` the previous state, so the reference's snapshot S is
-//   S(i,j) = type(i,j) == 0 ? next(i,j) : prev(i,j)      (interior cells)
+//   S(i,j) = type(i,j) == 0 (or a cut cell) ? next(i,j) : prev(i,j)   (interior cells)
 //   S(ring) = prev(ring)            ghost-fluid variants (snapshot of U_OLD)
 //   S(ring) = initial values        Regular (U_NEW's ring is never written)
 // and this pass writes next's ghost cells and ring from S.
@@ -34,7 +34,7 @@ struct View
     __device__ __forceinline__ double S(int i, int j, int k) const
     {
         long long o = (long long)j * pitch + i;
-        const double *b = (interior(i, j) && type[o] == 0) ? next : prev;
+        const double *b = (interior(i, j) && updated_cell(type[o])) ? next : prev;
         return state_ld(b, k, o, g);
     }
     __device__ __forceinline__ double N_(int i, int j, int k) const
@@ -336,12 +336,30 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) reduce_kernel(const ReduceArgs
     if (i < g.ng + g.n_x && j < g.ng + g.n_y)
     {
         long long o = (long long)j * g.pitch + i;
-        if (a.type[o] == 0)
+        if (a.type[o] == CELL_FLUID)
         {
             double v[4];
             for (int k = 0; k < 4; k++)
                 v[k] = state_ld(a.u, k, o, g);
             cell_stats(v, g.gamma, g.dx, g.dy, cs);
+        }
+        else if (a.type[o] == CELL_CUT && a.alpha)
+        {
+            // a cut cell: mass alpha rho; the CFL maxima only where alpha >= 0.5
+            // (smaller cells are mixed with their neighbours)
+            double v[4];
+            for (int k = 0; k < 4; k++)
+                v[k] = state_ld(a.u, k, o, g);
+            CellStats c1;
+            cell_stats(v, g.gamma, g.dx, g.dy, c1);
+            cs.mass += a.alpha[o] * c1.mass;
+            cs.nans += c1.nans;
+            if (a.alpha[o] >= 0.5)
+            {
+                cs.amax = fmax(cs.amax, c1.amax);
+                cs.umax = fmax(cs.umax, c1.umax);
+                cs.vmax = fmax(cs.vmax, c1.vmax);
+            }
         }
     }
     block_reduce_finalize<TILE_X * TILE_Y>(cs, a.st, a.partial, g, false, a.set_start, gridDim.x * gridDim.y,

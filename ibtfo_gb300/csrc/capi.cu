@@ -119,11 +119,20 @@ struct ibtfo_case
     double *ring_ic = nullptr; // [2][2*ng][4]
     unsigned *tiles = nullptr; // active sweep tiles
     int ntiles = 0;
+    // cut cells (BC_CCM): volume fractions, apertures, small-cell mixing lists
+    double *alpha = nullptr, *ax = nullptr, *ay = nullptr;
+    MixExchange *mix_ex = nullptr;
+    MixParticipant *mix_part = nullptr;
+    int *mix_links = nullptr;
+    double *mix_e = nullptr;
+    int nex = 0, npart = 0;
+    CcmLaunch ccm = nullptr;
     int nblocks = 0;
     bool geometry = false, state = false;
     SweepLaunch sweep = nullptr;
     cudaGraphExec_t graph = nullptr;
     int graph_steps = 0;
+    long long graph_launches = 0; // kernel launches in one replay of the graph
 };
 
 // Case buffers come from the device's stream-ordered pool; freed memory stays
@@ -192,7 +201,8 @@ ibtfo_status ibtfo_destroy(ibtfo_case *c)
     // device-wide synchronisation (other cases keep running)
     cudaStream_t fs = c->own ? c->own : c->stream;
     void *bufs[] = {c->buf[0], c->buf[1], c->ic, c->staging, c->phi, c->nx, c->ny, c->type, c->ghosts,
-                    c->st, c->partial, c->ring_ic, c->tiles};
+                    c->st, c->partial, c->ring_ic, c->tiles, c->alpha, c->ax, c->ay, c->mix_ex, c->mix_part,
+                    c->mix_links, c->mix_e};
     for (void *p : bufs)
         if (p)
             cudaFreeAsync(p, fs);
@@ -218,11 +228,13 @@ ibtfo_status ibtfo_create(const ibtfo_config *cfg, ibtfo_case **out)
     if (!(k.hi_x > k.lo_x) || !(k.hi_y > k.lo_y) || !(k.gamma > 1.0) || !(k.cfl_number > 0.0))
         return fail(IBTFO_EINVAL, "need hi > lo, gamma > 1, cfl_number > 0");
     if (k.scheme < 0 || k.scheme > 2 || k.riemann < 0 || k.riemann > 4 || k.limiter < 0 || k.limiter > 1 ||
-        k.boundary < 0 || k.boundary > 5 || k.global_boundary < 0 || k.global_boundary > 1 || k.precision < 0 ||
+        k.boundary < 0 || k.boundary > 6 || k.global_boundary < 0 || k.global_boundary > 1 || k.precision < 0 ||
         k.precision > 2)
         return fail(IBTFO_EINVAL, "unknown scheme/riemann/limiter/boundary/global_boundary/precision key");
     if (k.precision == IBTFO_PRECISION_FP32_COMPENSATED && k.riemann == IBTFO_RIEMANN_PVRS)
         return fail(IBTFO_EINVAL, "PVRS is available in the FP64 precisions only");
+    if (k.boundary == IBTFO_BOUNDARY_CCM && k.riemann == IBTFO_RIEMANN_PVRS)
+        return fail(IBTFO_EINVAL, "the cut-cell method runs HLL/HLLC, Steger-Warming or HLLC_Toro, not PVRS");
     if (k.global_boundary == IBTFO_GLOBAL_PERIODIC && (k.n_x < k.num_ghost_cell || k.n_y < k.num_ghost_cell))
         return fail(IBTFO_EINVAL, "periodic boundaries need n_x, n_y >= num_ghost_cell");
 
@@ -248,6 +260,8 @@ ibtfo_status ibtfo_create(const ibtfo_config *cfg, ibtfo_case **out)
     set_derived_constants(g);
     c->nblocks = ((k.n_x + TILE_X - 1) / TILE_X) * ((k.n_y + TILE_Y - 1) / TILE_Y);
     c->sweep = sweep_launcher(k.scheme, k.riemann, k.limiter, k.precision);
+    if (k.boundary == IBTFO_BOUNDARY_CCM)
+        c->ccm = ccm_launcher(k.scheme, k.riemann, k.limiter, k.precision);
 
     const size_t plane_bytes = sizeof(double) * (size_t)g.plane;
     retain_pool_memory(c->device);
@@ -269,6 +283,12 @@ ibtfo_status ibtfo_create(const ibtfo_config *cfg, ibtfo_case **out)
     A((void **)&c->st, sizeof(DevState));
     A((void **)&c->partial, sizeof(double) * (size_t)c->nblocks);
     A((void **)&c->ring_ic, sizeof(double) * 2 * 2 * g.ng * 4);
+    if (k.boundary == IBTFO_BOUNDARY_CCM)
+    {
+        A((void **)&c->alpha, plane_bytes);
+        A((void **)&c->ax, plane_bytes);
+        A((void **)&c->ay, plane_bytes);
+    }
     if (e == cudaSuccess)
         e = cudaStreamSynchronize(c->own);
     if (e != cudaSuccess)
@@ -326,7 +346,22 @@ static ibtfo_status geometry_from_phi(ibtfo_case *c)
         c->ghosts = nullptr;
         c->nghost = 0;
     }
-    int rc = setup_geometry(g, c->cfg.boundary, c->phi, c->nx, c->ny, c->type, &c->ghosts, &c->nghost, c->stream);
+    int rc;
+    if (c->cfg.boundary == IBTFO_BOUNDARY_CCM)
+    {
+        void *old[] = {c->mix_ex, c->mix_part, c->mix_links, c->mix_e};
+        for (void *p : old)
+            if (p)
+                cudaFreeAsync(p, c->stream);
+        c->mix_ex = nullptr;
+        c->mix_part = nullptr;
+        c->mix_links = nullptr;
+        c->mix_e = nullptr;
+        rc = ccm_setup(g, c->phi, c->alpha, c->ax, c->ay, c->type, &c->mix_ex, &c->nex, &c->mix_part, &c->npart,
+                       &c->mix_links, &c->mix_e, c->stream);
+    }
+    else
+        rc = setup_geometry(g, c->cfg.boundary, c->phi, c->nx, c->ny, c->type, &c->ghosts, &c->nghost, c->stream);
     if (rc == 0)
         rc = active_tiles(g, c->type, &c->tiles, &c->ntiles, c->stream);
     if (rc == 2)
@@ -374,6 +409,25 @@ ibtfo_status ibtfo_get_geometry(ibtfo_case *c, double *xy)
             r[4] = ny[o];
             r[5] = (double)t[o];
         }
+    return IBTFO_OK;
+}
+
+ibtfo_status ibtfo_get_cut_cells(ibtfo_case *c, double *alpha, double *ax, double *ay)
+{
+    if (!c || !alpha || !ax || !ay)
+        return fail(IBTFO_EINVAL, "null argument");
+    if (!c->alpha)
+        return fail(IBTFO_EINVAL, "not a cut-cell case");
+    if (!c->geometry)
+        return fail(IBTFO_ESTATE, "ibtfo_setup_geometry has not run");
+    cudaSetDevice(c->device);
+    const GridDesc &g = c->g;
+    CK(cudaStreamSynchronize(c->stream));
+    double *dst[3] = {alpha, ax, ay};
+    const double *src[3] = {c->alpha, c->ax, c->ay};
+    for (int k = 0; k < 3; k++)
+        CK(cudaMemcpy2D(dst[k], sizeof(double) * g.M, src[k], sizeof(double) * g.pitch, sizeof(double) * g.M, g.N,
+                        cudaMemcpyDeviceToHost));
     return IBTFO_OK;
 }
 
@@ -470,10 +524,39 @@ static void enqueue_boundary(ibtfo_case *c)
     }
 }
 
-static void enqueue_step(ibtfo_case *c, int guard)
+// TimeAdvance: the sweep (and, for cut cells, the small-cell mixing after it)
+static void enqueue_advance(ibtfo_case *c, int guard)
 {
+    if (c->ccm)
+    {
+        CcmArgs a{};
+        a.s = sweep_args(c, guard);
+        a.alpha = c->alpha;
+        a.ax = c->ax;
+        a.ay = c->ay;
+        c->ccm(a, dim3(c->ntiles), dim3(TILE_X * TILE_Y), c->stream);
+        count_launch();
+        MixArgs m{};
+        m.g = c->g;
+        m.buf0 = c->buf[0];
+        m.buf1 = c->buf[1];
+        m.st = c->st;
+        m.ex = c->mix_ex;
+        m.nex = c->nex;
+        m.part = c->mix_part;
+        m.npart = c->npart;
+        m.links = c->mix_links;
+        m.e = c->mix_e;
+        launch_mix(m, c->stream);
+        return;
+    }
     c->sweep(sweep_args(c, guard), dim3(c->ntiles), dim3(TILE_X * TILE_Y), c->stream);
     count_launch();
+}
+
+static void enqueue_step(ibtfo_case *c, int guard)
+{
+    enqueue_advance(c, guard);
     enqueue_boundary(c);
 }
 
@@ -533,6 +616,7 @@ static ibtfo_status finish_initial_state(ibtfo_case *c)
     r.st = c->st;
     r.partial = c->partial;
     r.set_start = 1;
+    r.alpha = c->alpha;
     launch_reduce(r, c->nblocks, c->stream);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(c->stream));
@@ -688,6 +772,8 @@ ibtfo_status ibtfo_case_bytes(const ibtfo_config *k, long long *resident, long l
     long long r = 2 * 4 * 8 * plane;                      // two state buffers
     if (k->boundary == IBTFO_BOUNDARY_REGULAR)
         r += 4 * 8 * plane;                               // Regular: initial state
+    if (k->boundary == IBTFO_BOUNDARY_CCM)
+        r += 3 * 8 * plane;                               // cut cells: alpha and the two apertures
     r += plane + (long long)sizeof(DevState) + 8 * nblocks + 4 * nblocks + 2 * 2 * k->num_ghost_cell * 4 * 8;
     // ghost records: at most every interior cell next to the outline, bounded
     // here by two layers around the domain perimeter per unit of perimeter
@@ -732,7 +818,7 @@ __global__ void export_unew_kernel(GridDesc g, const double *cur, const double *
     int j = (int)(q / g.M), i = (int)(q - (long long)j * g.M);
     long long o = (long long)j * g.pitch + i;
     bool in = i >= g.ng && i < g.ng + g.n_x && j >= g.ng && j < g.ng + g.n_y;
-    const double *b = in ? ((type[o] == 0) ? cur : prev) : ring_src;
+    const double *b = in ? (updated_cell(type[o]) ? cur : prev) : ring_src;
     for (int k = 0; k < 4; k++)
         aos[q * 4 + k] = state_ld(b, k, o, g);
 }
@@ -779,6 +865,7 @@ static ibtfo_status build_graph(ibtfo_case *c)
     long long before = g_launches.load();
     for (int s = 0; s < GRAPH_STEPS; s++)
         enqueue_step(c, 1);
+    c->graph_launches = g_launches.load() - before;
     g_launches.store(before); // captured launches are counted when replayed
     cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
     if (e != cudaSuccess)
@@ -800,8 +887,6 @@ ibtfo_status ibtfo_advance(ibtfo_case *c, int nsteps)
     if (nsteps < 0)
         return fail(IBTFO_EINVAL, "nsteps < 0");
     cudaSetDevice(c->device);
-    const int per_step = 1 + ((c->cfg.boundary != IBTFO_BOUNDARY_REGULAR &&
-                               c->cfg.global_boundary == IBTFO_GLOBAL_PERIODIC) ? 2 : 1);
     int left = nsteps;
     if (left >= GRAPH_STEPS)
     {
@@ -814,7 +899,7 @@ ibtfo_status ibtfo_advance(ibtfo_case *c, int nsteps)
         while (left >= GRAPH_STEPS)
         {
             CK(cudaGraphLaunch(c->graph, c->stream));
-            count_launch(GRAPH_STEPS * per_step);
+            count_launch((int)c->graph_launches);
             left -= GRAPH_STEPS;
         }
     }
@@ -831,8 +916,7 @@ ibtfo_status ibtfo_enqueue_sweep(ibtfo_case *c)
     if (!c->state)
         return fail(IBTFO_ESTATE, "no state: call ibtfo_set_state first");
     cudaSetDevice(c->device);
-    c->sweep(sweep_args(c, 1), dim3(c->ntiles), dim3(TILE_X * TILE_Y), c->stream);
-    count_launch();
+    enqueue_advance(c, 1);
     CK(cudaGetLastError());
     return IBTFO_OK;
 }
@@ -980,7 +1064,7 @@ int case_set_dt(ibtfo_case *c, double dt)
 int case_sweep_unguarded(ibtfo_case *c)
 {
     cudaSetDevice(c->device);
-    c->sweep(sweep_args(c, 0), dim3(c->ntiles), dim3(TILE_X * TILE_Y), c->stream);
+    enqueue_advance(c, 0);
     count_launch();
     CK(cudaGetLastError());
     return IBTFO_OK;
@@ -1010,6 +1094,7 @@ int case_reduce_current(ibtfo_case *c)
     r.st = c->st;
     r.partial = c->partial;
     r.set_start = 0;
+    r.alpha = c->alpha;
     launch_reduce(r, c->nblocks, c->stream);
     CK(cudaGetLastError());
     return IBTFO_OK;

@@ -246,7 +246,7 @@ __global__ void scheme_index_kernel(GridDesc g, int bc, const double *__restrict
 
 static inline unsigned nblk(long long n, int b) { return (unsigned)((n + b - 1) / b); }
 
-// one flag per tx x ty sweep tile: does it hold an interior fluid cell?
+// one flag per tx x ty sweep tile: does it hold an interior fluid (or cut) cell?
 __global__ void tile_flags_kernel(GridDesc g, const uint8_t *__restrict__ type, int tx, int ty, int ntx, int nty,
                                   uint8_t *flags)
 {
@@ -258,7 +258,7 @@ __global__ void tile_flags_kernel(GridDesc g, const uint8_t *__restrict__ type, 
     uint8_t f = 0;
     for (int j = j0; j < j0 + ty && j < g.ng + g.n_y && !f; j++)
         for (int i = i0; i < i0 + tx && i < g.ng + g.n_x; i++)
-            if (type[(long long)j * g.pitch + i] == 0)
+            if (updated_cell(type[(long long)j * g.pitch + i]))
             {
                 f = 1;
                 break;

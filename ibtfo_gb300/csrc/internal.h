@@ -8,7 +8,13 @@
 
 namespace ibtfo {
 
-enum Boundary { BC_REGULAR = 0, BC_IDW = 1, BC_LINEAR = 2, BC_RIEMANNGFM = 3, BC_BCGFM = 4, BC_HBCGFM = 5 };
+enum Boundary { BC_REGULAR = 0, BC_IDW = 1, BC_LINEAR = 2, BC_RIEMANNGFM = 3, BC_BCGFM = 4, BC_HBCGFM = 5, BC_CCM = 6 };
+
+// cell types: 0 fluid, 1 solid, 2 ghost-fluid ghost or domain ring; cut-cell
+// cases (BC_CCM) also have 3: a cell the body outline crosses
+enum { CELL_FLUID = 0, CELL_SOLID = 1, CELL_GHOST = 2, CELL_CUT = 3 };
+// cells whose state a sweep advances
+__host__ __device__ __forceinline__ bool updated_cell(uint8_t t) { return t == CELL_FLUID || t == CELL_CUT; }
 enum GlobalBC { GB_WALLS = 0, GB_PERIODIC = 1 };
 
 // Per-case scalars that live in device memory so that consecutive steps run
@@ -133,7 +139,57 @@ struct ReduceArgs
     DevState *st;
     double *partial;
     int set_start;         // also store mass as mass_start
+    const double *alpha;   // cut-cell volume fractions (BC_CCM), else null
 };
+
+// ---------------------------------------------------------------- cut cells
+//
+// Geometry of a cut-cell case (per cell, FP64): volume fraction alpha (fluid
+// area / cell area), aperture ax of the X face (i+1/2, j) and ay of the Y face
+// (i, j+1/2) (fluid length / face length).  Small cut cells (alpha < 0.5)
+// exchange conserved quantities with up to three neighbours after each
+// sweep; the exchanges and their participants are compact lists built once.
+struct CcmArgs
+{
+    SweepArgs s;
+    const double *alpha, *ax, *ay;
+};
+
+struct MixExchange   // E = w (U[t] - U[s]); alpha_s U_s += E, alpha_t U_t -= E
+{
+    long long s, t;  // cell offsets (j * pitch + i)
+    double w;        // beta alpha_s alpha_t / (alpha_s + alpha_t)
+};
+
+struct MixParticipant
+{
+    long long o;     // cell offset
+    double inv_alpha;
+    int first, count; // its links (exchange index, sign) in the link list
+};
+
+struct MixArgs
+{
+    GridDesc g;
+    double *buf0, *buf1;
+    DevState *st;
+    const MixExchange *ex;
+    int nex;
+    const MixParticipant *part;
+    int npart;
+    const int *links; // exchange index * 2 + (1 for the target side)
+    double *e;        // exchange values, 4 per exchange
+};
+
+typedef void (*CcmLaunch)(const CcmArgs &, dim3 grid, dim3 block, cudaStream_t s);
+CcmLaunch ccm_launcher(int scheme, int riemann, int limiter, int precision);
+void launch_mix(const MixArgs &a, cudaStream_t s);
+// geometry of a cut-cell case from the cell-centred level set: alpha, ax, ay,
+// the cell types, and the mixing lists (device arrays allocated here with
+// stream-ordered allocation); 0, 2 (allocation) or 5 (CUDA error)
+int ccm_setup(const GridDesc &g, const double *d_phi, double *d_alpha, double *d_ax, double *d_ay, uint8_t *d_type,
+              MixExchange **d_ex, int *nex, MixParticipant **d_part, int *npart, int **d_links, double **d_e,
+              cudaStream_t s);
 
 typedef void (*SweepLaunch)(const SweepArgs &, dim3 grid, dim3 block, cudaStream_t s);
 

@@ -184,7 +184,8 @@ ibtfo_status ibtfo_config_from_inp(const ibtfo_inp *p, ibtfo_config *cfg)
     static const char *const schemes[] = {"MUSCL", "MHM", "Godunov"};
     static const char *const riemanns[] = {"HLL", "HLLC", "PVRS", "StegerWarming", "HLLC_Toro"};
     static const char *const limiters[] = {"minmod", "VanLeer"};
-    static const char *const bounds[] = {"Regular", "IDWBaseGFM", "LinearBaseGFM", "RiemannBaseGFM", "BCGFM", "HBCGFM"};
+    static const char *const bounds[] = {"Regular", "IDWBaseGFM", "LinearBaseGFM", "RiemannBaseGFM", "BCGFM", "HBCGFM",
+                                         "CCM"};
     static const char *const globals[] = {"Walls", "Periodic"};
     static const char *const precs[] = {"FP64", "FP64_FAST", "FP32_COMPENSATED"};
     struct Slot
@@ -195,7 +196,7 @@ ibtfo_status ibtfo_config_from_inp(const ibtfo_inp *p, ibtfo_config *cfg)
         int *dst;
         int def;
     } slots[] = {{"Scheme", schemes, 3, &c.scheme, 0},        {"Riemann", riemanns, 5, &c.riemann, 0},
-                 {"Limiter", limiters, 2, &c.limiter, 0},     {"Boundary", bounds, 6, &c.boundary, 0},
+                 {"Limiter", limiters, 2, &c.limiter, 0},     {"Boundary", bounds, 7, &c.boundary, 0},
                  {"Global_Boundary", globals, 2, &c.global_boundary, 0}, {"Precision", precs, 3, &c.precision, 0}};
     char buf[256];
     for (const Slot &s : slots)

@@ -397,4 +397,107 @@ __device__ __forceinline__ int y_face_fast(const T c0[4], const T c1[4], const T
         return hll_fast<T, 2>(UD, UU, K, G) ? 0 : 0xF;
 }
 
+// ---------------------------------------------------------------- cut cells
+//
+// The cut-cell method has no reference counterpart, so its faces use the
+// plain HLL flux in both directions (no Y-face slot reuse), Steger-Warming, or
+// the contact-restoring HLLC.
+
+// HLL flux in either direction with Toro's PVRS wave-speed estimates
+// (p* >= 0, q_K = 1 for p* <= p_K; Toro 2009, eqs. 10.59-10.60), which stay
+// defined in strong expansions where the reference's HLL estimate takes the
+// square root of a negative number
+template <typename T, int NRM>
+__device__ __forceinline__ void hll_plain(const T UL[4], const T UR[4], const GasConst<T> &K, T F[4])
+{
+    const Prim<T> L = prim_fast<T, NRM>(UL, K), R = prim_fast<T, NRM>(UR, K);
+    T p_star = (T)0.5 * (L.p + R.p) + (T)0.125 * (L.un - R.un) * ((L.r + R.r) * (L.a + R.a));
+    p_star = p_star > (T)0 ? p_star : (T)0;
+    const T t = K.c1 * p_star;
+    const T qL = (p_star > L.p) ? sqrt_t(fma_t(t, rcp_t(L.p), K.c2)) : (T)1;
+    const T qR = (p_star > R.p) ? sqrt_t(fma_t(t, rcp_t(R.p), K.c2)) : (T)1;
+    const T S_L = L.un - L.a * qL;
+    const T S_R = R.un + R.a * qR;
+    T FL[4], FR[4];
+    flux_fast<T, NRM>(UL, L, FL);
+    flux_fast<T, NRM>(UR, R, FR);
+    if (S_L >= 0)
+    {
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            F[k] = FL[k];
+    }
+    else if (S_R <= 0)
+    {
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            F[k] = FR[k];
+    }
+    else
+    {
+        const T inv = rcp_t(S_R - S_L), srsl = S_R * S_L;
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            F[k] = (S_R * FL[k] - S_L * FR[k] + srsl * (UR[k] - UL[k])) * inv;
+    }
+}
+
+template <typename T, int NRM, int RIE>
+__device__ __forceinline__ void ccm_solve(const T UL[4], const T UR[4], const GasConst<T> &K, T F[4])
+{
+    if constexpr (RIE == SW)
+        sw_fast<T, NRM>(UL, UR, K, F);
+    else if constexpr (RIE == HLLCT)
+        hllc_toro<T, NRM>(UL, UR, K, F);
+    else
+        hll_plain<T, NRM>(UL, UR, K, F);
+}
+
+// One face of a cut-cell case, normal NRM (1: X, 2: Y), from the four cells
+// across it.  first_order: a stencil cell is cut or solid, so the face takes
+// the two cell averages (no slopes, no predictor); a reconstructed pair that
+// is not physical also falls back to the cell averages (positivity_fallback).
+template <typename T, int NRM, int SCH, int RIE, int LIM>
+__device__ __forceinline__ void ccm_face(const T c0[4], const T c1[4], const T c2[4], const T c3[4],
+                                         const GasConst<T> &K, T h2, bool first_order, T F[4])
+{
+    T UL[4], UR[4];
+    if (first_order || SCH == GODUNOV)
+    {
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+        {
+            UL[k] = c1[k];
+            UR[k] = c2[k];
+        }
+    }
+    else
+    {
+        face_states_fast<T, SCH, LIM>(c0, c1, c2, c3, UL, UR);
+        if (SCH == MHM)
+            mhm_predict_fast<T, NRM>(UL, UR, K, h2);
+        positivity_fallback(c1, c2, UL, UR); // every cut-cell solver: no face with p <= 0
+    }
+    ccm_solve<T, NRM, RIE>(UL, UR, K, F);
+}
+
+// Flux through a wall of outward unit normal (nx, ny) out of a cell of state
+// U: the Riemann problem between U and its mirror image (normal velocity
+// reversed), solved in the wall's frame.  Only its normal-momentum flux (the
+// wall pressure p_w) is kept: W = (0, p_w nx, p_w ny, 0), so no mass, energy
+// or tangential momentum crosses the wall whichever branch the solver takes.
+template <typename T, int RIE>
+__device__ __forceinline__ void ccm_wall_flux(const T U[4], T nx, T ny, const GasConst<T> &K, T W[4])
+{
+    const T mn = U[1] * nx + U[2] * ny, mt = -U[1] * ny + U[2] * nx;
+    const T UL[4] = {U[0], mn, mt, U[3]};
+    const T UR[4] = {U[0], -mn, mt, U[3]};
+    T F[4];
+    ccm_solve<T, 1, RIE>(UL, UR, K, F);
+    W[0] = (T)0;
+    W[1] = F[1] * nx;
+    W[2] = F[1] * ny;
+    W[3] = (T)0;
+}
+
 } // namespace ibtfo

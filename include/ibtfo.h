@@ -59,7 +59,15 @@ enum {
     IBTFO_BOUNDARY_LINEAR_GFM = 2,  /* LinearBaseGFM */
     IBTFO_BOUNDARY_RIEMANN_GFM = 3, /* RiemannBaseGFM (same algorithm as LinearBaseGFM) */
     IBTFO_BOUNDARY_BCGFM = 4,
-    IBTFO_BOUNDARY_HBCGFM = 5
+    IBTFO_BOUNDARY_HBCGFM = 5,
+    /* Cartesian cut cells, no reference counterpart: face apertures and
+     * volume fractions from the level set, a wall flux from the mirrored-state
+     * Riemann problem, first-order faces next to the body, and conservative
+     * mixing of cut cells with volume fraction below 0.5 with their
+     * neighbours (FP64 for the geometry, the cut-cell update and the
+     * mixing); plain HLL for the HLL/HLLC keys, Steger-Warming, HLLC_TORO;
+     * both FP64 precision keys run the same FP64 arithmetic */
+    IBTFO_BOUNDARY_CCM = 6
 };
 enum { IBTFO_GLOBAL_WALLS = 0, IBTFO_GLOBAL_PERIODIC = 1 };
 /* arithmetic of the step: FP64 evaluating the reference's expressions in
@@ -123,6 +131,11 @@ int ibtfo_num_sch(const ibtfo_case *c);
 ibtfo_status ibtfo_get_scheme_index(ibtfo_case *c, double *scheme_idx);
 /* number of ghost-fluid cells found by the set-up */
 int ibtfo_num_ghost_cells(const ibtfo_case *c);
+/* Cut-cell cases (IBTFO_BOUNDARY_CCM; no reference counterpart): volume
+ * fraction of each cell, aperture of its X face (i+1/2, j) and of its Y face
+ * (i, j+1/2), each M*N doubles (cell types are in ibtfo_get_geometry: 0
+ * fluid, 1 solid, 2 domain ring, 3 cut). */
+ibtfo_status ibtfo_get_cut_cells(ibtfo_case *c, double *alpha, double *ax, double *ay);
 
 /* Initial state (M*N*4 doubles): Initialize sets U_OLD = U_NEW = u0, then the
  * initial Boundary call, ComputeDt and CaculateMass

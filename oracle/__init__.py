@@ -26,11 +26,12 @@ GLOBAL_BCS = {"walls": 0, "periodic": 1}
 
 def build(force: bool = False) -> str:
     """Compile liboracle.so (gcc, -O2 -ffp-contract=off -fopenmp)."""
-    src = os.path.join(HERE, "ibtfo_oracle.c")
-    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= os.path.getmtime(src):
+    srcs = [os.path.join(HERE, "ibtfo_oracle.c"), os.path.join(HERE, "ccm_oracle.c")]
+    if not force and os.path.exists(LIB_PATH) and \
+            os.path.getmtime(LIB_PATH) >= max(os.path.getmtime(s) for s in srcs):
         return LIB_PATH
-    cmd = ["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-std=c11",
-           src, "-o", LIB_PATH, "-lm"]
+    cmd = ["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-std=c11"] + srcs + \
+        ["-o", LIB_PATH, "-lm"]
     subprocess.run(cmd, check=True)
     return LIB_PATH
 
@@ -169,3 +170,83 @@ def read_ref_record(path: str) -> dict:
     rec["u_new"] = take(cells * 4)
     assert off == len(data)
     return rec
+
+
+# ------------------------------------------------------------------ cut cells
+
+CCM_RIEMANNS = {"HLL": 0, "HLLC": 1, "StegerWarming": 3, "HLLC_Toro": 4}
+
+
+def _ccm_lib():
+    L = lib()
+    if not getattr(L, "_ccm_ready", False):
+        P = C.POINTER(C.c_double)
+        L.ccm_create.restype = C.c_void_p
+        L.ccm_create.argtypes = [C.c_int, C.c_int, C.c_int] + [C.c_double] * 7 + [C.c_int] * 4
+        L.ccm_destroy.argtypes = [C.c_void_p]
+        L.ccm_setup.argtypes = [C.c_void_p, P]
+        L.ccm_set_state.argtypes = [C.c_void_p, P]
+        L.ccm_run.argtypes = [C.c_void_p, C.c_int, P, P]
+        L.ccm_run.restype = C.c_int
+        L.ccm_get_state.argtypes = [C.c_void_p, P]
+        L.ccm_get_geometry.argtypes = [C.c_void_p, P, P, P, C.POINTER(C.c_ubyte)]
+        L.ccm_scalars.argtypes = [C.c_void_p, P]
+        L._ccm_ready = True
+    return L
+
+
+class CcmOracle:
+    """One cut-cell case on the CPU (FP64 restatement of the library's cut-cell method)."""
+
+    def __init__(self, n_x, n_y, ng=2, lo=(0.0, 0.0), hi=(1.0, 1.0), gamma=1.4, cfl=0.45, t_end=1e300,
+                 scheme="MUSCL", riemann="HLL", limiter="minmod", gbc="walls"):
+        self.L = _ccm_lib()
+        self.n_x, self.n_y, self.ng = n_x, n_y, ng
+        self.M, self.N = n_x + 2 * ng, n_y + 2 * ng
+        self.h = self.L.ccm_create(n_x, n_y, ng, lo[0], lo[1], hi[0], hi[1], gamma, cfl, t_end, SCHEMES[scheme],
+                                   CCM_RIEMANNS[riemann], LIMITERS[limiter], 1 if gbc == "periodic" else 0)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.ccm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def setup(self, phi):
+        phi = np.ascontiguousarray(phi, dtype=np.float64).reshape(-1)
+        assert phi.size == self.M * self.N
+        self.L.ccm_setup(self.h, _p(phi))
+
+    def set_state(self, u0):
+        u0 = np.ascontiguousarray(u0, dtype=np.float64).reshape(-1)
+        assert u0.size == self.M * self.N * 4
+        self.L.ccm_set_state(self.h, _p(u0))
+
+    def run(self, nsteps):
+        dts, ms = np.zeros(max(nsteps, 1)), np.zeros(max(nsteps, 1))
+        n = self.L.ccm_run(self.h, nsteps, _p(dts), _p(ms))
+        return dts[:n], ms[:n]
+
+    def get_state(self):
+        out = np.empty(self.M * self.N * 4)
+        self.L.ccm_get_state(self.h, _p(out))
+        return out
+
+    def geometry(self):
+        n = self.M * self.N
+        a, ax, ay = np.empty(n), np.empty(n), np.empty(n)
+        t = np.empty(n, dtype=np.uint8)
+        self.L.ccm_get_geometry(self.h, _p(a), _p(ax), _p(ay), t.ctypes.data_as(C.POINTER(C.c_ubyte)))
+        shp = (self.N, self.M)
+        return a.reshape(shp), ax.reshape(shp), ay.reshape(shp), t.reshape(shp)
+
+    def scalars(self):
+        out = np.zeros(6)
+        self.L.ccm_scalars(self.h, _p(out))
+        return {"dt": out[0], "now_t": out[1], "mass": out[2], "mass_start": out[3], "iter": int(out[4]),
+                "exchanges": int(out[5])}

@@ -1,0 +1,122 @@
+"""The cut-cell method on the CPU oracle (oracle/ccm_oracle.c).
+
+The reference has no cut-cell method, so these tests check the algorithm
+against properties it must have rather than against the reference:
+  * geometry: the solid area sum (1 - alpha) dx dy of a circle is pi r^2 to
+    second order; faces of full fluid cells have aperture 1; every small cut
+    cell has exchanges;
+  * free-stream preservation: gas at rest around bodies stays at rest (to
+    rounding of the cell contents alpha U) -- the wall pressure balances the
+    face pressures;
+  * conservation: in a periodic box with bodies, mass and energy sum alpha U
+    stay constant to rounding (every face flux and every mixing exchange is
+    antisymmetric, the wall carries no mass or energy);
+  * robustness: a Mach 3 shock over a cylinder runs without NaN."""
+import math
+
+import numpy as np
+import pytest
+
+oracle = pytest.importorskip("oracle")
+from ibtfo_gb300 import cases  # noqa: E402
+
+
+# CFL 0.3: a cut cell that is not mixed (alpha >= 0.5) sees up to twice the
+# Courant number of a full cell, and the update is unsplit; at 0.45 the
+# Steger-Warming scheme amplifies rounding next to the body
+CFL = 0.3
+
+
+def make(n_x, n_y, lo, hi, phi, u0, riemann="HLL", scheme="MUSCL", gbc="walls", cfl=CFL):
+    o = oracle.CcmOracle(n_x, n_y, 2, lo, hi, 1.4, cfl, 1e300, scheme, riemann, "minmod", gbc)
+    o.setup(phi)
+    o.set_state(u0)
+    return o
+
+
+def bodies_phi(g, bodies):
+    """min over bodies of the signed distance (circles as (xc, yc, r))."""
+    phi = np.full(g.M * g.N, 1e300)
+    for (xc, yc, r) in bodies:
+        phi = np.minimum(phi, cases.cylinder_phi(g, xc, yc, r))
+    return phi
+
+
+@pytest.mark.parametrize("n", [64, 128])
+def test_circle_area_and_apertures(n):
+    g = cases.Grid(n, n, 2, 0.0, 0.0, 1.0, 1.0)
+    r = 0.23
+    phi = cases.cylinder_phi(g, 0.51, 0.47, r)
+    u0 = cases.uniform_init(g, np.zeros(g.M * g.N))
+    o = make(n, n, (0, 0), (1, 1), phi, u0)
+    alpha, ax, ay, t = o.geometry()
+    inner = (slice(2, -2), slice(2, -2))
+    dx = 1.0 / n
+    solid = float(((1.0 - alpha[inner]) * dx * dx).sum())
+    assert abs(solid - math.pi * r * r) < 2.0 * dx * dx * 2 * math.pi * r  # O(dx^2) x perimeter/dx
+    fl = t == 0
+    jj, ii = np.nonzero(fl)
+    assert np.all(ax[jj, ii] == 1.0) and np.all(ax[jj, ii - 1] == 1.0)
+    assert np.all(ay[jj, ii] == 1.0) and np.all(ay[jj - 1, ii] == 1.0)
+    cut = t == 3
+    assert cut.sum() > 0 and np.all((alpha[cut] > 0) & (alpha[cut] <= 1))
+    assert o.scalars()["exchanges"] > 0
+
+
+@pytest.mark.parametrize("riemann", ["HLL", "StegerWarming", "HLLC_Toro"])
+def test_gas_at_rest_stays_at_rest(riemann):
+    g = cases.Grid(96, 64, 2, 0.0, 0.0, 1.5, 1.0)
+    phi = bodies_phi(g, [(0.4, 0.5, 0.17), (1.1, 0.35, 0.11), (1.05, 0.72, 0.09)])
+    u0 = cases.uniform_init(g, np.zeros(g.M * g.N), (1.0, 0.0, 0.0, 1.0))
+    o = make(96, 64, (0, 0), (1.5, 1.0), phi, u0, riemann=riemann)
+    alpha, _, _, t = o.geometry()
+    o.run(50)
+    u = o.get_state().reshape(g.N, g.M, 4)
+    ref = u0.reshape(g.N, g.M, 4)
+    full, cut = t == 0, t == 3
+    assert np.max(np.abs(u[full] - ref[full])) < 1e-12
+    # a cut cell's content alpha U (the updated quantity; U itself divides the
+    # rounding of the face/wall pressure balance by alpha, which can be tiny)
+    assert np.max(alpha[cut][:, None] * np.abs(u[cut] - ref[cut])) < 1e-12
+
+
+@pytest.mark.parametrize("riemann", ["HLL", "StegerWarming", "HLLC_Toro"])
+@pytest.mark.parametrize("scheme", ["MUSCL", "Godunov"])
+def test_mass_and_energy_conserved_in_periodic_box(riemann, scheme):
+    g = cases.Grid(80, 80, 2, 0.0, 0.0, 1.0, 1.0)
+    phi = bodies_phi(g, [(0.5, 0.5, 0.16), (0.2, 0.75, 0.07)])
+    x, y = g.coords()
+    # a periodic bump (the initial ring then holds periodic images as well)
+    rho = 1.0 + 0.2 * np.exp((np.cos(2 * np.pi * (x - 0.25)) + np.cos(2 * np.pi * (y - 0.3)) - 2.0) / 0.2)
+    u0 = cases.conserved(rho, 0.6, 0.25, 1.0 + 0.1 * rho, 1.4).reshape(-1)
+    o = make(80, 80, (0, 0), (1, 1), phi, u0, riemann=riemann, scheme=scheme, gbc="periodic")
+    alpha, _, _, t = o.geometry()
+    fl = (t == 0) | (t == 3)
+    w = np.where(fl, alpha, 0.0)[..., None]
+
+    def totals():
+        u = o.get_state().reshape(g.N, g.M, 4)
+        return (w * u).sum(axis=(0, 1))
+
+    t0 = totals()
+    o.run(100)
+    t1 = totals()
+    assert abs(t1[0] - t0[0]) <= 1e-12 * abs(t0[0])
+    assert abs(t1[3] - t0[3]) <= 1e-12 * abs(t0[3])
+    assert np.isfinite(t1).all()
+
+
+@pytest.mark.parametrize("riemann", ["HLL", "StegerWarming", "HLLC_Toro"])
+def test_mach3_shock_over_cylinder_runs(riemann):
+    g = cases.Grid(160, 80, 2, 0.0, 0.0, 2.0, 1.0)
+    phi = cases.cylinder_phi(g, 0.9, 0.5, 0.2)
+    o0 = oracle.CcmOracle(160, 80, 2, (0, 0), (2, 1), 1.4, CFL, 1e300, "MUSCL", riemann, "minmod", "walls")
+    o0.setup(phi)
+    _, _, _, t = o0.geometry()
+    u0 = cases.shock_init(g, t.reshape(-1), 3.0, 0.3)
+    o0.set_state(u0)
+    dts, ms = o0.run(600)  # the shock passes the cylinder
+    assert len(dts) == 600 and np.isfinite(ms).all()
+    u = o0.get_state().reshape(g.N, g.M, 4)
+    fl = (t == 0) | (t == 3)
+    assert np.isfinite(u[fl]).all() and (u[fl][:, 0] > 0).all()
