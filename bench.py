@@ -314,6 +314,80 @@ def served_request(ib, r, arrival, density_out=None):
                       right=(1.0, 0.0, 0.0, 1.0), arrival=arrival, density_out=density_out)
 
 
+def obstacle_bodies(ib, obstacles):
+    return [ib.circle(o.xc, o.yc, o.a) if o.kind == "circle" else ib.ellipse(o.xc, o.yc, o.a, o.b, o.theta)
+            for o in obstacles]
+
+
+def ccm_leg(steps=40, warmup=3, n_x=8192, n_y=4096, full=False):
+    """Mach 3 shock over 24 seeded obstacles with cut cells (8192x4096 on
+    [0,4]x[0,2]): set-up time (level set, cut-cell geometry, mixing lists,
+    initial state, all on the GPU), then `steps` timed steps of the FP32 form
+    with HLL and with Steger-Warming and of FP64 with HLL; the FP32 density
+    against FP64's after the same steps.  full: also the FP32 HLL run to
+    t_end = 1.0."""
+    import torch
+    import ibtfo_gb300 as ib
+    from ibtfo_gb300 import cases
+    w = cases.shock_obstacles(n_x, n_y)
+    g = w.grid
+    cells = g.n_x * g.n_y
+    obs = cases.random_obstacles()
+    post = cases.post_shock(3.0)
+    out = {"workload": f"{w.name}: Mach 3 shock at x = 0.5 over {len(obs)} seeded circles/ellipses (seed 20261203), "
+                       f"cut cells, CFL {w.cfl}", "cells": cells, "steps": steps, "legs": {}}
+    rho = {}
+    peak = measured_peaks()[0]
+    for riemann, prec in (("HLLC", "fp32c"), ("StegerWarming", "fp32c"), ("HLLC", "fp64_fast")):
+        stream = torch.cuda.Stream()
+        with ib.Case.from_workload(w, riemann=riemann, precision=prec, t_end=1e300, max_iter=2 ** 31 - 1) as c:
+            c.set_stream(stream.cuda_stream)
+            t0 = time.perf_counter()
+            c.setup_bodies(obstacle_bodies(ib, obs))
+            c.init_x_split(0.5, post, (1.0, 0.0, 0.0, 1.0))
+            c.release_geometry()
+            setup_s = time.perf_counter() - t0
+            with torch.cuda.stream(stream):
+                for _ in range(warmup):
+                    c.enqueue_sweep()
+                    c.enqueue_boundary()
+            stream.synchronize()
+            ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(steps)]
+            with torch.cuda.stream(stream):
+                for k in range(steps):
+                    ev[k][0].record(stream)
+                    c.enqueue_sweep()
+                    ev[k][1].record(stream)
+                    c.enqueue_boundary()
+                    ev[k][2].record(stream)
+            torch.cuda.synchronize()
+            step_ms = sum(e[0].elapsed_time(e[2]) for e in ev)
+            sweep_ms = sum(e[0].elapsed_time(e[1]) for e in ev)
+            p = c.progress()
+            out["legs"][f"{riemann}/{prec}"] = {
+                "value": job_rate(1, cells, steps, step_ms * 1e-3), "unit": METRIC, "ms_per_step": step_ms / steps,
+                "sweep_and_mixing_ms": sweep_ms / steps,
+                "roofline_frac": BYTES_PER_CELL * cells / (sweep_ms / steps * 1e-3) / 1e9 / peak,
+                "setup_s": setup_s, "nan_cells": p["nan_cells"], "now_t": p["now_t"]}
+            if riemann == "HLLC":
+                rho[prec] = c.density()
+    a, b = rho["fp32c"], rho["fp64_fast"]
+    d = np.abs(a - b)
+    out["fp32c_vs_fp64_density"] = {"l1": float(d.sum() / np.abs(b).sum()), "linf": float(d.max() / np.abs(b).max()),
+                                    "after_steps": warmup + steps}
+    if full:
+        with ib.Case.from_workload(w, riemann="HLLC", precision="fp32c", max_iter=2 ** 31 - 1) as c:
+            c.setup_bodies(obstacle_bodies(ib, obs))
+            c.init_x_split(0.5, post, (1.0, 0.0, 0.0, 1.0))
+            c.release_geometry()
+            t0 = time.perf_counter()
+            p = c.run()
+            secs = time.perf_counter() - t0
+        out["to_t_end"] = {"t_end": w.t_end, "steps": p["iter"], "seconds": secs, "nan_cells": p["nan_cells"],
+                           "Gcell_updates_per_s": job_rate(1, cells, p["iter"], secs)}
+    return out
+
+
 SERVE_RIEMANN = "HLLC_Toro"
 
 
@@ -403,10 +477,18 @@ def main():
     ap.add_argument("--serve-max-cells", type=int, default=None,
                     help="largest request grid (default: 2048^2 with --serve-only, 1024^2 in the full run)")
     ap.add_argument("--serve-only", action="store_true", help="run only the served-stream leg")
+    ap.add_argument("--ccm-only", action="store_true", help="run only the cut-cell (shock over obstacles) leg")
+    ap.add_argument("--ccm-full", action="store_true", help="cut-cell leg: also run to t_end = 1.0")
+    ap.add_argument("--no-ccm", action="store_true", help="skip the cut-cell leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.workload:
         profile_run(args)
+        return 0
+    if args.ccm_only:
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        print(json.dumps({"ccm": ccm_leg(full=args.ccm_full)}), flush=True)
         return 0
     if args.serve_only:
         import torch
@@ -474,6 +556,8 @@ def main():
         torch.distributed.destroy_process_group()
     if rank != 0:
         return 0
+    # the cut-cell workload (rank 0)
+    ccm = None if args.no_ccm else ccm_leg(full=args.ccm_full)
     # the served stream (rank 0; replicas would serve their own streams)
     serve = None
     if args.serve_requests > 0:
@@ -501,6 +585,7 @@ def main():
             "other_precision": {"precision": other, "value": job_rate(world, cells, K, r2["step_ms"] * 1e-3),
                                 "unit": METRIC, "sweep_ms": r2["sweep_ms"] / K},
             "serve": serve,
+            "cut_cells": ccm,
             "forms": {"workload": wv.name, "scheme": wv.scheme, "riemann": wv.riemann, "boundary": "periodic",
                       **forms},
             "final": {"iter": r["progress"]["iter"], "nan_cells": r["progress"]["nan_cells"]}}

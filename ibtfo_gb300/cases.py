@@ -293,3 +293,61 @@ def served_steps_estimate(r: ServedRequest, cfl=0.45, gamma=1.4):
     lam = u2 + math.sqrt(gamma * p2 / rho2)
     return int(math.ceil(r.t_end / (cfl * (r.width / r.n_x) / lam)))
 
+
+# shock over random obstacles (cut cells) -----------------------------------
+
+
+@dataclass
+class Obstacle:
+    kind: str      # "circle" or "ellipse"
+    xc: float
+    yc: float
+    a: float       # radius, or the semi-axis along theta
+    b: float       # the other semi-axis (= a for a circle)
+    theta: float
+
+
+def random_obstacles(n=24, seed=20261203, r_min=0.02, r_max=0.15, x_range=(1.0, 3.8), height=2.0, gap=0.01,
+                     max_tries=100000):
+    """`n` non-overlapping circles and ellipses: kind 50/50, radius (the
+    ellipse's major semi-axis) uniform in [r_min, r_max], an ellipse's minor
+    semi-axis 0.4-1.0 of it, orientation uniform in [0, pi), centre x uniform
+    in `x_range` and y uniform in [r, height - r], drawn with rejection of any
+    body whose bounding circle comes within `gap` of another's."""
+    rng = np.random.default_rng(seed)
+    out = []
+    tries = 0
+    while len(out) < n:
+        tries += 1
+        if tries > max_tries:
+            raise RuntimeError("could not place the obstacles without overlap")
+        ellipse = rng.random() < 0.5
+        r = rng.uniform(r_min, r_max)
+        b = r * rng.uniform(0.4, 1.0) if ellipse else r
+        th = rng.uniform(0.0, math.pi) if ellipse else 0.0
+        x = rng.uniform(*x_range)
+        y = rng.uniform(r, height - r)
+        if any(math.hypot(x - o.xc, y - o.yc) < r + o.a + gap for o in out):
+            continue
+        out.append(Obstacle("ellipse" if ellipse else "circle", x, y, r, b, th))
+    return out
+
+
+def obstacles_phi(g: Grid, obstacles):
+    """Host signed distance for circles only (ellipses: use the GPU set-up)."""
+    phi = np.full(g.M * g.N, 1e300)
+    for o in obstacles:
+        if o.kind != "circle":
+            raise ValueError("obstacles_phi handles circles; ellipses are built by Case.setup_bodies")
+        phi = np.minimum(phi, cylinder_phi(g, o.xc, o.yc, o.a))
+    return phi
+
+
+def shock_obstacles(n_x=8192, n_y=4096):
+    """Mach 3 shock over the 24 seeded obstacles, cut cells, [0,4] x [0,2],
+    t_end 1.0, shock at x = 0.5 into (1, 0, 0, 1).  CFL 0.3: an unmixed cut
+    cell (alpha >= 0.5) sees up to twice a full cell's Courant number in an
+    unsplit update."""
+    return Workload(f"shock_obstacles_{n_x}x{n_y}", Grid(n_x, n_y, 2, 0.0, 0.0, 4.0, 2.0), 1.4, 0.3, 1.0,
+                    "MUSCL", "HLLC", "minmod", "CCM", extra={"mach": 3.0, "x_shock": 0.5, "seed": 20261203})
+
