@@ -125,3 +125,43 @@ def test_ibtfo_run_executable(tmp_path):
     o.set_initial_state(ib.case_init("channel", cfg, o.get("XYCOORD"), inpo))
     o.run(15)
     assert rel_linf(u, o.get("U_OLD")) <= RTOL
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+def test_pinned_buffers_move_the_same_bytes_as_pageable_ones(precision):
+    """Transfers from and to page-locked host buffers (the e2e benchmark's)
+    give the same bytes and the same loop state as from numpy arrays."""
+    from ibtfo_gb300 import cases as _c
+    w = _c.inclined_channel(128, 64)
+    g = w.grid
+    phi = _c.channel_phi(g)
+    n = g.M * g.N * 4
+    outs = []
+    for pinned in (False, True):
+        with ib.Case.from_workload(w, precision=precision) as c:
+            c.setup_geometry(phi)
+            u0 = _c.channel_init(g, c.cell_types(), w.gamma)
+            if pinned:
+                pin = ib.PinnedBuffer(n)
+                pin.array[:] = u0
+                c.set_state_ptr(pin.ptr)
+            else:
+                c.set_state(u0)
+            c.advance(5)
+            if pinned:
+                c.get_state_ptr(pin.ptr)
+                u = pin.array.copy()
+                c.put_state_ptr(pin.ptr)       # round trip through the device
+                c.advance(3)
+                c.get_state_ptr(pin.ptr)
+                u2 = pin.array.copy()
+                pin.close()
+            else:
+                u = c.get_state()
+                c.put_state(u)
+                c.advance(3)
+                u2 = c.get_state()
+            outs.append((u, u2, c.progress()))
+    assert np.array_equal(outs[0][0], outs[1][0], equal_nan=True)
+    assert np.array_equal(outs[0][1], outs[1][1], equal_nan=True)
+    assert outs[0][2] == outs[1][2]
