@@ -165,6 +165,9 @@ SIGNATURES = {
     "ibtfo_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(_P)]),
     "ibtfo_host_free": (C.c_int, [_P]),
     "ibtfo_query": (C.c_int, [_P]),
+    "ibtfo_write_vtk": (C.c_int, [_P, C.c_char_p, C.c_int]),
+    "ibtfo_save_checkpoint": (C.c_int, [_P, C.c_char_p]),
+    "ibtfo_load_checkpoint": (C.c_int, [_P, C.c_char_p]),
     "ibtfo_setup_bodies": (C.c_int, [_P, C.POINTER(Body), C.c_int]),
     "ibtfo_init_x_split": (C.c_int, [_P, C.c_double, _DP, _DP]),
     "ibtfo_post_shock_state": (C.c_int, [C.c_double, C.c_double, _DP, _DP]),
@@ -401,6 +404,15 @@ class Case:
         out = np.empty(self.n_x * self.n_y)
         _check(lib().ibtfo_get_density(self.h, _dp(out), 1))
         return out.reshape(self.n_y, self.n_x)
+
+    def write_vtk(self, path, binary=False):
+        _check(lib().ibtfo_write_vtk(self.h, os.fsencode(path), 1 if binary else 0))
+
+    def save_checkpoint(self, path):
+        _check(lib().ibtfo_save_checkpoint(self.h, os.fsencode(path)))
+
+    def load_checkpoint(self, path):
+        _check(lib().ibtfo_load_checkpoint(self.h, os.fsencode(path)))
 
     def idle(self) -> bool:
         """True when nothing queued on the case's stream is pending (does not wait)."""

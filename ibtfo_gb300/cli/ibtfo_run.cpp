@@ -2,6 +2,7 @@
 // Test/InclineSod/InclineSod.cpp:30-204) on the GB300 library.
 //
 //   ibtfo_run case.inp [--case NAME] [--steps N] [--print-every K] [--out FILE]
+//                      [--vtk-every V [--vtk-binary]] [--checkpoint FILE] [--restart FILE]
 //
 // Reads the .inp numbers exactly as the reference's ParamReader does, plus the
 // slot keys Scheme / Riemann / Limiter / Boundary / Global_Boundary /
@@ -9,7 +10,11 @@
 // channel, isentropic_vortex).  Prints the reference's per-iteration line
 // ("iter : N.   dt :X.   time :T.  Mass loss :M") every K iterations (every
 // iteration by default, like the reference) and writes the final U_OLD
-// (M*N*4 doubles, reference layout) to FILE.
+// (M*N*4 doubles, reference layout) to FILE.  --vtk-every V writes
+// dat_0_<iter>.vtk at the start and every V iterations and lists them in
+// result.visit, as the reference's WriteData does (Src/Utils/WriteData.cpp:
+// 20-27); --checkpoint saves the final state to restart from, --restart
+// continues from such a file instead of the initial state.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -29,12 +34,16 @@ int main(int argc, char **argv)
 {
     if (argc < 2)
     {
-        fprintf(stderr, "usage: %s case.inp [--case NAME] [--steps N] [--print-every K] [--out FILE]\n", argv[0]);
+        fprintf(stderr,
+                "usage: %s case.inp [--case NAME] [--steps N] [--print-every K] [--out FILE] "
+                "[--vtk-every V [--vtk-binary]] [--checkpoint FILE] [--restart FILE]\n",
+                argv[0]);
         return 2;
     }
     const char *inp_path = argv[1];
-    std::string case_name, out_path;
-    long steps = -1, every = 1;
+    std::string case_name, out_path, ckpt_path, restart_path;
+    long steps = -1, every = 1, vtk_every = 0;
+    int vtk_binary = 0;
     for (int a = 2; a < argc; a++)
     {
         std::string s = argv[a];
@@ -46,6 +55,14 @@ int main(int argc, char **argv)
             every = atol(argv[++a]);
         else if (s == "--out" && a + 1 < argc)
             out_path = argv[++a];
+        else if (s == "--vtk-every" && a + 1 < argc)
+            vtk_every = atol(argv[++a]);
+        else if (s == "--vtk-binary")
+            vtk_binary = 1;
+        else if (s == "--checkpoint" && a + 1 < argc)
+            ckpt_path = argv[++a];
+        else if (s == "--restart" && a + 1 < argc)
+            restart_path = argv[++a];
         else
         {
             fprintf(stderr, "ibtfo_run: unknown argument %s\n", s.c_str());
@@ -77,22 +94,42 @@ int main(int argc, char **argv)
     printf(" ====  Geometry Initialize complete ====\n");
     if (ibtfo_case_init(case_name.c_str(), inp, &cfg, xy.data(), u.data()) != IBTFO_OK)
         return die("initial-state plug-in");
-    if (ibtfo_set_state(cs, u.data()) != IBTFO_OK)
-        return die("ibtfo_set_state");
+    if (restart_path.empty() ? ibtfo_set_state(cs, u.data()) != IBTFO_OK
+                             : ibtfo_load_checkpoint(cs, restart_path.c_str()) != IBTFO_OK)
+        return die(restart_path.empty() ? "ibtfo_set_state" : "ibtfo_load_checkpoint");
     ibtfo_progress p;
     ibtfo_get_progress(cs, &p);
     printf(" ====  Initial Mass is %g ====\n", p.mass_start);
+    auto write_vtk = [&](int iter) -> bool {
+        const std::string name = "dat_0_" + std::to_string(iter) + ".vtk";
+        FILE *visit = fopen("result.visit", "a");
+        if (!visit)
+            return false;
+        if (iter == 0)
+            fprintf(visit, "!NBLOCKS 1\n");
+        fprintf(visit, "%s\n", name.c_str());
+        fclose(visit);
+        return ibtfo_write_vtk(cs, name.c_str(), vtk_binary) == IBTFO_OK;
+    };
+    if (vtk_every > 0 && !write_vtk(p.iter))
+        return die("writing VTK");
     const long limit = steps >= 0 ? steps : cfg.max_iter;
     while (p.now_t < cfg.psy_time && p.iter < cfg.max_iter && p.iter < limit)
     {
         long n = std::min<long>(every, limit - p.iter);
+        if (vtk_every > 0)
+            n = std::min<long>(n, vtk_every - p.iter % vtk_every);
         if (ibtfo_advance(cs, (int)n) != IBTFO_OK || ibtfo_get_progress(cs, &p) != IBTFO_OK)
             return die("stepping");
         printf("iter : %d.   dt :%g.   time :%g.  Mass loss :%g\n", p.iter, p.dt, p.now_t,
                std::fabs(p.mass - p.mass_start));
-        if (every > 1 && p.iter % every != 0)
+        if (vtk_every > 0 && p.iter % vtk_every == 0 && !write_vtk(p.iter))
+            return die("writing VTK");
+        if (n > 1 && p.iter % n != 0 && p.now_t >= cfg.psy_time)
             break; // the loop condition stopped the queued iterations
     }
+    if (!ckpt_path.empty() && ibtfo_save_checkpoint(cs, ckpt_path.c_str()) != IBTFO_OK)
+        return die("ibtfo_save_checkpoint");
     if (!out_path.empty())
     {
         if (ibtfo_get_state(cs, u.data(), nullptr) != IBTFO_OK)

@@ -784,6 +784,169 @@ ibtfo_status ibtfo_case_bytes(const ibtfo_config *k, long long *resident, long l
     return IBTFO_OK;
 }
 
+// ---------------------------------------------------------------- output
+
+ibtfo_status ibtfo_write_vtk(ibtfo_case *c, const char *path, int binary)
+{
+    if (!c || !path)
+        return fail(IBTFO_EINVAL, "null argument");
+    if (!c->state)
+        return fail(IBTFO_ESTATE, "no state");
+    cudaSetDevice(c->device);
+    const GridDesc &g = c->g;
+    const size_t n = (size_t)g.n_x * g.n_y;
+    float *d = nullptr;
+    CK(cudaMallocAsync(&d, sizeof(float) * 4 * n, c->stream));
+    launch_vtk_fields(g, c->buf[0], c->buf[1], c->st, c->type, d, c->stream);
+    std::vector<float> h(4 * n);
+    DevState s;
+    CK(cudaMemcpyAsync(h.data(), d, sizeof(float) * 4 * n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(&s, c->st, sizeof(DevState), cudaMemcpyDeviceToHost, c->stream));
+    cudaFreeAsync(d, c->stream);
+    CK(cudaStreamSynchronize(c->stream));
+    const ibtfo_config &k = c->cfg;
+    if (write_vtk_file(path, g, k.lo_x, k.lo_y, k.hi_x - k.lo_x, k.hi_y - k.lo_y, s.now_t, h.data(), binary))
+        return fail(IBTFO_EINVAL, std::string("cannot write ") + path);
+    return IBTFO_OK;
+}
+
+static const char CK_MAGIC[8] = {'I', 'B', 'T', 'F', 'O', 'C', 'K', '1'};
+
+struct CheckpointHeader
+{
+    char magic[8];
+    int32_t version, header_bytes;
+    ibtfo_config cfg;
+    double dt, now_t, mass, mass_start;
+    int32_t iter, status, nan_cells, has_ic;
+};
+
+ibtfo_status ibtfo_save_checkpoint(ibtfo_case *c, const char *path)
+{
+    if (!c || !path)
+        return fail(IBTFO_EINVAL, "null argument");
+    if (!c->state)
+        return fail(IBTFO_ESTATE, "no state");
+    cudaSetDevice(c->device);
+    const GridDesc &g = c->g;
+    const size_t cells = (size_t)g.M * g.N;
+    DevState s;
+    CK(cudaMemcpyAsync(&s, c->st, sizeof(DevState), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    CheckpointHeader h;
+    std::memset(&h, 0, sizeof(h));
+    std::memcpy(h.magic, CK_MAGIC, 8);
+    h.version = 1;
+    h.header_bytes = (int32_t)sizeof(h);
+    h.cfg = c->cfg;
+    h.dt = s.dt;
+    h.now_t = s.now_t;
+    h.mass = s.mass;
+    h.mass_start = s.mass_start;
+    h.iter = s.iter;
+    h.status = s.status;
+    h.nan_cells = s.nan_cells;
+    h.has_ic = c->ic ? 1 : 0;
+    // the device buffers as they are (structure-of-arrays planes with the
+    // row pitch; in the FP32 form the float (hi, lo) planes): exact in both
+    // precisions
+    const size_t bytes = sizeof(double) * 4 * (size_t)g.plane;
+    std::vector<unsigned char> raw(bytes);
+    FILE *f = fopen(path, "wb");
+    if (!f)
+        return fail(IBTFO_EINVAL, std::string("cannot write ") + path);
+    bool ok = fwrite(&h, sizeof(h), 1, f) == 1;
+    const double *planes[2] = {c->buf[s.cur], c->ic};
+    for (int b = 0; b < 1 + h.has_ic && ok; b++)
+    {
+        cudaError_t e = cudaMemcpyAsync(raw.data(), planes[b], bytes, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess)
+        {
+            fclose(f);
+            return cuda_fail(e, "checkpoint read-back");
+        }
+        ok = fwrite(raw.data(), 1, bytes, f) == bytes;
+    }
+    if (ok && h.has_ic)
+    {
+        // the corner-column sources of the Regular domain edges, as the case holds them
+        std::vector<double> ring(2 * 2 * g.ng * 4);
+        cudaError_t e = cudaMemcpyAsync(ring.data(), c->ring_ic, sizeof(double) * ring.size(),
+                                        cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(c->stream);
+        ok = e == cudaSuccess && fwrite(ring.data(), sizeof(double), ring.size(), f) == ring.size();
+    }
+    ok = (fclose(f) == 0) && ok;
+    return ok ? IBTFO_OK : fail(IBTFO_EINVAL, std::string("cannot write ") + path);
+}
+
+ibtfo_status ibtfo_load_checkpoint(ibtfo_case *c, const char *path)
+{
+    if (!c || !path)
+        return fail(IBTFO_EINVAL, "null argument");
+    if (!c->geometry)
+        return fail(IBTFO_ESTATE, "set up the geometry before loading a checkpoint");
+    FILE *f = fopen(path, "rb");
+    if (!f)
+        return fail(IBTFO_EINVAL, std::string("cannot read ") + path);
+    CheckpointHeader h;
+    if (fread(&h, sizeof(h), 1, f) != 1 || std::memcmp(h.magic, CK_MAGIC, 8) != 0 || h.version != 1 ||
+        h.header_bytes != (int32_t)sizeof(h))
+    {
+        fclose(f);
+        return fail(IBTFO_EINVAL, std::string(path) + " is not a checkpoint of this library");
+    }
+    // everything but the loop's end (psy_time, max_iter) must match
+    ibtfo_config a = h.cfg, b = c->cfg;
+    a.psy_time = b.psy_time = 0.0;
+    a.max_iter = b.max_iter = 0;
+    if (std::memcmp(&a, &b, sizeof(a)) != 0 || h.has_ic != (c->ic ? 1 : 0))
+    {
+        fclose(f);
+        return fail(IBTFO_EINVAL, "the checkpoint's configuration differs from the case's");
+    }
+    cudaSetDevice(c->device);
+    const GridDesc &g = c->g;
+    const size_t bytes = sizeof(double) * 4 * (size_t)g.plane;
+    std::vector<unsigned char> u(bytes), ic;
+    std::vector<double> ring(2 * 2 * g.ng * 4);
+    bool ok = fread(u.data(), 1, bytes, f) == bytes;
+    if (ok && h.has_ic)
+    {
+        ic.resize(bytes);
+        ok = fread(ic.data(), 1, bytes, f) == bytes &&
+             fread(ring.data(), sizeof(double), ring.size(), f) == ring.size();
+    }
+    fclose(f);
+    if (!ok)
+        return fail(IBTFO_EINVAL, std::string(path) + " is truncated");
+    CK(cudaMemcpyAsync(c->buf[0], u.data(), bytes, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->buf[1], u.data(), bytes, cudaMemcpyHostToDevice, c->stream));
+    if (h.has_ic)
+    {
+        CK(cudaMemcpyAsync(c->ic, ic.data(), bytes, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(c->ring_ic, ring.data(), sizeof(double) * ring.size(), cudaMemcpyHostToDevice,
+                           c->stream));
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    DevState s{};
+    s.dt = h.dt;
+    s.now_t = h.now_t;
+    s.mass = h.mass;
+    s.mass_start = h.mass_start;
+    s.iter = h.iter;
+    s.status = h.status;
+    s.nan_cells = h.nan_cells;
+    s.cur = 0;
+    CK(cudaMemcpyAsync(c->st, &s, sizeof(DevState), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->state = true;
+    return IBTFO_OK;
+}
+
 ibtfo_status ibtfo_query(ibtfo_case *c)
 {
     if (!c)

@@ -266,6 +266,11 @@ void launch_x_split_init(const GridDesc &g, const uint8_t *type, double x_split,
                          const double R[4], double *buf, double *ring_ic, cudaStream_t s);
 void launch_density(const GridDesc &g, const double *b0, const double *b1, const DevState *st, double *out,
                     cudaStream_t s);
+// output.cu
+void launch_vtk_fields(const GridDesc &g, const double *b0, const double *b1, const DevState *st,
+                       const uint8_t *type, float *out, cudaStream_t s);
+int write_vtk_file(const char *path, const GridDesc &g, double lo_x, double lo_y, double Psy_L, double Psy_H,
+                   double now_t, const float *fields, int binary);
 
 // geometry set-up (geometry.cu)
 int active_tiles(const GridDesc &g, const uint8_t *d_type, unsigned **d_tiles, int *ntiles, cudaStream_t s);

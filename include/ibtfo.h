@@ -403,6 +403,23 @@ ibtfo_status ibtfo_server_run(ibtfo_server *s, double max_seconds);
 int ibtfo_server_poll(ibtfo_server *s, ibtfo_result *out, int max);
 ibtfo_status ibtfo_server_stats_get(ibtfo_server *s, ibtfo_server_stats *out);
 
+/* ---------------------------------------------------------------- output
+ *
+ * VTK file of the current state in the layout of the reference's WriteData
+ * (Src/Utils/WriteData.cpp:5-247): legacy structured points over the
+ * interior cells, fields density / x-vel / y-vel / pressure (non-fluid cells
+ * -1 and -100, density floored at 1e-6), the time as field data; binary = 0
+ * writes the reference's ASCII "%f" values, 1 big-endian floats. */
+ibtfo_status ibtfo_write_vtk(ibtfo_case *c, const char *path, int binary);
+/* Checkpoint (no reference counterpart): configuration, loop scalars and the
+ * current state buffer as the device holds it (plus, for Regular
+ * boundaries, the initial state and the corner sources), in native byte
+ * order.  ibtfo_load_checkpoint restores it into a case created with the
+ * same configuration (psy_time and max_iter may differ) whose geometry is
+ * set up; stepping then continues bit for bit as the saved run would. */
+ibtfo_status ibtfo_save_checkpoint(ibtfo_case *c, const char *path);
+ibtfo_status ibtfo_load_checkpoint(ibtfo_case *c, const char *path);
+
 /* IBTFO_OK when every operation queued on the case's stream has finished,
  * IBTFO_ETIMEOUT while some are pending (does not wait) */
 ibtfo_status ibtfo_query(ibtfo_case *c);
