@@ -166,6 +166,8 @@ SIGNATURES = {
     "ibtfo_host_free": (C.c_int, [_P]),
     "ibtfo_query": (C.c_int, [_P]),
     "ibtfo_write_vtk": (C.c_int, [_P, C.c_char_p, C.c_int]),
+    "ibtfo_write_vtk_async": (C.c_int, [_P, C.c_char_p, C.c_int]),
+    "ibtfo_output_wait": (C.c_int, [_P]),
     "ibtfo_save_checkpoint": (C.c_int, [_P, C.c_char_p]),
     "ibtfo_load_checkpoint": (C.c_int, [_P, C.c_char_p]),
     "ibtfo_setup_bodies": (C.c_int, [_P, C.POINTER(Body), C.c_int]),
@@ -405,8 +407,16 @@ class Case:
         _check(lib().ibtfo_get_density(self.h, _dp(out), 1))
         return out.reshape(self.n_y, self.n_x)
 
-    def write_vtk(self, path, binary=False):
-        _check(lib().ibtfo_write_vtk(self.h, os.fsencode(path), 1 if binary else 0))
+    def write_vtk(self, path, binary=False, wait=True):
+        """VTK file of the current state (the reference's WriteData layout).
+        wait=False writes it off the step path: the snapshot is taken in order
+        with the steps and the file is written while stepping continues
+        (output_wait() joins it)."""
+        fn = lib().ibtfo_write_vtk if wait else lib().ibtfo_write_vtk_async
+        _check(fn(self.h, os.fsencode(path), 1 if binary else 0))
+
+    def output_wait(self):
+        _check(lib().ibtfo_output_wait(self.h))
 
     def save_checkpoint(self, path):
         _check(lib().ibtfo_save_checkpoint(self.h, os.fsencode(path)))

@@ -2,7 +2,7 @@
 // Test/InclineSod/InclineSod.cpp:30-204) on the GB300 library.
 //
 //   ibtfo_run case.inp [--case NAME] [--steps N] [--print-every K] [--out FILE]
-//                      [--vtk-every V [--vtk-binary]] [--checkpoint FILE] [--restart FILE]
+//                      [--vtk [--vtk-every V] [--vtk-binary]] [--checkpoint FILE] [--restart FILE]
 //
 // Reads the .inp numbers exactly as the reference's ParamReader does, plus the
 // slot keys Scheme / Riemann / Limiter / Boundary / Global_Boundary /
@@ -10,11 +10,15 @@
 // channel, isentropic_vortex).  Prints the reference's per-iteration line
 // ("iter : N.   dt :X.   time :T.  Mass loss :M") every K iterations (every
 // iteration by default, like the reference) and writes the final U_OLD
-// (M*N*4 doubles, reference layout) to FILE.  --vtk-every V writes
-// dat_0_<iter>.vtk at the start and every V iterations and lists them in
-// result.visit, as the reference's WriteData does (Src/Utils/WriteData.cpp:
-// 20-27); --checkpoint saves the final state to restart from, --restart
-// continues from such a file instead of the initial state.
+// (M*N*4 doubles, reference layout) to FILE.  --vtk writes dat_0_<iter>.vtk
+// files listed in result.visit (Src/Utils/WriteData.cpp:20-27) when the
+// reference's test drivers do (Test/Sod/Sod.cpp:135-152): before an iteration
+// whose number is a multiple of the .inp's plot_per (default 100) when
+// plot_int is 0, else before the first iteration and whenever the time has
+// passed the next of plot_int equal fractions of Psy_time; and once after the
+// loop.  --vtk-every V sets plot_per = V, plot_int = 0.  --checkpoint saves
+// the final state to restart from; --restart continues from such a file
+// instead of the initial state.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -36,14 +40,14 @@ int main(int argc, char **argv)
     {
         fprintf(stderr,
                 "usage: %s case.inp [--case NAME] [--steps N] [--print-every K] [--out FILE] "
-                "[--vtk-every V [--vtk-binary]] [--checkpoint FILE] [--restart FILE]\n",
+                "[--vtk [--vtk-every V] [--vtk-binary]] [--checkpoint FILE] [--restart FILE]\n",
                 argv[0]);
         return 2;
     }
     const char *inp_path = argv[1];
     std::string case_name, out_path, ckpt_path, restart_path;
     long steps = -1, every = 1, vtk_every = 0;
-    int vtk_binary = 0;
+    int vtk = 0, vtk_binary = 0;
     for (int a = 2; a < argc; a++)
     {
         std::string s = argv[a];
@@ -52,11 +56,13 @@ int main(int argc, char **argv)
         else if (s == "--steps" && a + 1 < argc)
             steps = atol(argv[++a]);
         else if (s == "--print-every" && a + 1 < argc)
-            every = atol(argv[++a]);
+            every = std::max(1L, atol(argv[++a]));
         else if (s == "--out" && a + 1 < argc)
             out_path = argv[++a];
+        else if (s == "--vtk")
+            vtk = 1;
         else if (s == "--vtk-every" && a + 1 < argc)
-            vtk_every = atol(argv[++a]);
+            vtk = 1, vtk_every = atol(argv[++a]);
         else if (s == "--vtk-binary")
             vtk_binary = 1;
         else if (s == "--checkpoint" && a + 1 < argc)
@@ -109,25 +115,39 @@ int main(int argc, char **argv)
             fprintf(visit, "!NBLOCKS 1\n");
         fprintf(visit, "%s\n", name.c_str());
         fclose(visit);
-        return ibtfo_write_vtk(cs, name.c_str(), vtk_binary) == IBTFO_OK;
+        return ibtfo_write_vtk_async(cs, name.c_str(), vtk_binary) == IBTFO_OK;
     };
-    if (vtk_every > 0 && !write_vtk(p.iter))
-        return die("writing VTK");
+    double plot_per = 100, plot_int = 0;
+    ibtfo_inp_get(inp, "plot_per", 100, &plot_per);
+    ibtfo_inp_get(inp, "plot_int", 0, &plot_int);
+    if (vtk_every > 0)
+        plot_per = (double)vtk_every, plot_int = 0;
+    const long per = std::max<long>(1, (long)plot_per);
+    const int n_int = (int)plot_int;
+    int output_int = 1;
     const long limit = steps >= 0 ? steps : cfg.max_iter;
     while (p.now_t < cfg.psy_time && p.iter < cfg.max_iter && p.iter < limit)
     {
-        long n = std::min<long>(every, limit - p.iter);
-        if (vtk_every > 0)
-            n = std::min<long>(n, vtk_every - p.iter % vtk_every);
+        if (vtk)
+        {
+            const bool due = n_int == 0 ? p.iter % per == 0
+                                        : (p.now_t > output_int * cfg.psy_time / n_int || p.iter == 0);
+            if (due && !write_vtk(p.iter))
+                return die("writing VTK");
+            if (due && n_int != 0 && p.iter > 0)
+                output_int++;
+        }
+        long n = std::min<long>(every - p.iter % every, limit - p.iter);
+        if (vtk)
+            n = n_int == 0 ? std::min<long>(n, per - p.iter % per) : 1; // the time rule looks at every iteration
         if (ibtfo_advance(cs, (int)n) != IBTFO_OK || ibtfo_get_progress(cs, &p) != IBTFO_OK)
             return die("stepping");
-        printf("iter : %d.   dt :%g.   time :%g.  Mass loss :%g\n", p.iter, p.dt, p.now_t,
-               std::fabs(p.mass - p.mass_start));
-        if (vtk_every > 0 && p.iter % vtk_every == 0 && !write_vtk(p.iter))
-            return die("writing VTK");
-        if (n > 1 && p.iter % n != 0 && p.now_t >= cfg.psy_time)
-            break; // the loop condition stopped the queued iterations
+        if (p.iter % every == 0 || p.now_t >= cfg.psy_time || p.iter >= limit)
+            printf("iter : %d.   dt :%g.   time :%g.  Mass loss :%g\n", p.iter, p.dt, p.now_t,
+                   std::fabs(p.mass - p.mass_start));
     }
+    if (vtk && (!write_vtk(p.iter) || ibtfo_output_wait(cs) != IBTFO_OK))
+        return die("writing VTK");
     if (!ckpt_path.empty() && ibtfo_save_checkpoint(cs, ckpt_path.c_str()) != IBTFO_OK)
         return die("ibtfo_save_checkpoint");
     if (!out_path.empty())

@@ -133,6 +133,7 @@ struct ibtfo_case
     cudaGraphExec_t graph = nullptr;
     int graph_steps = 0;
     long long graph_launches = 0; // kernel launches in one replay of the graph
+    VtkWriter *vtk = nullptr;     // asynchronous VTK output, created on first use
 };
 
 // Case buffers come from the device's stream-ordered pool; freed memory stays
@@ -197,6 +198,7 @@ ibtfo_status ibtfo_destroy(ibtfo_case *c)
         cudaStreamSynchronize(c->stream);
     if (c->graph)
         cudaGraphExecDestroy(c->graph);
+    vtk_writer_destroy(c->vtk, c->own ? c->own : c->stream);
     // stream-ordered frees: the memory returns to the device pool without a
     // device-wide synchronisation (other cases keep running)
     cudaStream_t fs = c->own ? c->own : c->stream;
@@ -797,7 +799,7 @@ ibtfo_status ibtfo_write_vtk(ibtfo_case *c, const char *path, int binary)
     const size_t n = (size_t)g.n_x * g.n_y;
     float *d = nullptr;
     CK(cudaMallocAsync(&d, sizeof(float) * 4 * n, c->stream));
-    launch_vtk_fields(g, c->buf[0], c->buf[1], c->st, c->type, d, c->stream);
+    launch_vtk_fields(g, c->buf[0], c->buf[1], c->st, c->type, d, nullptr, c->stream);
     std::vector<float> h(4 * n);
     DevState s;
     CK(cudaMemcpyAsync(h.data(), d, sizeof(float) * 4 * n, cudaMemcpyDeviceToHost, c->stream));
@@ -807,6 +809,33 @@ ibtfo_status ibtfo_write_vtk(ibtfo_case *c, const char *path, int binary)
     const ibtfo_config &k = c->cfg;
     if (write_vtk_file(path, g, k.lo_x, k.lo_y, k.hi_x - k.lo_x, k.hi_y - k.lo_y, s.now_t, h.data(), binary))
         return fail(IBTFO_EINVAL, std::string("cannot write ") + path);
+    return IBTFO_OK;
+}
+
+ibtfo_status ibtfo_write_vtk_async(ibtfo_case *c, const char *path, int binary)
+{
+    if (!c || !path)
+        return fail(IBTFO_EINVAL, "null argument");
+    if (!c->state)
+        return fail(IBTFO_ESTATE, "no state");
+    cudaSetDevice(c->device);
+    if (!c->vtk && !(c->vtk = vtk_writer_create(c->device, c->g, c->stream)))
+        return fail(IBTFO_ENOMEM, "VTK snapshot buffers");
+    const ibtfo_config &k = c->cfg;
+    std::string why;
+    if (vtk_writer_submit(c->vtk, c->g, c->buf[0], c->buf[1], c->st, c->type, c->stream, path, binary, k.lo_x,
+                          k.lo_y, k.hi_x - k.lo_x, k.hi_y - k.lo_y, &why))
+        return fail(IBTFO_EINVAL, why);
+    return IBTFO_OK;
+}
+
+ibtfo_status ibtfo_output_wait(ibtfo_case *c)
+{
+    if (!c)
+        return fail(IBTFO_EINVAL, "null argument");
+    std::string why;
+    if (c->vtk && vtk_writer_wait(c->vtk, &why))
+        return fail(IBTFO_EINVAL, why);
     return IBTFO_OK;
 }
 

@@ -4,6 +4,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <string>
 #include <vector>
 
 namespace ibtfo {
@@ -268,9 +269,16 @@ void launch_density(const GridDesc &g, const double *b0, const double *b1, const
                     cudaStream_t s);
 // output.cu
 void launch_vtk_fields(const GridDesc &g, const double *b0, const double *b1, const DevState *st,
-                       const uint8_t *type, float *out, cudaStream_t s);
+                       const uint8_t *type, float *out, double *now_t, cudaStream_t s);
 int write_vtk_file(const char *path, const GridDesc &g, double lo_x, double lo_y, double Psy_L, double Psy_H,
                    double now_t, const float *fields, int binary);
+struct VtkWriter;
+VtkWriter *vtk_writer_create(int device, const GridDesc &g, cudaStream_t s);
+int vtk_writer_submit(VtkWriter *w, const GridDesc &g, const double *b0, const double *b1, const DevState *st,
+                      const uint8_t *type, cudaStream_t s, const char *path, int binary, double lo_x, double lo_y,
+                      double Psy_L, double Psy_H, std::string *why);
+int vtk_writer_wait(VtkWriter *w, std::string *why);
+void vtk_writer_destroy(VtkWriter *w, cudaStream_t s);
 
 // geometry set-up (geometry.cu)
 int active_tiles(const GridDesc &g, const uint8_t *d_type, unsigned **d_tiles, int *ntiles, cudaStream_t s);

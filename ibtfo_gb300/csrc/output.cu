@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/ibtfo.h"
@@ -22,12 +23,16 @@
 
 namespace ibtfo {
 
-// density, x-vel, y-vel, pressure of the interior cells (row-major n_y x n_x)
+// density, x-vel, y-vel, pressure of the interior cells (row-major n_y x n_x);
+// with `now_t` set, thread 0 also copies the loop time there
 __global__ void vtk_fields_kernel(GridDesc g, const double *__restrict__ b0, const double *__restrict__ b1,
-                                  const DevState *__restrict__ st, const uint8_t *__restrict__ type, float *out)
+                                  const DevState *__restrict__ st, const uint8_t *__restrict__ type, float *out,
+                                  double *now_t)
 {
     const long long n = (long long)g.n_x * g.n_y;
     long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (now_t && c == 0)
+        *now_t = st->now_t;
     if (c >= n)
         return;
     const double *buf = st->cur ? b1 : b0;
@@ -49,10 +54,10 @@ __global__ void vtk_fields_kernel(GridDesc g, const double *__restrict__ b0, con
 }
 
 void launch_vtk_fields(const GridDesc &g, const double *b0, const double *b1, const DevState *st,
-                       const uint8_t *type, float *out, cudaStream_t s)
+                       const uint8_t *type, float *out, double *now_t, cudaStream_t s)
 {
     const long long n = (long long)g.n_x * g.n_y;
-    vtk_fields_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(g, b0, b1, st, type, out);
+    vtk_fields_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(g, b0, b1, st, type, out, now_t);
     count_launch();
 }
 
@@ -122,6 +127,116 @@ int write_vtk_file(const char *path, const GridDesc &g, double lo_x, double lo_y
     }
     const int ok = ferror(f) == 0;
     return (fclose(f) == 0 && ok) ? 0 : -1;
+}
+
+// Asynchronous VTK output.  submit() derives the four float fields into a
+// device snapshot on the case's stream (one kernel, in order with the steps),
+// then a copy stream moves the snapshot to pinned host memory while the case
+// keeps stepping, and a host thread writes the file.  One write is in flight
+// at a time: the next submit() or wait() joins it first, which also keeps the
+// snapshot from being overwritten while it is copied.
+struct VtkWriter
+{
+    int device = 0;
+    size_t n = 0;          // interior cells
+    float *dev = nullptr;  // 4*n floats, then the loop time
+    float *host = nullptr; // pinned copy of dev
+    cudaStream_t copy = nullptr;
+    cudaEvent_t ready = nullptr, copied = nullptr;
+    std::thread worker;
+    int status = 0; // 0, or -1: the last finished write failed
+    std::string failed;
+};
+
+static size_t snapshot_bytes(size_t n) { return ((sizeof(float) * 4 * n + 7) & ~(size_t)7) + sizeof(double); }
+
+VtkWriter *vtk_writer_create(int device, const GridDesc &g, cudaStream_t s)
+{
+    VtkWriter *w = new VtkWriter;
+    w->device = device;
+    w->n = (size_t)g.n_x * g.n_y;
+    const size_t bytes = snapshot_bytes(w->n);
+    if (cudaMallocAsync(&w->dev, bytes, s) != cudaSuccess || cudaMallocHost(&w->host, bytes) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&w->copy, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&w->ready, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&w->copied, cudaEventDisableTiming) != cudaSuccess)
+    {
+        vtk_writer_destroy(w, s);
+        return nullptr;
+    }
+    return w;
+}
+
+// joins the write in flight; 0, or -1 with `why` when a write failed since
+// the last call
+int vtk_writer_wait(VtkWriter *w, std::string *why)
+{
+    if (w->worker.joinable())
+        w->worker.join();
+    const int rc = w->status;
+    if (rc && why)
+        *why = w->failed;
+    w->status = 0;
+    return rc;
+}
+
+int vtk_writer_submit(VtkWriter *w, const GridDesc &g, const double *b0, const double *b1, const DevState *st,
+                      const uint8_t *type, cudaStream_t s, const char *path, int binary, double lo_x, double lo_y,
+                      double Psy_L, double Psy_H, std::string *why)
+{
+    const int prev = vtk_writer_wait(w, why);
+    const size_t bytes = snapshot_bytes(w->n);
+    double *t_dev = (double *)((char *)w->dev + bytes - sizeof(double));
+    launch_vtk_fields(g, b0, b1, st, type, w->dev, t_dev, s);
+    if (cudaGetLastError() != cudaSuccess || cudaEventRecord(w->ready, s) != cudaSuccess ||
+        cudaStreamWaitEvent(w->copy, w->ready, 0) != cudaSuccess ||
+        cudaMemcpyAsync(w->host, w->dev, bytes, cudaMemcpyDeviceToHost, w->copy) != cudaSuccess ||
+        cudaEventRecord(w->copied, w->copy) != cudaSuccess)
+    {
+        if (why)
+            *why = "queueing the VTK snapshot failed";
+        return -1;
+    }
+    const std::string file(path);
+    const GridDesc gd = g;
+    w->worker = std::thread([w, file, gd, binary, lo_x, lo_y, Psy_L, Psy_H, bytes]() {
+        cudaSetDevice(w->device);
+        if (cudaEventSynchronize(w->copied) != cudaSuccess)
+        {
+            w->status = -1;
+            w->failed = "copying the VTK snapshot failed";
+            return;
+        }
+        double now_t;
+        std::memcpy(&now_t, (const char *)w->host + bytes - sizeof(double), sizeof(double));
+        if (write_vtk_file(file.c_str(), gd, lo_x, lo_y, Psy_L, Psy_H, now_t, w->host, binary))
+        {
+            w->status = -1;
+            w->failed = "cannot write " + file;
+        }
+    });
+    return prev;
+}
+
+void vtk_writer_destroy(VtkWriter *w, cudaStream_t s)
+{
+    if (!w)
+        return;
+    vtk_writer_wait(w, nullptr);
+    if (w->copy)
+    {
+        cudaStreamSynchronize(w->copy);
+        cudaStreamDestroy(w->copy);
+    }
+    if (w->ready)
+        cudaEventDestroy(w->ready);
+    if (w->copied)
+        cudaEventDestroy(w->copied);
+    if (w->host)
+        cudaFreeHost(w->host);
+    if (w->dev)
+        cudaFreeAsync(w->dev, s);
+    delete w;
 }
 
 } // namespace ibtfo

@@ -411,6 +411,14 @@ ibtfo_status ibtfo_server_stats_get(ibtfo_server *s, ibtfo_server_stats *out);
  * -1 and -100, density floored at 1e-6), the time as field data; binary = 0
  * writes the reference's ASCII "%f" values, 1 big-endian floats. */
 ibtfo_status ibtfo_write_vtk(ibtfo_case *c, const char *path, int binary);
+/* The same file written off the step path: the fields of the current state
+ * are derived into a device snapshot in order with the case's steps, then
+ * copied to pinned host memory on a second stream and written by a host
+ * thread while the case keeps stepping.  One write is in flight per case;
+ * the next call (or ibtfo_output_wait) waits for it and reports a failure of
+ * it (IBTFO_EINVAL, the reason in ibtfo_last_error). */
+ibtfo_status ibtfo_write_vtk_async(ibtfo_case *c, const char *path, int binary);
+ibtfo_status ibtfo_output_wait(ibtfo_case *c);
 /* Checkpoint (no reference counterpart): configuration, loop scalars and the
  * current state buffer as the device holds it (plus, for Regular
  * boundaries, the initial state and the corner sources), in native byte

@@ -127,6 +127,34 @@ def test_ibtfo_run_executable(tmp_path):
     assert rel_linf(u, o.get("U_OLD")) <= RTOL
 
 
+def test_ibtfo_run_vtk_series_and_restart(tmp_path):
+    """--vtk writes dat_0_<iter>.vtk and result.visit at the reference
+    drivers' points (every plot_per iterations, then once after the loop);
+    --checkpoint then --restart continues as one uninterrupted run."""
+    exe = os.path.join(os.path.dirname(ib.LIB_PATH), "ibtfo_run")
+    inp = tmp_path / "channel.inp"
+    inp.write_text("#channel\nN_x=96\nN_y=48\nlo_x=0\nlo_y=0\nhi_x=2\nhi_y=1\nCFL_number=0.45\n"
+                   "Psy_time=0.2\nnum_ghost_cell=2\ngamma=1.4\nangle=30\nwidth=0.25\n"
+                   "Scheme = MUSCL\nRiemann = HLLC\nLimiter = minmod\nBoundary = IDWBaseGFM\nCase = channel\n")
+
+    def run(*args, cwd):
+        cwd.mkdir(exist_ok=True)
+        p = subprocess.run([exe, str(inp), *args], capture_output=True, text=True, timeout=300, cwd=cwd)
+        assert p.returncode == 0, p.stderr
+        return p.stdout
+
+    one = tmp_path / "one"
+    run("--steps", "20", "--print-every", "20", "--vtk-every", "8", "--out", str(one / "u.bin"), cwd=one)
+    assert (one / "result.visit").read_text().split() == ["!NBLOCKS", "1", "dat_0_0.vtk", "dat_0_8.vtk",
+                                                          "dat_0_16.vtk", "dat_0_20.vtk"]
+    for k in (0, 8, 16, 20):
+        assert (one / f"dat_0_{k}.vtk").read_text().startswith("# vtk DataFile Version 2.0")
+    two = tmp_path / "two"
+    run("--steps", "9", "--checkpoint", str(two / "c.ckpt"), cwd=two)
+    run("--steps", "20", "--restart", str(two / "c.ckpt"), "--out", str(two / "u.bin"), cwd=two)
+    assert np.array_equal(np.fromfile(one / "u.bin"), np.fromfile(two / "u.bin"))
+
+
 @pytest.mark.parametrize("precision", ["fp64", "fp32c"])
 def test_pinned_buffers_move_the_same_bytes_as_pageable_ones(precision):
     """Transfers from and to page-locked host buffers (the e2e benchmark's)

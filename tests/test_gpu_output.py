@@ -73,6 +73,31 @@ def test_vtk_ascii_and_binary(tmp_path):
         assert np.array_equal(v, e.astype(np.float32))
 
 
+def test_vtk_written_off_the_step_path_matches_the_synchronous_file(tmp_path):
+    """The asynchronous writer snapshots the state in order with the steps:
+    files queued between advances equal the synchronous files of the same
+    states, and the stepping itself is unchanged."""
+    w, c = channel_case()
+    with c:
+        for k in range(3):
+            c.advance(5)
+            c.write_vtk(str(tmp_path / f"s{k}.vtk"), binary=True)
+        ref = c.get_state()
+    w, c = channel_case()
+    with c:
+        for k in range(3):
+            c.advance(5)
+            c.write_vtk(str(tmp_path / f"a{k}.vtk"), binary=True, wait=False)
+        c.output_wait()
+        assert np.array_equal(c.get_state(), ref)
+        c.write_vtk(str(tmp_path / "missing" / "x.vtk"), wait=False)
+        with pytest.raises(ib.IbtfoError, match="cannot write"):
+            c.output_wait()
+        c.output_wait()  # the failure is reported once
+    for k in range(3):
+        assert (tmp_path / f"a{k}.vtk").read_bytes() == (tmp_path / f"s{k}.vtk").read_bytes()
+
+
 def _sod(precision):
     g = cases.Grid(120, 30, 2, 0.0, 0.0, 1.0, 0.25)
     w = cases.Workload("sod", g, 1.4, 0.5, 1e300, "MUSCL", "HLLC", "minmod", "Regular")
