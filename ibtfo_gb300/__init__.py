@@ -21,7 +21,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libibtfo_gb300.so")
 
-SCHEMES = {"MUSCL": 0, "MHM": 1, "Godunov": 2}
+SCHEMES = {"MUSCL": 0, "MHM": 1, "Godunov": 2, "Lax": 3}
+TIME_ADVANCES = {"SingleStep": 0, "RK2": 1}
 RIEMANNS = {"HLL": 0, "HLLC": 1, "PVRS": 2, "StegerWarming": 3, "HLLC_Toro": 4}
 LIMITERS = {"minmod": 0, "VanLeer": 1}
 BOUNDARIES = {"Regular": 0, "IDWBaseGFM": 1, "LinearBaseGFM": 2, "RiemannBaseGFM": 3, "BCGFM": 4, "HBCGFM": 5,
@@ -44,7 +45,7 @@ class Config(C.Structure):
                 ("gamma", C.c_double), ("cfl_number", C.c_double), ("psy_time", C.c_double),
                 ("max_iter", C.c_int), ("scheme", C.c_int), ("riemann", C.c_int), ("limiter", C.c_int),
                 ("boundary", C.c_int), ("global_boundary", C.c_int), ("precision", C.c_int),
-                ("reserved", C.c_int * 7)]
+                ("time_advance", C.c_int), ("reserved", C.c_int * 6)]
 
 
 class Progress(C.Structure):
@@ -260,11 +261,11 @@ class Case:
 
     def __init__(self, n_x, n_y, ng=2, lo=(0.0, 0.0), hi=(1.0, 1.0), gamma=1.4, cfl=0.5, t_end=1.0,
                  max_iter=100000, scheme="MUSCL", riemann="HLL", limiter="minmod", boundary="Regular",
-                 gbc="walls", precision="fp64"):
+                 gbc="walls", precision="fp64", time="SingleStep"):
         L = lib()
         cfg = Config(n_x, n_y, ng, lo[0], lo[1], hi[0], hi[1], gamma, cfl, t_end, max_iter,
                      SCHEMES[scheme], RIEMANNS[riemann], LIMITERS[limiter], BOUNDARIES[boundary], GLOBAL_BCS[gbc],
-                     PRECISIONS[precision])
+                     PRECISIONS[precision], TIME_ADVANCES[time])
         h = _P()
         _check(L.ibtfo_create(C.byref(cfg), C.byref(h)))
         self.h = h
@@ -675,9 +676,11 @@ def case_init(name, cfg, xycoord, inp=None):
 
 
 def config(n_x, n_y, ng=2, lo=(0.0, 0.0), hi=(1.0, 1.0), gamma=1.4, cfl=0.5, t_end=1.0, max_iter=100000,
-           scheme="MUSCL", riemann="HLL", limiter="minmod", boundary="Regular", gbc="walls", precision="fp64"):
+           scheme="MUSCL", riemann="HLL", limiter="minmod", boundary="Regular", gbc="walls", precision="fp64",
+           time="SingleStep"):
     return Config(n_x, n_y, ng, lo[0], lo[1], hi[0], hi[1], gamma, cfl, t_end, max_iter, SCHEMES[scheme],
-                  RIEMANNS[riemann], LIMITERS[limiter], BOUNDARIES[boundary], GLOBAL_BCS[gbc], PRECISIONS[precision])
+                  RIEMANNS[riemann], LIMITERS[limiter], BOUNDARIES[boundary], GLOBAL_BCS[gbc], PRECISIONS[precision],
+                  TIME_ADVANCES[time])
 
 
 class PinnedBuffer:

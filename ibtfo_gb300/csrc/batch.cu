@@ -352,7 +352,7 @@ ibtfo_status ibtfo_batch_create(const ibtfo_batch_config *cfg, ibtfo_batch **out
     if (k.precision != IBTFO_PRECISION_FP64_FAST && k.precision != IBTFO_PRECISION_FP32_COMPENSATED)
         return bfail(IBTFO_EINVAL, "batches run the fp64_fast or FP32 compensated precision");
     if (k.scheme < 0 || k.scheme > 2 || k.riemann < 0 || k.riemann > 4 || k.limiter < 0 || k.limiter > 1)
-        return bfail(IBTFO_EINVAL, "unknown scheme/riemann/limiter key");
+        return bfail(IBTFO_EINVAL, "unknown scheme/riemann/limiter key (batches run MUSCL, MHM or Godunov)");
     if (k.tile_shape < 0 || k.tile_shape >= SHAPE_COUNT || k.ctas_per_sm < 0 || k.graph_steps < 0)
         return bfail(IBTFO_EINVAL, "bad tile_shape / ctas_per_sm / graph_steps");
     ibtfo_batch *b = new ibtfo_batch();
@@ -449,6 +449,8 @@ ibtfo_status ibtfo_batch_add(ibtfo_batch *b, ibtfo_case *c, int *slot)
         return bfail(IBTFO_ESTATE, "no state: call ibtfo_set_state before adding the case");
     if (fa.bc == BC_CCM)
         return bfail(IBTFO_EINVAL, "cut-cell cases run one per launch (their mixing step is not batched)");
+    if (case_time_advance(c) != IBTFO_TIME_SINGLESTEP)
+        return bfail(IBTFO_EINVAL, "Time = RK2 cases run one per launch");
     const int r0 = (rie == IBTFO_RIEMANN_HLLC) ? IBTFO_RIEMANN_HLL : rie;
     const int r1 = (b->cfg.riemann == IBTFO_RIEMANN_HLLC) ? IBTFO_RIEMANN_HLL : b->cfg.riemann;
     if (sch != b->cfg.scheme || r0 != r1 || lim != b->cfg.limiter || prec != b->cfg.precision)

@@ -28,11 +28,14 @@ SweepLaunch sweep_launcher_godunov_fast(int riemann, int limiter);
 SweepLaunch sweep_launcher_muscl_f32(int riemann, int limiter);
 SweepLaunch sweep_launcher_mhm_f32(int riemann, int limiter);
 SweepLaunch sweep_launcher_godunov_f32(int riemann, int limiter);
+SweepLaunch sweep_launcher_lax();
 
 SweepLaunch sweep_launcher(int scheme, int riemann, int limiter, int precision)
 {
     const int r = (riemann == HLLC) ? HLL : riemann; // HLLC/Riemann_solver.cpp is HLL
     const bool fast = (precision == IBTFO_PRECISION_FP64_FAST);
+    if (scheme == LAX)
+        return sweep_launcher_lax(); // strict FP64 for both FP64 keys
     if (precision == IBTFO_PRECISION_FP32_COMPENSATED)
     {
         switch (scheme)
@@ -229,10 +232,13 @@ ibtfo_status ibtfo_create(const ibtfo_config *cfg, ibtfo_case **out)
         return fail(IBTFO_EINVAL, "grid too large (n_x, n_y <= 262144 and at most 2^31 cells)");
     if (!(k.hi_x > k.lo_x) || !(k.hi_y > k.lo_y) || !(k.gamma > 1.0) || !(k.cfl_number > 0.0))
         return fail(IBTFO_EINVAL, "need hi > lo, gamma > 1, cfl_number > 0");
-    if (k.scheme < 0 || k.scheme > 2 || k.riemann < 0 || k.riemann > 4 || k.limiter < 0 || k.limiter > 1 ||
+    if (k.scheme < 0 || k.scheme > 3 || k.riemann < 0 || k.riemann > 4 || k.limiter < 0 || k.limiter > 1 ||
         k.boundary < 0 || k.boundary > 6 || k.global_boundary < 0 || k.global_boundary > 1 || k.precision < 0 ||
-        k.precision > 2)
-        return fail(IBTFO_EINVAL, "unknown scheme/riemann/limiter/boundary/global_boundary/precision key");
+        k.precision > 2 || k.time_advance < 0 || k.time_advance > 1)
+        return fail(IBTFO_EINVAL, "unknown scheme/riemann/limiter/boundary/global_boundary/precision/time key");
+    if ((k.scheme == IBTFO_SCHEME_LAX || k.time_advance == IBTFO_TIME_RK2) &&
+        (k.precision == IBTFO_PRECISION_FP32_COMPENSATED || k.boundary == IBTFO_BOUNDARY_CCM))
+        return fail(IBTFO_EINVAL, "Scheme = Lax and Time = RK2 run in the FP64 precisions without cut cells");
     if (k.precision == IBTFO_PRECISION_FP32_COMPENSATED && k.riemann == IBTFO_RIEMANN_PVRS)
         return fail(IBTFO_EINVAL, "PVRS is available in the FP64 precisions only");
     if (k.boundary == IBTFO_BOUNDARY_CCM && k.riemann == IBTFO_RIEMANN_PVRS)
@@ -558,6 +564,21 @@ static void enqueue_advance(ibtfo_case *c, int guard)
 
 static void enqueue_step(ibtfo_case *c, int guard)
 {
+    if (c->cfg.time_advance == IBTFO_TIME_RK2)
+    {
+        // first stage and its Boundary + Global_Boundary, then the second
+        // stage with the average (the loop accounting happens there)
+        SweepArgs a = sweep_args(c, guard);
+        a.stage = 1;
+        c->sweep(a, dim3(c->ntiles), dim3(TILE_X * TILE_Y), c->stream);
+        count_launch();
+        enqueue_boundary(c);
+        a.stage = 2;
+        c->sweep(a, dim3(c->ntiles), dim3(TILE_X * TILE_Y), c->stream);
+        count_launch();
+        enqueue_boundary(c);
+        return;
+    }
     enqueue_advance(c, guard);
     enqueue_boundary(c);
 }
@@ -1243,6 +1264,7 @@ int case_batch_view(ibtfo_case *c, SweepArgs *sa, FillArgs *fa, int *scheme, int
 }
 
 cudaStream_t case_stream(const ibtfo_case *c) { return c->stream; }
+int case_time_advance(const ibtfo_case *c) { return c->cfg.time_advance; }
 int case_device(const ibtfo_case *c) { return c->device; }
 
 int case_set_dt(ibtfo_case *c, double dt)

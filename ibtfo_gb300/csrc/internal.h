@@ -114,6 +114,7 @@ struct SweepArgs
     double t_end;
     int max_iter;
     int guard;               // apply the reference loop condition before stepping
+    int stage;               // 0: one step; Time = RK2: 1 the first stage, 2 the second stage and average
 };
 
 struct FillArgs
@@ -307,6 +308,7 @@ double case_cfl(const ibtfo_case *c);
 int case_batch_view(ibtfo_case *c, SweepArgs *s, FillArgs *f, int *scheme, int *riemann, int *limiter,
                     int *precision, int *has_state);
 cudaStream_t case_stream(const ibtfo_case *c);
+int case_time_advance(const ibtfo_case *c);
 int case_device(const ibtfo_case *c);
 double case_gamma(const ibtfo_case *c);
 void set_last_error(const char *msg);

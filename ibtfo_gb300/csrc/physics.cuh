@@ -13,7 +13,7 @@
 
 namespace ibtfo {
 
-enum Scheme { MUSCL = 0, MHM = 1, GODUNOV = 2 };
+enum Scheme { MUSCL = 0, MHM = 1, GODUNOV = 2, LAX = 3 };
 enum Riemann { HLL = 0, HLLC = 1, PVRS = 2, SW = 3, HLLCT = 4 };
 enum Limiter { MINMOD = 0, VANLEER = 1 };
 

@@ -35,13 +35,32 @@ __device__ __forceinline__ void atomic_max_nonneg(unsigned long long *addr, doub
 // blocks to finish computes the next dt and advances the reference loop
 // accounting.  Deterministic: the mass partials are summed in a fixed order
 // (by block index `bid`) whichever block finishes last.  Called by every
-// thread of the block.
+// thread of the block.  A first RK2 stage (`first_stage`) commits nothing:
+// its last block only hands the stage's buffer to the boundary pass.
 template <int NT>
 __device__ __forceinline__ void block_commit_finalize(double a, double u, double v, double m, int n, DevState *st,
                                                       double *partial, const GridDesc &g, bool step_accounting,
-                                                      bool set_start, unsigned nblocks, unsigned bid)
+                                                      bool set_start, unsigned nblocks, unsigned bid,
+                                                      bool first_stage = false)
 {
     __shared__ bool last;
+    if (first_stage)
+    {
+        if (threadIdx.x == 0)
+        {
+            __threadfence();
+            unsigned t = atomicAdd(&st->ticket, 1u);
+            if (t == nblocks - 1)
+            {
+                volatile DevState *vs = st;
+                vs->cur = vs->cur ^ 1;
+                vs->fill_pending = 1;
+                vs->ticket = 0u;
+                __threadfence();
+            }
+        }
+        return;
+    }
     if (threadIdx.x == 0)
     {
         if (a > 0) atomic_max_nonneg(&st->amax_bits, a);
@@ -105,6 +124,17 @@ __device__ __forceinline__ void block_commit_finalize(double a, double u, double
     __syncthreads(); // msum and `last` are reused by the next tile of a persistent CTA
 }
 
+// Second RK2 stage: the cell's new state is 0.5 (U0 + w), w the advanced
+// first-stage state and U0 the state at the start of the step, which the
+// output buffer still holds at this cell (RK2.cpp:41-43 without the
+// reference's stride mix-up; the first stage never writes that buffer)
+__device__ __forceinline__ void rk2_average(const double *V, long long o, long long P, double v[4])
+{
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+        v[k] = 0.5 * (V[k * P + o] + v[k]);
+}
+
 // Per-thread CFL maxima, mass and NaN count of the cells a thread updated
 struct CellStats
 {
@@ -117,8 +147,14 @@ struct CellStats
 template <int NT>
 __device__ __forceinline__ void block_reduce_finalize(CellStats cs, DevState *st, double *partial, const GridDesc &g,
                                                       bool step_accounting, bool set_start, unsigned nblocks,
-                                                      unsigned bid)
+                                                      unsigned bid, bool first_stage = false)
 {
+    if (first_stage)
+    {
+        __syncthreads(); // every thread of the block has stored its cells
+        block_commit_finalize<NT>(0, 0, 0, 0, 0, st, partial, g, false, false, nblocks, bid, true);
+        return;
+    }
     __shared__ double red[4][NT / 32];
     __shared__ int rnan[NT / 32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -204,10 +240,12 @@ struct SweepSmem64
 
 // Advance the tile whose first interior cell is (i0, j0) from U into V and
 // accumulate the statistics of the updated cells.  All NT threads call it.
+// stage 2 (the second RK2 stage) stores 0.5 (V + the advanced state) instead,
+// V holding the state at the start of the step; stage 1 gathers no statistics.
 template <int SCH, int RIE, int LIM, int FAST, int TX, int TY, int NT>
 __device__ __forceinline__ void sweep_tile64(SweepSmem64<TX, TY> &s, const GridDesc &g, const double *__restrict__ U,
                                              double *__restrict__ V, const uint8_t *__restrict__ type, int i0, int j0,
-                                             double dt, CellStats &cs)
+                                             double dt, CellStats &cs, int stage = 0)
 {
     constexpr int WX = TX + 4, WY = TY + 4;
     const long long P = g.plane;
@@ -314,9 +352,13 @@ __device__ __forceinline__ void sweep_tile64(SweepSmem64<TX, TY> &s, const GridD
             }
             if constexpr (RIE == HLLCT)
                 pressure_floor(v);
+            if (stage == 2)
+                rk2_average(V, (long long)j * pitch + i, P, v);
 #pragma unroll
             for (int k = 0; k < 4; k++)
                 V[k * P + (long long)j * pitch + i] = v[k];
+            if (stage == 1)
+                continue;
             if (FAST)
                 cell_stats_fast(v, K, g.dxdy, cs);
             else
@@ -351,9 +393,9 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_kernel(const SweepArgs a
     const int i0 = g.ng + (int)(tile & 0xFFFFu) * TILE_X;
     const int j0 = g.ng + (int)(tile >> 16) * TILE_Y;
     CellStats cs;
-    sweep_tile64<SCH, RIE, LIM, FAST, TILE_X, TILE_Y, NT>(s, g, U, V, a.type, i0, j0, dt, cs);
+    sweep_tile64<SCH, RIE, LIM, FAST, TILE_X, TILE_Y, NT>(s, g, U, V, a.type, i0, j0, dt, cs, a.stage);
     block_reduce_finalize<NT>(cs, st, a.partial, g, true, false, gridDim.x * gridDim.y,
-                              blockIdx.y * gridDim.x + blockIdx.x);
+                              blockIdx.y * gridDim.x + blockIdx.x, a.stage == 1);
 }
 
 template <int SCH, int RIE, int LIM, int FAST>

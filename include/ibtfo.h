@@ -37,7 +37,16 @@ typedef enum ibtfo_status {
 
 /* selection keys: the reference Makefile slots Scheme / Riemann / Limiter /
  * Boundary (Test/Sod/Makefile:1-7) and the per-case Global_Boundary plug-in */
-enum { IBTFO_SCHEME_MUSCL = 0, IBTFO_SCHEME_MHM = 1, IBTFO_SCHEME_GODUNOV = 2 };
+/* LAX: the reference's Lax-Friedrichs scheme (Lax/Lax_Scheme.cpp; no Riemann
+ * solver or limiter), FP64 precisions, not with cut cells or in batches */
+enum { IBTFO_SCHEME_MUSCL = 0, IBTFO_SCHEME_MHM = 1, IBTFO_SCHEME_GODUNOV = 2, IBTFO_SCHEME_LAX = 3 };
+/* the reference's Time slot (Test/Sod/Makefile:5).  RK2: Heun's two-stage
+ * method, U1 = U0 + dt L(U0) with its Boundary and Global_Boundary passes,
+ * then 0.5 (U0 + U1 + dt L(U1)) on fluid cells, both stages with the dt of
+ * the step (the two-stage method Src/Base/TimeAdvance/RK2/RK2.cpp describes;
+ * that file itself does not compile).  FP64 precisions, not with cut cells
+ * or in batches. */
+enum { IBTFO_TIME_SINGLESTEP = 0, IBTFO_TIME_RK2 = 1 };
 /* HLLC is the reference's HLLC directory, whose solver is HLL (including the
  * Y-face slot reuse); HLLC_TORO is a contact-restoring HLLC with no
  * reference counterpart, with two positivity safeguards: a face whose
@@ -88,8 +97,9 @@ typedef struct ibtfo_config {
     double gamma, cfl_number, psy_time;
     int max_iter;
     int scheme, riemann, limiter, boundary, global_boundary;
-    int precision;   /* IBTFO_PRECISION_* */
-    int reserved[7]; /* zero */
+    int precision;    /* IBTFO_PRECISION_* */
+    int time_advance; /* IBTFO_TIME_* */
+    int reserved[6];  /* zero */
 } ibtfo_config;
 
 /* The reference time-loop scalars after the last completed step. */

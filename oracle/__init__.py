@@ -17,7 +17,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 
-SCHEMES = {"MUSCL": 0, "MHM": 1, "Godunov": 2}
+SCHEMES = {"MUSCL": 0, "MHM": 1, "Godunov": 2, "Lax": 3}
+TIME_ADVANCES = {"SingleStep": 0, "RK2": 1}
 RIEMANNS = {"HLL": 0, "HLLC": 1, "PVRS": 2, "StegerWarming": 3}
 LIMITERS = {"minmod": 0, "VanLeer": 1}
 BOUNDARIES = {"Regular": 0, "IDWBaseGFM": 1, "LinearBaseGFM": 2, "RiemannBaseGFM": 3, "BCGFM": 4, "HBCGFM": 5}
@@ -49,6 +50,7 @@ def lib():
         L.or_create.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                 C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
         L.or_destroy.argtypes = [C.c_void_p]
+        L.or_set_time_advance.argtypes = [C.c_void_p, C.c_int]
         L.or_set_threads.argtypes = [C.c_int]
         L.or_num_sch.argtypes = [C.c_void_p]
         L.or_setup_geometry.argtypes = [C.c_void_p, P]
@@ -80,7 +82,7 @@ class OracleCase:
     """One case on the CPU oracle (FP64, reference array-of-structures layout)."""
 
     def __init__(self, n_x, n_y, ng=2, lo=(0.0, 0.0), hi=(1.0, 1.0), gamma=1.4, cfl=0.5, scheme="MUSCL",
-                 riemann="HLL", limiter="minmod", boundary="Regular", gbc="walls"):
+                 riemann="HLL", limiter="minmod", boundary="Regular", gbc="walls", time="SingleStep"):
         self.L = lib()
         self.n_x, self.n_y, self.ng = n_x, n_y, ng
         self.M, self.N = n_x + 2 * ng, n_y + 2 * ng
@@ -89,6 +91,7 @@ class OracleCase:
         if not h:
             raise ValueError("oracle rejected the configuration")
         self.h = h
+        self.L.or_set_time_advance(h, TIME_ADVANCES[time])
         self.nsch = self.L.or_num_sch(h)
 
     def close(self):

@@ -24,7 +24,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 
-SCHEMES = ("MUSCL", "MHM", "Godunov")
+SCHEMES = ("MUSCL", "MHM", "Godunov")  # and Lax, below
 RIEMANNS = ("HLL", "HLLC", "PVRS", "StegerWarming")
 LIMITERS = ("minmod", "VanLeer")
 BOUNDARIES = ("Regular", "IDWBaseGFM", "LinearBaseGFM", "RiemannBaseGFM", "BCGFM", "HBCGFM")
@@ -56,6 +56,8 @@ def default_variants():
     v += [("MUSCL", "HLL", "minmod", "Regular", "refsod")]
     v += [("MUSCL", "HLL", "minmod", b, "refincline") for b in ("IDWBaseGFM", "LinearBaseGFM", "BCGFM", "HBCGFM")]
     v += [("MUSCL", "HLL", "minmod", "IDWBaseGFM", "refvortex")]
+    # Scheme = Lax takes no Riemann solver or limiter; the Makefile still links one of each
+    v += [("Lax", "HLL", "minmod", b, "file") for b in BOUNDARIES]
     return v
 
 

@@ -23,8 +23,9 @@ struct or_case
 {
     int n_x, n_y, ng, M, N, nsch;
     double lo_x, lo_y, hi_x, hi_y, gamma, cfl;
-    int scheme, riemann, limiter, boundary, gbc;
+    int scheme, riemann, limiter, boundary, gbc, time_advance;
     double *U_OLD, *U_NEW, *U_TMP, *XY, *SCH;
+    double *U_RK; /* RK2: the state at the start of the step */
     double dt, now_t, mass_start, mass_now;
     int iter;
 };
@@ -94,7 +95,7 @@ void or_destroy(or_case *c)
 {
     if (!c)
         return;
-    free(c->U_OLD); free(c->U_NEW); free(c->U_TMP); free(c->XY); free(c->SCH);
+    free(c->U_OLD); free(c->U_NEW); free(c->U_TMP); free(c->XY); free(c->SCH); free(c->U_RK);
     free(c);
 }
 
@@ -615,13 +616,59 @@ static void mhm_predict(or_case *c, int ydir, double dt, double h)
                 T_(i, j, S_UR, k) = T_(i, j, S_UR, k) + 0.5 * (T_(i, j, S_FL, k) - T_(i, j, S_FR, k)) * dt / h;
 }
 
-/* Advance: MUSCL_Scheme.cpp:6-152, MHM_Scheme.cpp:5-203, Godunov_Scheme.cpp:6-140 */
+/* Lax_Scheme.cpp:15-60: U_TMP = U_OLD and Conserve2Flux (Conserve2Flux.cpp:2-37)
+ * over every cell, then the Lax-Friedrichs update of the fluid cells.  The
+ * fluxes are kept in scratch slots 2 (F) and 3 (G), as in the Lax
+ * scheme's own layout (Lax/EQDefine.H: U_TMP, U_TMPRK, F_OLD, G_OLD). */
+static void lax_advance(or_case *c, double dt)
+{
+    const int M = c->M, N = c->N, ng = c->ng, n_x = c->n_x;
+    const double g = c->gamma;
+    const double dx = (c->hi_x - c->lo_x) / c->n_x;
+    const double dy = (c->hi_y - c->lo_y) / c->n_y;
+    const double *U = c->U_OLD;
+    double *V = c->U_NEW;
+#pragma omp parallel for
+    for (int j = 0; j < N; j++)
+        for (int i = 0; i < M; i++)
+        {
+            double rho = U_(U, i, j, 0);
+            double u = U_(U, i, j, 1) / rho;
+            double v = U_(U, i, j, 2) / rho;
+            double p = (g - 1) * (U_(U, i, j, 3) - 0.5 * rho * (u * u + v * v));
+            T_(i, j, 2, 0) = rho * u;
+            T_(i, j, 2, 1) = rho * u * u + p;
+            T_(i, j, 2, 2) = rho * u * v;
+            T_(i, j, 2, 3) = (U_(U, i, j, 3) + p) * u;
+            T_(i, j, 3, 0) = rho * v;
+            T_(i, j, 3, 1) = rho * u * v;
+            T_(i, j, 3, 2) = rho * v * v + p;
+            T_(i, j, 3, 3) = (U_(U, i, j, 3) + p) * v;
+        }
+#pragma omp parallel for
+    for (int j = ng; j < N - ng; j++)
+        for (int i = ng; i < n_x + ng; i++)
+            for (int k = 0; k < 4; k++)
+                if (XY_(i, j, 5) == 0)
+                    U_(V, i, j, k) = 0.25 * (U_(U, i - 1, j, k) + U_(U, i + 1, j, k) + U_(U, i, j + 1, k) +
+                                             U_(U, i, j - 1, k)) -
+                                     0.5 * dt * (T_(i + 1, j, 2, k) - T_(i - 1, j, 2, k)) / dx -
+                                     0.5 * dt * (T_(i, j + 1, 3, k) - T_(i, j - 1, 3, k)) / dy;
+}
+
+/* Advance: MUSCL_Scheme.cpp:6-152, MHM_Scheme.cpp:5-203, Godunov_Scheme.cpp:6-140,
+ * Lax_Scheme.cpp:2-64 */
 void or_advance(or_case *c, double dt)
 {
     const int ng = c->ng, N = c->N, n_x = c->n_x;
     const double dx = (c->hi_x - c->lo_x) / c->n_x;
     const double dy = (c->hi_y - c->lo_y) / c->n_y;
     double *U = c->U_OLD, *V = c->U_NEW;
+    if (c->scheme == OR_LAX)
+    {
+        lax_advance(c, dt);
+        return;
+    }
 
     recon_x(c);
     if (c->scheme == OR_MHM)
@@ -1104,6 +1151,42 @@ void or_set_initial_state(or_case *c, const double *u0)
     c->iter = 0;
 }
 
+void or_set_time_advance(or_case *c, int time_advance) { c->time_advance = time_advance; }
+
+/* Time = RK2 (Src/Base/TimeAdvance/RK2/RK2.cpp:12-48 names the stages: Advance,
+ * Boundary, Global_Boundary, Advance, then U_NEW = 0.5 (U_OLD + U_TMPRK) on
+ * fluid cells and U_NEW = U_OLD elsewhere).  That file does not compile
+ * (its signatures lack ndevices/device), its second Advance stores U_TMPRK
+ * with the state's stride (4 per cell) while the average reads it with the
+ * scratch stride, and by the time of the average Boundary has overwritten
+ * U_OLD with the first stage.  This restates the two-stage method the file
+ * describes, Heun's method: U1 = U0 + dt L(U0) with its ghost and edge
+ * fills, U_NEW = 0.5 (U0 + (U1 + dt L(U1))) on fluid cells (U1 elsewhere),
+ * both stages with the dt computed before the step. */
+static void rk2_advance(or_case *c, double dt)
+{
+    const int ng = c->ng, N = c->N, n_x = c->n_x;
+    const long n = (long)c->M * c->N * 4;
+    if (!c->U_RK)
+        c->U_RK = (double *)malloc(sizeof(double) * n);
+    memcpy(c->U_RK, c->U_OLD, sizeof(double) * n);
+    or_advance(c, dt);
+    or_boundary(c);
+    or_global_boundary(c);
+    or_advance(c, dt);
+    double *U = c->U_OLD, *V = c->U_NEW, *U0 = c->U_RK;
+#pragma omp parallel for
+    for (int j = ng; j < N - ng; j++)
+        for (int i = ng; i < n_x + ng; i++)
+            for (int k = 0; k < 4; k++)
+            {
+                if (XY_(i, j, 5) == 0)
+                    U_(V, i, j, k) = 0.5 * (U_(U0, i, j, k) + U_(V, i, j, k));
+                else
+                    U_(V, i, j, k) = U_(U, i, j, k);
+            }
+}
+
 /* time loop, Test/Sod/Sod.cpp:123-181: the dt applied in a step is the one
  * computed before it, and now_t advances by the dt computed after it (:176) */
 int or_run(or_case *c, int nsteps, double t_end, int max_iter, double *dts, double *masses)
@@ -1111,7 +1194,10 @@ int or_run(or_case *c, int nsteps, double t_end, int max_iter, double *dts, doub
     int done = 0;
     while (c->now_t < t_end && c->iter < max_iter && done < nsteps)
     {
-        or_advance(c, c->dt);
+        if (c->time_advance == OR_RK2)
+            rk2_advance(c, c->dt);
+        else
+            or_advance(c, c->dt);
         or_boundary(c);
         or_global_boundary(c);
         c->dt = or_compute_dt(c);

@@ -24,7 +24,8 @@
 extern "C" {
 #endif
 
-enum { OR_MUSCL = 0, OR_MHM = 1, OR_GODUNOV = 2 };
+enum { OR_MUSCL = 0, OR_MHM = 1, OR_GODUNOV = 2, OR_LAX = 3 };
+enum { OR_SINGLESTEP = 0, OR_RK2 = 1 };
 enum { OR_HLL = 0, OR_HLLC = 1, OR_PVRS = 2, OR_SW = 3 };
 enum { OR_MINMOD = 0, OR_VANLEER = 1 };
 enum { OR_REGULAR = 0, OR_IDW = 1, OR_LINEAR = 2, OR_RIEMANNGFM = 3, OR_BCGFM = 4, OR_HBCGFM = 5 };
@@ -35,6 +36,8 @@ typedef struct or_case or_case;
 or_case *or_create(int n_x, int n_y, int ng, double lo_x, double lo_y, double hi_x, double hi_y,
                    double gamma, double cfl, int scheme, int riemann, int limiter, int boundary, int gbc);
 void or_destroy(or_case *c);
+/* Time = SingleStep (default) or RK2 (two-stage, see or_run) */
+void or_set_time_advance(or_case *c, int time_advance);
 void or_set_threads(int n);
 int or_num_sch(const or_case *c);
 

@@ -8,7 +8,7 @@ sequences, now_t, and for ghost-fluid variants the geometry (XYCOORD) and the
 per-cell boundary data (SCHEME_IDX).
 
 Run in a container that has the reference sources:
-    python oracle/build_ref.py && python tests/golden/gen_golden.py
+    python oracle/build_ref.py && python tests/golden/gen_golden.py [fixture ...]
 """
 from __future__ import annotations
 
@@ -144,15 +144,24 @@ def fixtures():
                    base("refincline", 48, 48, (0, 0), (1, 1), 0.3, 0.3, "MUSCL", "HLL", "minmod", b, "refincline",
                         plugin_params={"angle": 30.0, "AxisD": 0.4, "rho_L": 1, "u_L": 0, "v_L": 0, "p_L": 1,
                                        "rho_R": 0.125, "u_R": 0, "v_R": 0, "p_R": 0.1}), 10))
+    # Scheme = Lax (Lax_Scheme.cpp): four-state problem, Sod tube to t_end, ghost-fluid channel
+    fx.append(("quad_Lax", base("quadrants", 32, 24, (0, 0), (1, 0.75), 0.3, 1.0, "Lax"), 10))
+    fx.append(("sodtube_Lax", base("sod_x", 80, 20, (0, 0), (1, 0.25), 0.5, 0.2, "Lax"), 1000))
+    for b in ("IDWBaseGFM", "BCGFM"):
+        fx.append((f"channel_Lax_{b}", base("channel", 64, 32, (0, 0), (2, 1), 0.45, 0.2, "Lax", "HLL", "minmod", b), 10))
     fx.append(("refvortex_MUSCL_HLL_minmod_IDWBaseGFM",
                base("refvortex", 48, 48, (0, 0), (1, 1), 0.3, 1.0, "MUSCL", "HLL", "minmod", "IDWBaseGFM", "refvortex",
                     plugin_params={"fa": 1.0, "fw": 0, "f0": 0, "f1": 1.0}), 10))
     return fx
 
 
-def main():
+def main(argv=None):
+    """Writes every fixture, or those whose names are given."""
+    names = set((argv if argv is not None else sys.argv[1:]))
     oracle.set_threads(1)
     for name, cfg, n in fixtures():
+        if names and name not in names:
+            continue
         rec = run_fixture(name, cfg, n)
         u = rec["u_old"]
         print(f"{name:48s} iters={rec['iters']:4d} now_t={rec['now_t']:.6g} nan={int(np.isnan(u).sum())}")

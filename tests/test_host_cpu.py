@@ -52,6 +52,16 @@ def test_config_from_inp():
 def test_unknown_slot_value_rejected():
     with pytest.raises(ib.IbtfoError):
         ib.Inp(text="Boundary = OIDWBaseGFM\n").config()
+    with pytest.raises(ib.IbtfoError):
+        ib.Inp(text="Time = RK4\n").config()
+
+
+def test_scheme_and_time_slots_of_the_makefile():
+    # Test/Sod/Makefile:1,5: Scheme = Lax | MUSCL | MHM | Godunov, Time = SingleStep | RK2
+    cfg = ib.Inp(text="Scheme = Lax\nTime = RK2\n").config()
+    assert cfg.scheme == ib.SCHEMES["Lax"] and cfg.time_advance == ib.TIME_ADVANCES["RK2"]
+    cfg = ib.Inp(text="Scheme = MUSCL\n").config()
+    assert cfg.time_advance == ib.TIME_ADVANCES["SingleStep"]
 
 
 def _cfg_of(fx):

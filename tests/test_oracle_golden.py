@@ -52,6 +52,8 @@ def test_fixture_set_covers_every_variant():
     for s in ("MUSCL", "MHM", "Godunov"):
         for r in ("HLL", "HLLC", "PVRS", "StegerWarming"):
             assert any(k[0] == s and k[1] == r for k in seen), (s, r)
+    assert any(k[0] == "Lax" and k[3] == "Regular" for k in seen)
+    assert any(k[0] == "Lax" and k[3] != "Regular" for k in seen)
     for b in ("Regular", "IDWBaseGFM", "LinearBaseGFM", "RiemannBaseGFM", "BCGFM", "HBCGFM"):
         assert any(k[3] == b for k in seen), b
     assert any(k[2] == "VanLeer" for k in seen)
