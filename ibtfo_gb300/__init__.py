@@ -146,6 +146,7 @@ SIGNATURES = {
     "ibtfo_set_state": (C.c_int, [_P, _DP]),
     "ibtfo_get_state": (C.c_int, [_P, _DP, _DP]),
     "ibtfo_put_state": (C.c_int, [_P, _DP]),
+    "ibtfo_step_host": (C.c_int, [_P, _DP, _DP, C.POINTER(Progress)]),
     "ibtfo_advance": (C.c_int, [_P, C.c_int]),
     "ibtfo_enqueue_sweep": (C.c_int, [_P]),
     "ibtfo_enqueue_boundary": (C.c_int, [_P]),
@@ -357,6 +358,15 @@ class Case:
 
     def get_state_ptr(self, host_ptr: int):
         _check(lib().ibtfo_get_state(self.h, C.cast(C.c_void_p(host_ptr), _DP), None))
+
+    def step_host_ptr(self, in_ptr: int, out_ptr: int):
+        """One step on host buffers (raw addresses, M*N*4 doubles each; may be
+        the same): put the state, step, read the new state back; returns the
+        progress."""
+        p = Progress()
+        _check(lib().ibtfo_step_host(self.h, C.cast(C.c_void_p(in_ptr), _DP), C.cast(C.c_void_p(out_ptr), _DP),
+                                     C.byref(p)))
+        return p.as_dict()
 
     # ---------------------------------------------------------- stepping
     def set_stream(self, stream_ptr: int | None):

@@ -411,4 +411,103 @@ void launch_soa_to_aos(const double *soa, double *aos, const GridDesc &g, cudaSt
     count_launch();
 }
 
+// the same conversions over rows [r0, r1), with the current buffer taken from
+// the device state when the kernel runs (so a step queued before it counts)
+__global__ void aos_to_cur_rows_kernel(const double *__restrict__ aos, double *b0, double *b1, DevState *st,
+                                       GridDesc g, int r0, int r1)
+{
+    long long c = (long long)r0 * g.M + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r0 == 0 && c == 0)
+        st->step_cur = st->cur; // read by the snapshot conversions of this step
+    if (c >= (long long)r1 * g.M)
+        return;
+    double *soa = st->cur ? b1 : b0;
+    int j = (int)(c / g.M), i = (int)(c - (long long)j * g.M);
+    long long o = (long long)j * g.pitch + i;
+    for (int k = 0; k < 4; k++)
+        state_st(soa, k, o, aos[c * 4 + k], g);
+}
+
+__global__ void cur_rows_to_aos_kernel(const double *b0, const double *b1, const DevState *__restrict__ st,
+                                       double *__restrict__ aos, GridDesc g, int r0, int r1)
+{
+    long long c = (long long)r0 * g.M + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= (long long)r1 * g.M)
+        return;
+    const double *soa = st->cur ? b1 : b0;
+    int j = (int)(c / g.M), i = (int)(c - (long long)j * g.M);
+    long long o = (long long)j * g.pitch + i;
+    for (int k = 0; k < 4; k++)
+        aos[c * 4 + k] = state_ld(soa, k, o, g);
+}
+
+void launch_aos_to_cur_rows(const double *aos, double *b0, double *b1, const DevState *st, const GridDesc &g, int r0,
+                            int r1, cudaStream_t s)
+{
+    long long n = (long long)(r1 - r0) * g.M;
+    if (n <= 0)
+        return;
+    aos_to_cur_rows_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(aos, b0, b1, const_cast<DevState *>(st), g,
+                                                                      r0, r1);
+    count_launch();
+}
+
+__global__ void snapshot_rows_to_aos_kernel(const double *b0, const double *b1, const DevState *__restrict__ st,
+                                            const uint8_t *__restrict__ type, double *__restrict__ aos, GridDesc g,
+                                            int r0, int r1)
+{
+    long long c = (long long)r0 * g.M + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= (long long)r1 * g.M)
+        return;
+    const int cur = st->step_cur;
+    int j = (int)(c / g.M), i = (int)(c - (long long)j * g.M);
+    long long o = (long long)j * g.pitch + i;
+    const double *src = (type[o] == CELL_FLUID) ? (cur ? b0 : b1) : (cur ? b1 : b0);
+    for (int k = 0; k < 4; k++)
+        aos[c * 4 + k] = state_ld(src, k, o, g);
+}
+
+void launch_snapshot_to_aos_rows(const double *b0, const double *b1, const DevState *st, const uint8_t *type,
+                                 double *aos, const GridDesc &g, int r0, int r1, cudaStream_t s)
+{
+    long long n = (long long)(r1 - r0) * g.M;
+    if (n <= 0)
+        return;
+    snapshot_rows_to_aos_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(b0, b1, st, type, aos, g, r0, r1);
+    count_launch();
+}
+
+__global__ void gather_cells_kernel(const double *b0, const double *b1, const DevState *__restrict__ st,
+                                    const long long *__restrict__ idx, int n, double *__restrict__ out, GridDesc g)
+{
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n)
+        return;
+    const double *src = st->cur ? b1 : b0;
+    long long c = idx[q];
+    int j = (int)(c / g.M), i = (int)(c - (long long)j * g.M);
+    long long o = (long long)j * g.pitch + i;
+    for (int k = 0; k < 4; k++)
+        out[(long long)q * 4 + k] = state_ld(src, k, o, g);
+}
+
+void launch_gather_cells(const double *b0, const double *b1, const DevState *st, const long long *idx, int n,
+                         double *out, const GridDesc &g, cudaStream_t s)
+{
+    if (n <= 0)
+        return;
+    gather_cells_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(b0, b1, st, idx, n, out, g);
+    count_launch();
+}
+
+void launch_cur_to_aos_rows(const double *b0, const double *b1, const DevState *st, double *aos, const GridDesc &g,
+                            int r0, int r1, cudaStream_t s)
+{
+    long long n = (long long)(r1 - r0) * g.M;
+    if (n <= 0)
+        return;
+    cur_rows_to_aos_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(b0, b1, st, aos, g, r0, r1);
+    count_launch();
+}
+
 } // namespace ibtfo

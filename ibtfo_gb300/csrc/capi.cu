@@ -137,7 +137,56 @@ struct ibtfo_case
     int graph_steps = 0;
     long long graph_launches = 0; // kernel launches in one replay of the graph
     VtkWriter *vtk = nullptr;     // asynchronous VTK output, created on first use
+    // ibtfo_step_host: row bands of the pipelined host-buffer step
+    std::vector<int> band_rows;   // NBANDS + 1 array-row offsets of the host-to-device chunks
+    std::vector<int> out_rows;    // NBANDS + 1 array-row offsets of the device-to-host chunks
+    std::vector<int> band_tiles;  // NBANDS + 1 offsets into the active-tile list
+    std::vector<long long> post_idx; // cells the boundary pass writes (ghost cells, then the domain ring)
+    long long *d_post_idx = nullptr;
+    double *d_post = nullptr, *h_post = nullptr; // their values after the step (device, pinned host)
+    cudaStream_t h2d = nullptr, d2h = nullptr, sw[2] = {nullptr, nullptr};
+    cudaEvent_t ev_in[8] = {}, ev_conv[8] = {}, ev_out[8] = {}, ev_sw[2] = {}, ev_done = nullptr;
 };
+
+// Row bands of ibtfo_step_host.  Band k sweeps the active tiles whose tile
+// row lies in [k*nty/NB, (k+1)*nty/NB); its transfer chunk ends at the last
+// array row that band's stencil reads (two rows above its tiles), so band k
+// can start once chunks 0..k are on the device.
+static const int NBANDS = 8;
+// bench.py counts this many device-to-host bytes for each progress read
+static_assert(sizeof(DevState) == 112, "DevState size changed: update the byte count of a progress read");
+static void make_bands(ibtfo_case *c, const std::vector<unsigned> &tiles)
+{
+    const GridDesc &g = c->g;
+    const int nty = (g.n_y + TILE_Y - 1) / TILE_Y;
+    c->band_rows.assign(NBANDS + 1, 0);
+    c->out_rows.assign(NBANDS + 1, 0);
+    c->band_tiles.assign(NBANDS + 1, 0);
+    size_t t = 0;
+    for (int k = 1; k <= NBANDS; k++)
+    {
+        const int tb = (int)((long long)k * nty / NBANDS);
+        c->band_rows[k] = (k == NBANDS) ? g.N : std::min(g.N, g.ng + tb * TILE_Y + 2);
+        c->out_rows[k] = (k == NBANDS) ? g.N : std::min(g.N, g.ng + tb * TILE_Y);
+        while (t < tiles.size() && (int)(tiles[t] >> 16) < tb)
+            t++;
+        c->band_tiles[k] = (k == NBANDS) ? (int)tiles.size() : (int)t;
+    }
+}
+
+// the cells a boundary pass writes: the ghost list, then every cell outside
+// the interior (the domain ring)
+static void make_post_cells(ibtfo_case *c, const std::vector<GhostRec> &gl)
+{
+    const GridDesc &g = c->g;
+    c->post_idx.clear();
+    for (const GhostRec &r : gl)
+        c->post_idx.push_back((long long)g.M * r.j + r.i);
+    for (int j = 0; j < g.N; j++)
+        for (int i = 0; i < g.M; i++)
+            if (i < g.ng || i >= g.n_x + g.ng || j < g.ng || j >= g.n_y + g.ng)
+                c->post_idx.push_back((long long)g.M * j + i);
+}
 
 // Case buffers come from the device's stream-ordered pool; freed memory stays
 // in the pool (no release threshold) so that cases created and destroyed
@@ -202,12 +251,27 @@ ibtfo_status ibtfo_destroy(ibtfo_case *c)
     if (c->graph)
         cudaGraphExecDestroy(c->graph);
     vtk_writer_destroy(c->vtk, c->own ? c->own : c->stream);
+    for (cudaStream_t s : {c->h2d, c->d2h, c->sw[0], c->sw[1]})
+        if (s)
+        {
+            cudaStreamSynchronize(s);
+            cudaStreamDestroy(s);
+        }
+    for (int k = 0; k < NBANDS; k++)
+        for (cudaEvent_t e : {c->ev_in[k], c->ev_conv[k], c->ev_out[k]})
+            if (e)
+                cudaEventDestroy(e);
+    for (cudaEvent_t e : {c->ev_sw[0], c->ev_sw[1], c->ev_done})
+        if (e)
+            cudaEventDestroy(e);
+    if (c->h_post)
+        cudaFreeHost(c->h_post);
     // stream-ordered frees: the memory returns to the device pool without a
     // device-wide synchronisation (other cases keep running)
     cudaStream_t fs = c->own ? c->own : c->stream;
     void *bufs[] = {c->buf[0], c->buf[1], c->ic, c->staging, c->phi, c->nx, c->ny, c->type, c->ghosts,
                     c->st, c->partial, c->ring_ic, c->tiles, c->alpha, c->ax, c->ay, c->mix_ex, c->mix_part,
-                    c->mix_links, c->mix_e};
+                    c->mix_links, c->mix_e, c->d_post_idx, c->d_post};
     for (void *p : bufs)
         if (p)
             cudaFreeAsync(p, fs);
@@ -370,8 +434,27 @@ static ibtfo_status geometry_from_phi(ibtfo_case *c)
     }
     else
         rc = setup_geometry(g, c->cfg.boundary, c->phi, c->nx, c->ny, c->type, &c->ghosts, &c->nghost, c->stream);
+    std::vector<unsigned> tile_list;
     if (rc == 0)
-        rc = active_tiles(g, c->type, &c->tiles, &c->ntiles, c->stream);
+        rc = active_tiles(g, c->type, &c->tiles, &c->ntiles, c->stream, &tile_list);
+    if (rc == 0)
+    {
+        make_bands(c, tile_list);
+        std::vector<GhostRec> gl(c->nghost);
+        if (c->nghost && (cudaMemcpyAsync(gl.data(), c->ghosts, sizeof(GhostRec) * c->nghost, cudaMemcpyDeviceToHost,
+                                          c->stream) != cudaSuccess ||
+                          cudaStreamSynchronize(c->stream) != cudaSuccess))
+            rc = 5;
+        make_post_cells(c, gl);
+        if (c->d_post_idx)
+            cudaFreeAsync(c->d_post_idx, c->stream);
+        if (c->d_post)
+            cudaFreeAsync(c->d_post, c->stream);
+        if (c->h_post)
+            cudaFreeHost(c->h_post);
+        c->d_post_idx = nullptr;
+        c->d_post = c->h_post = nullptr; // allocated by the first ibtfo_step_host
+    }
     if (rc == 2)
         return fail(IBTFO_ENOMEM, "geometry allocation failed");
     if (rc != 0)
@@ -1158,6 +1241,175 @@ ibtfo_status ibtfo_step(ibtfo_case *c, ibtfo_progress *p)
     if (p)
         return ibtfo_get_progress(c, p);
     CK(cudaStreamSynchronize(c->stream));
+    return IBTFO_OK;
+}
+
+// streams, events and buffers of ibtfo_step_host, created on first use
+static cudaError_t ensure_pipeline(ibtfo_case *c)
+{
+    cudaError_t e = cudaSuccess;
+    if (!c->ev_done)
+    {
+        for (cudaStream_t *s : {&c->h2d, &c->d2h, &c->sw[0], &c->sw[1]})
+            if (e == cudaSuccess)
+                e = cudaStreamCreateWithFlags(s, cudaStreamNonBlocking);
+        for (int k = 0; k < NBANDS && e == cudaSuccess; k++)
+            for (cudaEvent_t *v : {&c->ev_in[k], &c->ev_conv[k], &c->ev_out[k]})
+                if (e == cudaSuccess)
+                    e = cudaEventCreateWithFlags(v, cudaEventDisableTiming);
+        for (cudaEvent_t *v : {&c->ev_sw[0], &c->ev_sw[1], &c->ev_done})
+            if (e == cudaSuccess)
+                e = cudaEventCreateWithFlags(v, cudaEventDisableTiming);
+    }
+    const size_t n = c->post_idx.size();
+    if (e == cudaSuccess && n && !c->d_post_idx)
+    {
+        e = cudaMallocAsync(&c->d_post_idx, sizeof(long long) * n, c->stream);
+        if (e == cudaSuccess)
+            e = cudaMallocAsync(&c->d_post, sizeof(double) * 4 * n, c->stream);
+        if (e == cudaSuccess)
+            e = cudaMallocHost(&c->h_post, sizeof(double) * 4 * n);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(c->d_post_idx, c->post_idx.data(), sizeof(long long) * n, cudaMemcpyHostToDevice,
+                                c->stream);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(c->stream);
+    }
+    return e;
+}
+
+// The step when the banded pipeline does not apply (cut cells, RK2): the
+// whole state in, the step, the whole state out, still in row chunks.
+static ibtfo_status step_host_plain(ibtfo_case *c, const double *u_in, double *u_out)
+{
+    const GridDesc &g = c->g;
+    const size_t row = sizeof(double) * 4 * (size_t)g.M;
+    for (int k = 0; k < NBANDS; k++)
+    {
+        const int r0 = c->band_rows[k], r1 = c->band_rows[k + 1];
+        if (r1 > r0)
+            CK(cudaMemcpyAsync(c->staging + (size_t)r0 * 4 * g.M, u_in + (size_t)r0 * 4 * g.M, row * (r1 - r0),
+                               cudaMemcpyHostToDevice, c->h2d));
+        CK(cudaEventRecord(c->ev_in[k], c->h2d));
+        CK(cudaStreamWaitEvent(c->stream, c->ev_in[k], 0));
+        launch_aos_to_cur_rows(c->staging, c->buf[0], c->buf[1], c->st, g, r0, r1, c->stream);
+    }
+    enqueue_step(c, 0);
+    for (int k = 0; k < NBANDS; k++)
+    {
+        const int r0 = c->band_rows[k], r1 = c->band_rows[k + 1];
+        launch_cur_to_aos_rows(c->buf[0], c->buf[1], c->st, c->staging, g, r0, r1, c->stream);
+        CK(cudaEventRecord(c->ev_out[k], c->stream));
+        CK(cudaStreamWaitEvent(c->d2h, c->ev_out[k], 0));
+        if (r1 > r0)
+            CK(cudaMemcpyAsync(u_out + (size_t)r0 * 4 * g.M, c->staging + (size_t)r0 * 4 * g.M, row * (r1 - r0),
+                               cudaMemcpyDeviceToHost, c->d2h));
+    }
+    CK(cudaEventRecord(c->ev_done, c->d2h));
+    CK(cudaStreamWaitEvent(c->stream, c->ev_done, 0));
+    return IBTFO_OK;
+}
+
+// The banded pipeline.  Row chunk k goes host -> device on one copy stream;
+// the case's stream converts it into the current state buffer; band k of the
+// sweep (the tiles of tile rows [k*nty/8, (k+1)*nty/8), which read array
+// rows up to the end of chunk k) runs on one of two sweep streams, so that
+// consecutive bands overlap on the SMs; right behind it the band's rows are
+// converted back (fluid cells from the step's output, other cells from its
+// input) and go device -> host on the second copy stream while later bands
+// compute.  After the last band the boundary pass writes the ghost cells and
+// the domain ring; those cells alone are gathered, copied and scattered
+// into u_out on the host.  Every copy of u_in lands before any write to
+// u_out, so u_out may be u_in.
+static ibtfo_status step_host_banded(ibtfo_case *c, const double *u_in, double *u_out)
+{
+    const GridDesc &g = c->g;
+    const size_t row = sizeof(double) * 4 * (size_t)g.M;
+    for (int k = 0; k < NBANDS; k++)
+    {
+        const int r0 = c->band_rows[k], r1 = c->band_rows[k + 1];
+        if (r1 > r0)
+            CK(cudaMemcpyAsync(c->staging + (size_t)r0 * 4 * g.M, u_in + (size_t)r0 * 4 * g.M, row * (r1 - r0),
+                               cudaMemcpyHostToDevice, c->h2d));
+        CK(cudaEventRecord(c->ev_in[k], c->h2d));
+    }
+    SweepArgs a = sweep_args(c, 0);
+    a.nblocks = c->ntiles;
+    for (int k = 0; k < NBANDS; k++)
+    {
+        CK(cudaStreamWaitEvent(c->stream, c->ev_in[k], 0));
+        launch_aos_to_cur_rows(c->staging, c->buf[0], c->buf[1], c->st, g, c->band_rows[k], c->band_rows[k + 1],
+                               c->stream);
+        CK(cudaEventRecord(c->ev_conv[k], c->stream));
+        cudaStream_t s = c->sw[k & 1];
+        CK(cudaStreamWaitEvent(s, c->ev_conv[k], 0));
+        const int t0 = c->band_tiles[k], t1 = c->band_tiles[k + 1];
+        if (t1 > t0)
+        {
+            a.tile0 = t0;
+            c->sweep(a, dim3(t1 - t0), dim3(TILE_X * TILE_Y), s);
+            count_launch();
+        }
+        const int o0 = c->out_rows[k], o1 = c->out_rows[k + 1];
+        launch_snapshot_to_aos_rows(c->buf[0], c->buf[1], c->st, c->type, c->staging, g, o0, o1, s);
+        CK(cudaEventRecord(c->ev_out[k], s));
+        CK(cudaStreamWaitEvent(c->d2h, c->ev_out[k], 0));
+        if (o1 > o0)
+            CK(cudaMemcpyAsync(u_out + (size_t)o0 * 4 * g.M, c->staging + (size_t)o0 * 4 * g.M, row * (o1 - o0),
+                               cudaMemcpyDeviceToHost, c->d2h));
+    }
+    for (int q = 0; q < 2; q++)
+    {
+        CK(cudaEventRecord(c->ev_sw[q], c->sw[q]));
+        CK(cudaStreamWaitEvent(c->stream, c->ev_sw[q], 0));
+    }
+    enqueue_boundary(c);
+    const int n = (int)c->post_idx.size();
+    launch_gather_cells(c->buf[0], c->buf[1], c->st, c->d_post_idx, n, c->d_post, g, c->stream);
+    CK(cudaEventRecord(c->ev_done, c->stream));
+    CK(cudaStreamWaitEvent(c->d2h, c->ev_done, 0));
+    if (n)
+        CK(cudaMemcpyAsync(c->h_post, c->d_post, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, c->d2h));
+    CK(cudaEventRecord(c->ev_done, c->d2h));
+    CK(cudaStreamWaitEvent(c->stream, c->ev_done, 0));
+    return IBTFO_OK;
+}
+
+ibtfo_status ibtfo_step_host(ibtfo_case *c, const double *u_in, double *u_out, ibtfo_progress *p)
+{
+    if (!c || !u_in || !u_out)
+        return fail(IBTFO_EINVAL, "null argument");
+    if (!c->state)
+        return fail(IBTFO_ESTATE, "no state: call ibtfo_set_state first");
+    cudaSetDevice(c->device);
+    CK(ensure_staging(c));
+    CK(ensure_pipeline(c));
+    // every helper stream starts after what is already queued on the case's stream
+    CK(cudaEventRecord(c->ev_done, c->stream));
+    for (cudaStream_t s : {c->h2d, c->d2h, c->sw[0], c->sw[1]})
+        CK(cudaStreamWaitEvent(s, c->ev_done, 0));
+    const bool banded = !c->ccm && c->cfg.time_advance == IBTFO_TIME_SINGLESTEP;
+    ibtfo_status st = banded ? step_host_banded(c, u_in, u_out) : step_host_plain(c, u_in, u_out);
+    if (st != IBTFO_OK)
+        return st;
+    CK(cudaGetLastError());
+    ibtfo_progress q;
+    st = ibtfo_get_progress(c, p ? p : &q); // waits for the copies
+    if (st != IBTFO_OK)
+        return st;
+    if (banded)
+    {
+        const size_t n = c->post_idx.size();
+        for (size_t t = 0; t < n; t++)
+        {
+            double *d = u_out + c->post_idx[t] * 4;
+            const double *v = c->h_post + t * 4;
+            d[0] = v[0];
+            d[1] = v[1];
+            d[2] = v[2];
+            d[3] = v[3];
+        }
+    }
     return IBTFO_OK;
 }
 

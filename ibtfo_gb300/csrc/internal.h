@@ -35,6 +35,7 @@ struct DevState
     int nan_step;      // running count of the launch in progress
     unsigned int ticket;       // blocks finished in the current reduction launch
     int status;                // bit flags, see STATUS_*
+    int step_cur;              // ibtfo_step_host: the buffer that held the state when its step began
     double last_amax, last_umax, last_vmax; // maxima behind the latest dt
 };
 
@@ -115,6 +116,8 @@ struct SweepArgs
     int max_iter;
     int guard;               // apply the reference loop condition before stepping
     int stage;               // 0: one step; Time = RK2: 1 the first stage, 2 the second stage and average
+    int tile0;               // a step split over several launches: first tile of this launch
+    int nblocks;             // ... and the tiles of the whole step (0: one launch, its grid)
 };
 
 struct FillArgs
@@ -204,6 +207,19 @@ void launch_fill(const FillArgs &a, cudaStream_t s);
 void launch_reduce(const ReduceArgs &a, int nblocks_max, cudaStream_t s);
 void launch_aos_to_soa(const double *aos, double *soa, const GridDesc &g, cudaStream_t s);
 void launch_soa_to_aos(const double *soa, double *aos, const GridDesc &g, cudaStream_t s);
+// rows [r0, r1) of the current state buffer (picked on the device by st->cur)
+void launch_aos_to_cur_rows(const double *aos, double *b0, double *b1, const DevState *st, const GridDesc &g, int r0,
+                            int r1, cudaStream_t s);
+void launch_cur_to_aos_rows(const double *b0, const double *b1, const DevState *st, double *aos, const GridDesc &g,
+                            int r0, int r1, cudaStream_t s);
+// rows [r0, r1) of a step in flight (before its boundary pass): fluid cells
+// from the step's output buffer, the rest from its input (st->step_cur)
+void launch_snapshot_to_aos_rows(const double *b0, const double *b1, const DevState *st, const uint8_t *type,
+                                 double *aos, const GridDesc &g, int r0, int r1, cudaStream_t s);
+// the cells a boundary pass writes (linear indices M*j + i), gathered from the
+// current buffer into out[q*4 + k]
+void launch_gather_cells(const double *b0, const double *b1, const DevState *st, const long long *idx, int n,
+                         double *out, const GridDesc &g, cudaStream_t s);
 
 // ---------------------------------------------------------------- batches
 //
@@ -282,7 +298,8 @@ int vtk_writer_wait(VtkWriter *w, std::string *why);
 void vtk_writer_destroy(VtkWriter *w, cudaStream_t s);
 
 // geometry set-up (geometry.cu)
-int active_tiles(const GridDesc &g, const uint8_t *d_type, unsigned **d_tiles, int *ntiles, cudaStream_t s);
+int active_tiles(const GridDesc &g, const uint8_t *d_type, unsigned **d_tiles, int *ntiles, cudaStream_t s,
+                 std::vector<unsigned> *host_list = nullptr);
 // host list of the tx x ty tiles holding at least one fluid cell (bx | by << 16);
 // 0, or 2 (allocation) / 5 (CUDA error)
 int active_tile_list(const GridDesc &g, const uint8_t *d_type, int tx, int ty, std::vector<unsigned> &list,

@@ -255,12 +255,13 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_f32_kernel(const SweepAr
     const int cur = st->cur;
     const float *U = reinterpret_cast<const float *>(cur ? a.buf1 : a.buf0);
     float *V = reinterpret_cast<float *>(cur ? a.buf0 : a.buf1);
-    const unsigned tile = a.tiles[blockIdx.x];
+    const unsigned bid = a.tile0 + blockIdx.x;
+    const unsigned tile = a.tiles[bid];
     const int i0 = g.ng + (int)(tile & 0xFFFFu) * TILE_X;
     const int j0 = g.ng + (int)(tile >> 16) * TILE_Y;
     CellStats32 cs;
     sweep_tile32<SCH, RIE, LIM, TILE_X, TILE_Y, NT>(s, g, U, V, a.type, i0, j0, dt, cs);
-    block_reduce_finalize32<NT>(cs, st, a.partial, g, gridDim.x * gridDim.y, blockIdx.y * gridDim.x + blockIdx.x);
+    block_reduce_finalize32<NT>(cs, st, a.partial, g, a.nblocks ? a.nblocks : gridDim.x, bid);
 }
 
 template <int SCH, int RIE, int LIM>

@@ -389,13 +389,14 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_kernel(const SweepArgs a
     // tiles without fluid cells are skipped: nothing in them is updated or
     // counted by the reference (updates, ComputeDt and CaculateMass all test
     // the cell type), so the launch covers the active tiles only
-    const unsigned tile = a.tiles[blockIdx.x];
+    const unsigned bid = a.tile0 + blockIdx.x;
+    const unsigned tile = a.tiles[bid];
     const int i0 = g.ng + (int)(tile & 0xFFFFu) * TILE_X;
     const int j0 = g.ng + (int)(tile >> 16) * TILE_Y;
     CellStats cs;
     sweep_tile64<SCH, RIE, LIM, FAST, TILE_X, TILE_Y, NT>(s, g, U, V, a.type, i0, j0, dt, cs, a.stage);
-    block_reduce_finalize<NT>(cs, st, a.partial, g, true, false, gridDim.x * gridDim.y,
-                              blockIdx.y * gridDim.x + blockIdx.x, a.stage == 1);
+    block_reduce_finalize<NT>(cs, st, a.partial, g, true, false, a.nblocks ? a.nblocks : gridDim.x, bid,
+                              a.stage == 1);
 }
 
 template <int SCH, int RIE, int LIM, int FAST>

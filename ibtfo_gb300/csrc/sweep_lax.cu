@@ -43,7 +43,8 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) lax_kernel(const SweepArgs a)
     const int cur = st->cur;
     const double *U = cur ? a.buf1 : a.buf0;
     double *V = cur ? a.buf0 : a.buf1;
-    const unsigned tile = a.tiles[blockIdx.x];
+    const unsigned bid = a.tile0 + blockIdx.x;
+    const unsigned tile = a.tiles[bid];
     const int i0 = g.ng + (int)(tile & 0xFFFFu) * TILE_X;
     const int j0 = g.ng + (int)(tile >> 16) * TILE_Y;
     const long long P = g.plane;
@@ -104,7 +105,8 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) lax_kernel(const SweepArgs a)
         if (a.stage != 1)
             cell_stats(v, gam, g.dx, g.dy, cs);
     }
-    block_reduce_finalize<NT>(cs, st, a.partial, g, true, false, gridDim.x, blockIdx.x, a.stage == 1);
+    block_reduce_finalize<NT>(cs, st, a.partial, g, true, false, a.nblocks ? a.nblocks : gridDim.x, bid,
+                              a.stage == 1);
 }
 
 void launch_lax(const SweepArgs &a, dim3 grid, dim3 block, cudaStream_t s)

@@ -198,6 +198,14 @@ ibtfo_status ibtfo_case_bytes(const ibtfo_config *cfg, long long *resident, long
  * loop accounting, dt or U_NEW: the host-buffer round trip of a caller that
  * keeps its own copy of the state between steps. */
 ibtfo_status ibtfo_put_state(ibtfo_case *c, const double *u_old);
+/* One time-loop iteration on host arrays: u_in (M*N*4 doubles) replaces the
+ * current state as ibtfo_put_state does, the step runs as ibtfo_step does,
+ * and the new U_OLD is written to u_out (which may be u_in); waits for the
+ * result and fills `p` (may be NULL).  The transfers go in row chunks on two
+ * copy streams, overlapped with the layout conversion and the sweep (rows of
+ * the sweep start once their stencil is on the device): from page-locked
+ * host memory the copies run concurrently with the kernels. */
+ibtfo_status ibtfo_step_host(ibtfo_case *c, const double *u_in, double *u_out, ibtfo_progress *p);
 
 /* Queues `nsteps` iterations of the reference loop body (Sod.cpp:154-177:
  * TimeAdvance, Boundary, Global_Boundary, ComputeDt, CaculateMass,

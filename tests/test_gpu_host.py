@@ -193,3 +193,64 @@ def test_pinned_buffers_move_the_same_bytes_as_pageable_ones(precision):
     assert np.array_equal(outs[0][0], outs[1][0], equal_nan=True)
     assert np.array_equal(outs[0][1], outs[1][1], equal_nan=True)
     assert outs[0][2] == outs[1][2]
+
+
+@pytest.mark.parametrize("kind,precision", [("channel", "fp64_fast"), ("channel", "fp64"), ("channel", "fp32c"),
+                                            ("channel_rk2", "fp64_fast"), ("ccm", "fp32c"), ("sod", "fp64")])
+@pytest.mark.parametrize("in_place", [True, False])
+def test_step_host_equals_put_step_get(kind, precision, in_place):
+    """ibtfo_step_host (row-chunked copies overlapped with the banded sweep)
+    leaves the same state, progress and output bytes as ibtfo_put_state +
+    ibtfo_step + ibtfo_get_state, step after step."""
+    from ibtfo_gb300 import cases as _c
+    if kind.startswith("channel"):
+        w = _c.inclined_channel(512, 256)
+        g = w.grid
+        phi = _c.channel_phi(g)
+        kw = dict(precision=precision, time="RK2" if kind.endswith("rk2") else "SingleStep")
+
+        def make():
+            c = ib.Case.from_workload(w, **kw)
+            c.setup_geometry(phi)
+            c.set_state(_c.channel_init(g, c.cell_types(), w.gamma))
+            return c
+    elif kind == "ccm":
+        g = _c.Grid(192, 128, 2, 0.0, 0.0, 1.5, 1.0)
+
+        def make():
+            c = ib.Case(g.n_x, g.n_y, lo=(0, 0), hi=(1.5, 1.0), cfl=0.3, riemann="HLLC", boundary="CCM",
+                        precision=precision)
+            c.setup_geometry(_c.cylinder_phi(g, 0.6, 0.5, 0.2))
+            c.set_state(_c.shock_init(g, c.cell_types(), 2.0, 0.2))
+            return c
+    else:
+        g = _c.Grid(200, 40, 2, 0.0, 0.0, 1.0, 0.2)
+        phi, u0 = _c.sod_x(g)
+
+        def make():
+            c = ib.Case(g.n_x, g.n_y, lo=(0, 0), hi=(1.0, 0.2), cfl=0.5, precision=precision)
+            c.setup_geometry(phi)
+            c.set_state(u0)
+            return c
+    n = (g.n_x + 2 * g.ng) * (g.n_y + 2 * g.ng) * 4
+    ref, got = [], []
+    with make() as a:
+        u = a.get_state()
+        for _ in range(4):
+            a.put_state_ptr(u.ctypes.data)
+            a.step()
+            u = a.get_state()
+            ref.append((u.copy(), a.progress()))
+    with make() as b:
+        pin_in = ib.PinnedBuffer(n)
+        pin_out = pin_in if in_place else ib.PinnedBuffer(n)
+        b.get_state_ptr(pin_in.ptr)
+        for k in range(4):
+            p = b.step_host_ptr(pin_in.ptr, pin_out.ptr)
+            got.append((pin_out.array.copy(), p))
+            if not in_place:
+                pin_in.array[:] = pin_out.array
+        assert np.array_equal(b.get_state(), got[-1][0], equal_nan=True)
+    for (ur, pr), (ug, pg) in zip(ref, got):
+        assert np.array_equal(ur, ug, equal_nan=True)
+        assert pr == pg
