@@ -146,7 +146,30 @@ struct ibtfo_case
     double *d_post = nullptr, *h_post = nullptr; // their values after the step (device, pinned host)
     cudaStream_t h2d = nullptr, d2h = nullptr, sw[2] = {nullptr, nullptr};
     cudaEvent_t ev_in[8] = {}, ev_conv[8] = {}, ev_out[8] = {}, ev_sw[2] = {}, ev_done = nullptr;
+    // the banded step captured as a CUDA graph for one pair of page-locked host arrays
+    cudaGraphExec_t host_graph = nullptr;
+    const double *host_graph_in = nullptr;
+    double *host_graph_out = nullptr;
+    long long host_graph_launches = 0;
 };
+
+// graphs embed the case's kernel arguments and buffers: dropped whenever those change
+static void drop_graphs(ibtfo_case *c)
+{
+    if (c->graph)
+    {
+        cudaGraphExecDestroy(c->graph);
+        c->graph = nullptr;
+        c->graph_steps = 0;
+    }
+    if (c->host_graph)
+    {
+        cudaGraphExecDestroy(c->host_graph);
+        c->host_graph = nullptr;
+        c->host_graph_in = nullptr;
+        c->host_graph_out = nullptr;
+    }
+}
 
 // Row bands of ibtfo_step_host.  Band k sweeps the active tiles whose tile
 // row lies in [k*nty/NB, (k+1)*nty/NB); its transfer chunk ends at the last
@@ -248,8 +271,7 @@ ibtfo_status ibtfo_destroy(ibtfo_case *c)
     cudaSetDevice(c->device);
     if (c->stream)
         cudaStreamSynchronize(c->stream);
-    if (c->graph)
-        cudaGraphExecDestroy(c->graph);
+    drop_graphs(c);
     vtk_writer_destroy(c->vtk, c->own ? c->own : c->stream);
     for (cudaStream_t s : {c->h2d, c->d2h, c->sw[0], c->sw[1]})
         if (s)
@@ -383,12 +405,7 @@ ibtfo_status ibtfo_set_stream(ibtfo_case *c, void *stream)
     cudaSetDevice(c->device);
     CK(cudaStreamSynchronize(c->stream));
     c->stream = stream ? (cudaStream_t)stream : c->own;
-    if (c->graph)
-    {
-        cudaGraphExecDestroy(c->graph);
-        c->graph = nullptr;
-        c->graph_steps = 0;
-    }
+    drop_graphs(c);
     return IBTFO_OK;
 }
 
@@ -459,12 +476,7 @@ static ibtfo_status geometry_from_phi(ibtfo_case *c)
         return fail(IBTFO_ENOMEM, "geometry allocation failed");
     if (rc != 0)
         return cuda_fail(cudaGetLastError(), "geometry set-up");
-    if (c->graph)
-    {
-        cudaGraphExecDestroy(c->graph);
-        c->graph = nullptr;
-        c->graph_steps = 0;
-    }
+    drop_graphs(c);
     CK(cudaStreamSynchronize(c->stream));
     c->geometry = true;
     c->state = false;
@@ -1384,14 +1396,59 @@ ibtfo_status ibtfo_step_host(ibtfo_case *c, const double *u_in, double *u_out, i
     cudaSetDevice(c->device);
     CK(ensure_staging(c));
     CK(ensure_pipeline(c));
-    // every helper stream starts after what is already queued on the case's stream
-    CK(cudaEventRecord(c->ev_done, c->stream));
-    for (cudaStream_t s : {c->h2d, c->d2h, c->sw[0], c->sw[1]})
-        CK(cudaStreamWaitEvent(s, c->ev_done, 0));
     const bool banded = !c->ccm && c->cfg.time_advance == IBTFO_TIME_SINGLESTEP;
-    ibtfo_status st = banded ? step_host_banded(c, u_in, u_out) : step_host_plain(c, u_in, u_out);
-    if (st != IBTFO_OK)
-        return st;
+    // page-locked arrays: the banded step replays as one CUDA graph (captured
+    // for this pair of arrays; about 100 stream operations in one launch)
+    bool graph = false;
+    if (banded)
+    {
+        cudaPointerAttributes ai, ao;
+        graph = cudaPointerGetAttributes(&ai, u_in) == cudaSuccess && ai.type == cudaMemoryTypeHost &&
+                cudaPointerGetAttributes(&ao, u_out) == cudaSuccess && ao.type == cudaMemoryTypeHost;
+        cudaGetLastError();
+    }
+    ibtfo_status st = IBTFO_OK;
+    if (graph && (c->host_graph_in != u_in || c->host_graph_out != u_out || !c->host_graph))
+    {
+        if (c->host_graph)
+            cudaGraphExecDestroy(c->host_graph);
+        c->host_graph = nullptr;
+        cudaGraph_t gr;
+        long long before = g_launches.load();
+        CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        cudaEventRecord(c->ev_done, c->stream);
+        for (cudaStream_t s : {c->h2d, c->d2h, c->sw[0], c->sw[1]})
+            cudaStreamWaitEvent(s, c->ev_done, 0);
+        st = step_host_banded(c, u_in, u_out);
+        c->host_graph_launches = g_launches.load() - before;
+        g_launches.store(before); // counted when replayed
+        cudaError_t e = cudaStreamEndCapture(c->stream, &gr);
+        if (st != IBTFO_OK)
+            return st;
+        if (e != cudaSuccess)
+            return cuda_fail(e, "capturing the host step");
+        e = cudaGraphInstantiate(&c->host_graph, gr, 0);
+        cudaGraphDestroy(gr);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "instantiating the host step");
+        c->host_graph_in = u_in;
+        c->host_graph_out = u_out;
+    }
+    if (graph)
+    {
+        CK(cudaGraphLaunch(c->host_graph, c->stream));
+        count_launch((int)c->host_graph_launches);
+    }
+    else
+    {
+        // every helper stream starts after what is already queued on the case's stream
+        CK(cudaEventRecord(c->ev_done, c->stream));
+        for (cudaStream_t s : {c->h2d, c->d2h, c->sw[0], c->sw[1]})
+            CK(cudaStreamWaitEvent(s, c->ev_done, 0));
+        st = banded ? step_host_banded(c, u_in, u_out) : step_host_plain(c, u_in, u_out);
+        if (st != IBTFO_OK)
+            return st;
+    }
     CK(cudaGetLastError());
     ibtfo_progress q;
     st = ibtfo_get_progress(c, p ? p : &q); // waits for the copies
@@ -1473,15 +1530,7 @@ ibtfo_status ibtfo_host_free(void *p)
 // ---------------------------------------------------------------- internal
 namespace ibtfo {
 
-static void drop_graph(ibtfo_case *c)
-{
-    if (c->graph)
-    {
-        cudaGraphExecDestroy(c->graph);
-        c->graph = nullptr;
-        c->graph_steps = 0;
-    }
-}
+static void drop_graph(ibtfo_case *c) { drop_graphs(c); }
 
 int case_set_gas(ibtfo_case *c, double gamma, double cfl)
 {

@@ -197,11 +197,12 @@ def test_pinned_buffers_move_the_same_bytes_as_pageable_ones(precision):
 
 @pytest.mark.parametrize("kind,precision", [("channel", "fp64_fast"), ("channel", "fp64"), ("channel", "fp32c"),
                                             ("channel_rk2", "fp64_fast"), ("ccm", "fp32c"), ("sod", "fp64")])
-@pytest.mark.parametrize("in_place", [True, False])
-def test_step_host_equals_put_step_get(kind, precision, in_place):
-    """ibtfo_step_host (row-chunked copies overlapped with the banded sweep)
-    leaves the same state, progress and output bytes as ibtfo_put_state +
-    ibtfo_step + ibtfo_get_state, step after step."""
+@pytest.mark.parametrize("in_place,pinned", [(True, True), (False, True), (True, False)])
+def test_step_host_equals_put_step_get(kind, precision, in_place, pinned):
+    """ibtfo_step_host (row-chunked copies overlapped with the banded sweep,
+    replayed as a CUDA graph for page-locked arrays) leaves the same state,
+    progress and output bytes as ibtfo_put_state + ibtfo_step +
+    ibtfo_get_state, step after step."""
     from ibtfo_gb300 import cases as _c
     if kind.startswith("channel"):
         w = _c.inclined_channel(512, 256)
@@ -242,14 +243,19 @@ def test_step_host_equals_put_step_get(kind, precision, in_place):
             u = a.get_state()
             ref.append((u.copy(), a.progress()))
     with make() as b:
-        pin_in = ib.PinnedBuffer(n)
-        pin_out = pin_in if in_place else ib.PinnedBuffer(n)
-        b.get_state_ptr(pin_in.ptr)
+        if pinned:
+            pin_in = ib.PinnedBuffer(n)
+            pin_out = pin_in if in_place else ib.PinnedBuffer(n)
+            a_in, a_out, p_in, p_out = pin_in.array, pin_out.array, pin_in.ptr, pin_out.ptr
+        else:
+            a_in = a_out = np.zeros(n)
+            p_in = p_out = a_in.ctypes.data
+        b.get_state_ptr(p_in)
         for k in range(4):
-            p = b.step_host_ptr(pin_in.ptr, pin_out.ptr)
-            got.append((pin_out.array.copy(), p))
+            p = b.step_host_ptr(p_in, p_out)
+            got.append((a_out.copy(), p))
             if not in_place:
-                pin_in.array[:] = pin_out.array
+                a_in[:] = a_out
         assert np.array_equal(b.get_state(), got[-1][0], equal_nan=True)
     for (ur, pr), (ug, pg) in zip(ref, got):
         assert np.array_equal(ur, ug, equal_nan=True)
