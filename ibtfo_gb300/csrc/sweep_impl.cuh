@@ -217,7 +217,7 @@ __device__ __forceinline__ void cell_stats_fast(const double v[4], const GasCons
     const double ir = rcp_t(v[0]);
     const double u = v[1] * ir, w = v[2] * ir;
     const double p = K.gm1 * (v[3] - 0.5 * v[0] * (u * u + w * w));
-    const double a = pow_half(K.g * p * ir);
+    const double a = sqrt_t(K.g * ir * p);
     cs.amax = fmax(cs.amax, a);
     cs.umax = fmax(cs.umax, fabs(u));
     cs.vmax = fmax(cs.vmax, fabs(w));
