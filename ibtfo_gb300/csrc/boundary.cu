@@ -356,7 +356,7 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) reduce_kernel(const ReduceArgs
             cs.nans += c1.nans;
             if (a.alpha[o] >= 0.5)
             {
-                cs.amax = fmax(cs.amax, c1.amax);
+                cs.a2max = fmax(cs.a2max, c1.a2max);
                 cs.umax = fmax(cs.umax, c1.umax);
                 cs.vmax = fmax(cs.vmax, c1.vmax);
             }

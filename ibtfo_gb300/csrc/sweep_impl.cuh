@@ -135,10 +135,13 @@ __device__ __forceinline__ void rk2_average(const double *V, long long o, long l
         v[k] = 0.5 * (V[k * P + o] + v[k]);
 }
 
-// Per-thread CFL maxima, mass and NaN count of the cells a thread updated
+// Per-thread CFL maxima, mass and NaN count of the cells a thread updated.
+// The sound speed enters as its square (a2max); the block takes one square
+// root of the maximum, which equals the maximum of the roots (the root is
+// monotone and correctly rounded; NaN and negative squares drop out of both).
 struct CellStats
 {
-    double amax = 0.0, umax = 0.0, vmax = 0.0, mass = 0.0;
+    double amax = 0.0, a2max = 0.0, umax = 0.0, vmax = 0.0, mass = 0.0;
     int nans = 0;
 };
 
@@ -155,13 +158,14 @@ __device__ __forceinline__ void block_reduce_finalize(CellStats cs, DevState *st
         block_commit_finalize<NT>(0, 0, 0, 0, 0, st, partial, g, false, false, nblocks, bid, true);
         return;
     }
-    __shared__ double red[4][NT / 32];
+    __shared__ double red[5][NT / 32];
     __shared__ int rnan[NT / 32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1)
     {
         cs.amax = fmax(cs.amax, __shfl_xor_sync(0xffffffffu, cs.amax, o));
+        cs.a2max = fmax(cs.a2max, __shfl_xor_sync(0xffffffffu, cs.a2max, o));
         cs.umax = fmax(cs.umax, __shfl_xor_sync(0xffffffffu, cs.umax, o));
         cs.vmax = fmax(cs.vmax, __shfl_xor_sync(0xffffffffu, cs.vmax, o));
         cs.mass += __shfl_xor_sync(0xffffffffu, cs.mass, o);
@@ -173,6 +177,7 @@ __device__ __forceinline__ void block_reduce_finalize(CellStats cs, DevState *st
         red[1][wid] = cs.umax;
         red[2][wid] = cs.vmax;
         red[3][wid] = cs.mass;
+        red[4][wid] = cs.a2max;
         rnan[wid] = cs.nans;
     }
     __syncthreads();
@@ -180,16 +185,19 @@ __device__ __forceinline__ void block_reduce_finalize(CellStats cs, DevState *st
     int n = 0;
     if (threadIdx.x == 0)
     {
+        double a2 = red[4][0];
         a = red[0][0], u = red[1][0], v = red[2][0], m = red[3][0];
         n = rnan[0];
         for (int w = 1; w < NT / 32; w++)
         {
             a = fmax(a, red[0][w]);
+            a2 = fmax(a2, red[4][w]);
             u = fmax(u, red[1][w]);
             v = fmax(v, red[2][w]);
             m += red[3][w];
             n += rnan[w];
         }
+        a = fmax(a, sqrt(a2));
     }
     block_commit_finalize<NT>(a, u, v, m, n, st, partial, g, step_accounting, set_start, nblocks, bid);
 }
@@ -202,8 +210,7 @@ __device__ __forceinline__ void cell_stats(const double v[4], double gam, double
     double u = v[1] / v[0];
     double w = v[2] / v[0];
     double p = (gam - 1) * (v[3] - 0.5 * rho * (u * u + w * w));
-    double a = pow_half(gam * p / rho);
-    cs.amax = fmax(cs.amax, a);
+    cs.a2max = fmax(cs.a2max, gam * p / rho); // pow(gam p / rho, 0.5) taken once per block
     cs.umax = fmax(cs.umax, fabs(u));
     cs.vmax = fmax(cs.vmax, fabs(w));
     cs.mass += v[0] * dx * dy;
@@ -217,8 +224,7 @@ __device__ __forceinline__ void cell_stats_fast(const double v[4], const GasCons
     const double ir = rcp_t(v[0]);
     const double u = v[1] * ir, w = v[2] * ir;
     const double p = K.gm1 * (v[3] - 0.5 * v[0] * (u * u + w * w));
-    const double a = sqrt_t(K.g * ir * p);
-    cs.amax = fmax(cs.amax, a);
+    cs.a2max = fmax(cs.a2max, K.g * ir * p);
     cs.umax = fmax(cs.umax, fabs(u));
     cs.vmax = fmax(cs.vmax, fabs(w));
     cs.mass += v[0] * dxdy;
@@ -277,14 +283,16 @@ __device__ __forceinline__ void sweep_tile64(SweepSmem64<TX, TY> &s, const GridD
     const double gam = g.gamma;
     const GasConst<double> K(gam, g.gm1, g.c1, g.c2, g.igm1, g.ig2);
     const double hx2 = FASTPHYS ? s.sC[2] : 0.0, hy2 = FASTPHYS ? s.sC[3] : 0.0; // MHM predictor of physics_fast
-    constexpr int NXF = (TX + 1) * (TY + 1);
+    // X faces of the tile's rows (sF rows 1..TY) and all Y faces; the X faces
+    // of the row below the tile (sF row 0) follow below, where needed
+    constexpr int NXF = (TX + 1) * TY;
     constexpr int NYF = TX * (TY + 1);
     for (int q = tid; q < NXF + NYF; q += NT)
     {
         double c0[4], c1[4], c2[4], c3[4], f[4];
         if (q < NXF)
         {
-            int r = q / (TX + 1), fc = q - r * (TX + 1);
+            int r = q / (TX + 1) + 1, fc = q - (r - 1) * (TX + 1);
 #pragma unroll
             for (int k = 0; k < 4; k++)
             {
@@ -321,6 +329,30 @@ __device__ __forceinline__ void sweep_tile64(SweepSmem64<TX, TY> &s, const GridD
                 s.sG[k][r][c] = f[k];
             s.sKeep[r][c] = (unsigned char)keep;
         }
+    }
+    __syncthreads();
+    // a bottom Y face (j0 - 1/2) that kept the X-face flux of its slot, as
+    // the reference's Y solver does in some branches, reads the X face
+    // (i + 1/2, j0 - 1): solved only for those columns
+    if (tid < TX && s.sKeep[0][tid])
+    {
+        const int fc = tid + 1;
+        double c0[4], c1[4], c2[4], c3[4], f[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+        {
+            c0[k] = s.sU[k][1][fc];
+            c1[k] = s.sU[k][1][fc + 1];
+            c2[k] = s.sU[k][1][fc + 2];
+            c3[k] = s.sU[k][1][fc + 3];
+        }
+        if (FASTPHYS)
+            x_face_fast<double, SCH, RIE, LIM>(c0, c1, c2, c3, K, hx2, f);
+        else
+            x_face<SCH, RIE, LIM>(c0, c1, c2, c3, gam, dt, g.dx, f);
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            s.sF[k][0][fc] = f[k];
     }
     __syncthreads();
 
