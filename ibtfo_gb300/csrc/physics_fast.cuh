@@ -148,19 +148,21 @@ __device__ __forceinline__ Prim<T> prim_fast(const T U[4], const GasConst<T> &K)
     s.ir = rcp_t(U[0]);
     s.un = U[NRM] * s.ir;
     s.ut = U[3 - NRM] * s.ir;
-    s.p = K.gm1 * (U[3] - (T)0.5 * s.r * (s.un * s.un + s.ut * s.ut));
+    // rho (un^2 + ut^2) = m_n un + m_t ut
+    s.p = K.gm1 * fma_t((T)-0.5, fma_t(U[NRM], s.un, U[3 - NRM] * s.ut), U[3]);
     s.gi = K.g * s.ir;
     s.a = sqrt_t(s.gi * s.p);
     return s;
 }
 
 // physical flux normal to the face; components in state order
+// (the mass flux rho un is the normal momentum itself)
 template <typename T, int NRM>
 __device__ __forceinline__ void flux_fast(const T U[4], const Prim<T> &s, T F[4])
 {
-    const T m = s.r * s.un;
+    const T m = U[NRM];
     F[0] = m;
-    F[NRM] = m * s.un + s.p;
+    F[NRM] = fma_t(m, s.un, s.p);
     F[3 - NRM] = m * s.ut;
     F[3] = (U[3] + s.p) * s.un;
 }
@@ -319,7 +321,7 @@ __device__ __forceinline__ T internal_energy(const T U[4])
 {
     const T ir = rcp_t(U[0]);
     const T u = U[1] * ir, v = U[2] * ir;
-    return U[3] - (T)0.5 * U[0] * (u * u + v * v);
+    return fma_t((T)-0.5, fma_t(U[1], u, U[2] * v), U[3]);
 }
 
 // positive density and an internal energy above 1e-6 E (NaN fails)

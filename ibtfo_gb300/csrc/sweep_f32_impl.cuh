@@ -239,7 +239,7 @@ __device__ __forceinline__ void block_reduce_finalize32(CellStats32 cs, DevState
 
 // one case: one CTA per active tile
 template <int SCH, int RIE, int LIM>
-__global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_f32_kernel(const SweepArgs a)
+__global__ void __launch_bounds__(TILE_X *TILE_Y, 6) sweep_f32_kernel(const SweepArgs a)
 {
     constexpr int NT = TILE_X * TILE_Y;
     extern __shared__ __align__(16) unsigned char smem_raw[];

@@ -223,7 +223,7 @@ __device__ __forceinline__ void cell_stats_fast(const double v[4], const GasCons
 {
     const double ir = rcp_t(v[0]);
     const double u = v[1] * ir, w = v[2] * ir;
-    const double p = K.gm1 * (v[3] - 0.5 * v[0] * (u * u + w * w));
+    const double p = K.gm1 * fma(-0.5, fma(v[1], u, v[2] * w), v[3]);
     cs.a2max = fmax(cs.a2max, K.g * ir * p);
     cs.umax = fmax(cs.umax, fabs(u));
     cs.vmax = fmax(cs.vmax, fabs(w));
