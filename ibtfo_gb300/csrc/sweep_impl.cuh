@@ -401,7 +401,9 @@ __device__ __forceinline__ void sweep_tile64(SweepSmem64<TX, TY> &s, const GridD
 
 // one case: one CTA per active tile
 template <int SCH, int RIE, int LIM, int FAST>
-__global__ void __launch_bounds__(TILE_X *TILE_Y) sweep_kernel(const SweepArgs a)
+// fp64_fast with HLL or Steger-Warming fits 64 registers: 4 CTAs per SM
+__global__ void __launch_bounds__(TILE_X *TILE_Y, (FAST && (RIE == HLL || RIE == SW)) ? 4 : 1)
+    sweep_kernel(const SweepArgs a)
 {
     constexpr int NT = TILE_X * TILE_Y;
     extern __shared__ __align__(16) unsigned char smem_raw[];
