@@ -89,12 +89,11 @@ __device__ __forceinline__ double minmod_t(double a, double b)
                     mb <= 0x7ff0000000000000LL;
     return ok ? ((ma > mb) ? b : a) : 0.0;
 }
+// FP32: the reference's form, a product and two compares on the FP32 pipes
+// (a product below the smallest float counts as not positive)
 __device__ __forceinline__ float minmod_t(float a, float b)
 {
-    const int ia = __float_as_int(a), ib = __float_as_int(b);
-    const int ma = ia & 0x7fffffff, mb = ib & 0x7fffffff;
-    const bool ok = ((ia ^ ib) >= 0) && ma != 0 && mb != 0 && ma <= 0x7f800000 && mb <= 0x7f800000;
-    return ok ? ((ma > mb) ? b : a) : 0.0f;
+    return (a * b > 0.0f) ? ((fabsf(a) > fabsf(b)) ? b : a) : 0.0f;
 }
 
 // VanLeer as the reference macro expands (physics.cuh lim_vanleer)

@@ -79,29 +79,42 @@ __device__ __forceinline__ void sweep_tile32(SweepSmem32<TX, TY> &s, const GridD
         s.sC[3] = 0.5f * s.sC[1];
     }
 
-    for (int q = tid; q < 4 * WX * WY; q += NT)
+    // stage the tile and its halo: one index computation per cell, four planes
+    for (int q = tid; q < WX * WY; q += NT)
     {
-        int k = q / (WX * WY);
-        int r = q - k * (WX * WY);
-        int ly = r / WX, lx = r - ly * WX;
-        int gi = i0 - 2 + lx, gj = j0 - 2 + ly;
-        float v = 0.0f;
+        const int ly = q / WX, lx = q - ly * WX;
+        const int gi = i0 - 2 + lx, gj = j0 - 2 + ly;
+        float v[4] = {0.0f, 0.0f, 0.0f, 0.0f};
         if (gi < g.M && gj < g.N)
-            v = U[k * P + (long long)gj * pitch + gi];
-        s.sU[k][ly][lx] = v;
+        {
+            const float *src = U + (long long)gj * pitch + gi;
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                v[k] = src[k * P];
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            s.sU[k][ly][lx] = v[k];
     }
     __syncthreads();
 
     const GasConst<float> K(g.gf, g.gm1f, g.c1f, g.c2f, g.igm1f, g.ig2f);
     const float hx2 = s.sC[2], hy2 = s.sC[3];
-    constexpr int NXF = (TX + 1) * (TY + 1);
+    // X faces of the tile's rows (sF rows 1..TY; a warp reads one row of sU:
+    // columns 0..TX-1 first, the last column after) and all Y faces; the X
+    // faces of the row below the tile follow below, where needed
+    constexpr int NXF = (TX + 1) * TY;
     constexpr int NYF = TX * (TY + 1);
     for (int q = tid; q < NXF + NYF; q += NT)
     {
         float c0[4], c1[4], c2[4], c3[4], f[4];
         if (q < NXF)
         {
-            int r = q / (TX + 1), fc = q - r * (TX + 1);
+            int r, fc;
+            if (q < TX * TY)
+                r = q / TX + 1, fc = q - (r - 1) * TX;
+            else
+                r = q - TX * TY + 1, fc = TX;
 #pragma unroll
             for (int k = 0; k < 4; k++)
             {
@@ -134,6 +147,26 @@ __device__ __forceinline__ void sweep_tile32(SweepSmem32<TX, TY> &s, const GridD
                 s.sG[k][r][c] = f[k];
             s.sKeep[r][c] = (unsigned char)keep;
         }
+    }
+    __syncthreads();
+    // X faces (i + 1/2, j0 - 1), read only where a bottom Y face kept the X
+    // flux of its slot (the reference's Y-solver aliasing)
+    if (tid < TX && s.sKeep[0][tid])
+    {
+        const int fc = tid + 1;
+        float c0[4], c1[4], c2[4], c3[4], f[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+        {
+            c0[k] = s.sU[k][1][fc];
+            c1[k] = s.sU[k][1][fc + 1];
+            c2[k] = s.sU[k][1][fc + 2];
+            c3[k] = s.sU[k][1][fc + 3];
+        }
+        x_face_fast<float, SCH, RIE, LIM>(c0, c1, c2, c3, K, hx2, f);
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            s.sF[k][0][fc] = f[k];
     }
     __syncthreads();
 

@@ -266,17 +266,23 @@ __device__ __forceinline__ void sweep_tile64(SweepSmem64<TX, TY> &s, const GridD
         s.sC[3] = 0.5 * s.sC[1];
     }
 
-    // stage the tile and its halo (always inside the padded array: ng >= 2)
-    for (int q = tid; q < 4 * WX * WY; q += NT)
+    // stage the tile and its halo (always inside the padded array: ng >= 2),
+    // one index computation per cell for the four planes
+    for (int q = tid; q < WX * WY; q += NT)
     {
-        int k = q / (WX * WY);
-        int r = q - k * (WX * WY);
-        int ly = r / WX, lx = r - ly * WX;
-        int gi = i0 - 2 + lx, gj = j0 - 2 + ly;
-        double v = 0.0;
+        const int ly = q / WX, lx = q - ly * WX;
+        const int gi = i0 - 2 + lx, gj = j0 - 2 + ly;
+        double v[4] = {0.0, 0.0, 0.0, 0.0};
         if (gi < g.M && gj < g.N)
-            v = U[k * P + (long long)gj * pitch + gi];
-        s.sU[k][ly][lx] = v;
+        {
+            const double *src = U + (long long)gj * pitch + gi;
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                v[k] = src[k * P];
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            s.sU[k][ly][lx] = v[k];
     }
     __syncthreads();
 
@@ -292,7 +298,11 @@ __device__ __forceinline__ void sweep_tile64(SweepSmem64<TX, TY> &s, const GridD
         double c0[4], c1[4], c2[4], c3[4], f[4];
         if (q < NXF)
         {
-            int r = q / (TX + 1) + 1, fc = q - (r - 1) * (TX + 1);
+            int r, fc; // a warp reads one row of sU: columns 0..TX-1 first, the last column after
+            if (q < TX * TY)
+                r = q / TX + 1, fc = q - (r - 1) * TX;
+            else
+                r = q - TX * TY + 1, fc = TX;
 #pragma unroll
             for (int k = 0; k < 4; k++)
             {
