@@ -87,31 +87,45 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) ccm_sweep_kernel(const CcmArgs
         s.sC[2] = (T)0.5 * s.sC[0];
         s.sC[3] = (T)0.5 * s.sC[1];
     }
-    for (int q = tid; q < 4 * WX * WY; q += NT)
+    // stage the tile, its halo and their cell types: one index computation per cell
+    for (int q = tid; q < WX * WY; q += NT)
     {
-        const int k = q / (WX * WY);
-        const int r = q - k * (WX * WY);
-        const int ly = r / WX, lx = r - ly * WX;
+        const int ly = q / WX, lx = q - ly * WX;
         const int gi = i0 - 2 + lx, gj = j0 - 2 + ly;
-        const bool in = gi < g.M && gj < g.N;
-        const long long o = (long long)gj * pitch + gi;
-        s.sU[k][ly][lx] = in ? U[k * P + o] : (T)0;
-        if (k == 0)
-            s.sT[ly][lx] = in ? a.type[o] : (uint8_t)CELL_SOLID;
+        T v[4] = {(T)0, (T)0, (T)0, (T)0};
+        uint8_t t = (uint8_t)CELL_SOLID;
+        if (gi < g.M && gj < g.N)
+        {
+            const long long o = (long long)gj * pitch + gi;
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                v[k] = U[k * P + o];
+            t = a.type[o];
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            s.sU[k][ly][lx] = v[k];
+        s.sT[ly][lx] = t;
     }
     __syncthreads();
 
     GasConst<T> K = (PREC == 2) ? GasConst<T>(g.gf, g.gm1f, g.c1f, g.c2f, g.igm1f, g.ig2f)
                                 : GasConst<T>(g.gamma, g.gm1, g.c1, g.c2, g.igm1, g.ig2);
     const T hx2 = s.sC[2], hy2 = s.sC[3];
-    constexpr int NXF = (TX + 1) * (TY + 1);
+    // X faces of the tile's rows (sF rows 1..TY; a warp reads one row of sU:
+    // columns 0..TX-1 first, the last column after) and all Y faces
+    constexpr int NXF = (TX + 1) * TY;
     constexpr int NYF = TX * (TY + 1);
     for (int q = tid; q < NXF + NYF; q += NT)
     {
         T c0[4], c1[4], c2[4], c3[4], f[4];
         if (q < NXF)
         {
-            const int r = q / (TX + 1), fc = q - r * (TX + 1);
+            int r, fc;
+            if (q < TX * TY)
+                r = q / TX + 1, fc = q - (r - 1) * TX;
+            else
+                r = q - TX * TY + 1, fc = TX;
 #pragma unroll
             for (int k = 0; k < 4; k++)
             {
