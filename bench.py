@@ -54,9 +54,12 @@ def profile_run(args):
     run `--steps` steps, print ms/step.  No CPU leg, no extra legs."""
     import torch
     from ibtfo_gb300 import cases
-    w = cases.vortex_periodic(args.size) if args.workload == "vortex" else cases.inclined_channel(args.size,
-                                                                                                  args.size // 2)
-    inputs = vortex_inputs if args.workload == "vortex" else channel_inputs
+    if args.workload == "vortex":
+        w, inputs = cases.vortex_periodic(args.size), vortex_inputs
+    elif args.workload == "obstacles":
+        w, inputs = cases.shock_obstacles(args.size, args.size // 2), obstacle_inputs
+    else:
+        w, inputs = cases.inclined_channel(args.size, args.size // 2), channel_inputs
     r = gpu_arm(args, 0, 1, 0, precision=args.precision, e2e=False, w=w, inputs=inputs, steps=args.steps)
     print(json.dumps({"workload": w.name, "precision": args.precision, "steps": args.steps,
                       "ms_per_step": r["step_ms"] / args.steps, "sweep_ms": r["sweep_ms"] / args.steps,
@@ -194,6 +197,14 @@ def vortex_inputs(w, case):
     phi, u0 = cases.isentropic_vortex(w.grid)
     case.setup_geometry(phi)
     case.set_state(u0)
+
+
+def obstacle_inputs(w, case):
+    import ibtfo_gb300 as ib
+    from ibtfo_gb300 import cases
+    case.setup_bodies(obstacle_bodies(ib, cases.random_obstacles()))
+    case.init_x_split(0.5, cases.post_shock(3.0), (1.0, 0.0, 0.0, 1.0))
+    case.release_geometry()
 
 
 def vortex_errors(w, rhos):
@@ -468,7 +479,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--profile-workload", dest="workload", choices=("channel", "vortex"), default=None,
+    ap.add_argument("--profile-workload", dest="workload", choices=("channel", "vortex", "obstacles"), default=None,
                     help="only step this workload (profiler captures)")
     ap.add_argument("--size", type=int, default=4096, help="grid size for --profile-workload")
     ap.add_argument("--precision", default=PRECISION, choices=("fp64", "fp64_fast", "fp32c"))

@@ -5,6 +5,7 @@
 // and the boundary pass.  Because dt and the loop condition live on the
 // device, ibtfo_advance queues any number of steps without a host round trip;
 // chunks of steps are captured once into a CUDA graph and replayed.
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -188,7 +189,9 @@ static void make_bands(ibtfo_case *c, const std::vector<unsigned> &tiles)
     size_t t = 0;
     for (int k = 1; k <= NBANDS; k++)
     {
-        const int tb = (int)((long long)k * nty / NBANDS);
+        // the first and the last band half as tall as the others: the
+        // pipeline waits for the first chunk alone and drains the last one alone
+        const int tb = (k == NBANDS) ? nty : (int)((long long)(2 * k - 1) * nty / (2 * NBANDS - 2));
         c->band_rows[k] = (k == NBANDS) ? g.N : std::min(g.N, g.ng + tb * TILE_Y + 2);
         c->out_rows[k] = (k == NBANDS) ? g.N : std::min(g.N, g.ng + tb * TILE_Y);
         while (t < tiles.size() && (int)(tiles[t] >> 16) < tb)
@@ -209,6 +212,7 @@ static void make_post_cells(ibtfo_case *c, const std::vector<GhostRec> &gl)
         for (int i = 0; i < g.M; i++)
             if (i < g.ng || i >= g.n_x + g.ng || j < g.ng || j >= g.n_y + g.ng)
                 c->post_idx.push_back((long long)g.M * j + i);
+    std::sort(c->post_idx.begin(), c->post_idx.end()); // the host writes them in address order
 }
 
 // Case buffers come from the device's stream-ordered pool; freed memory stays
