@@ -453,6 +453,120 @@ __device__ __forceinline__ void sw_y(const double UD[4], const double UU[4], dou
 
 #undef IBTFO_SW_LAM
 
+// ---------------------------------------------------------------- PVRS stray store
+//
+// In the reference's PVRS Y solver the branch at PVRS/Riemann_solver.cpp:547-550
+// stores the energy flux (E_U + p_U) v_U of cell c at U_TMP[c*4 + 3]: the
+// state's indexing applied to the 28-double scratch records, i.e. component 3
+// of scratch slot c mod 7 of cell c/7.  With the serial row-major loop the
+// target cell is already solved; for c mod 7 == 2 the store replaces the
+// energy component of that cell's Y-face flux (slot 2), which the Y update
+// then uses.  The sweep reproduces this in pull form: the Y face of cell c'
+// recomputes the solve of its only possible source, cell 7 c' + 2.
+//
+// That solve reads the face states the reference's scratch slots hold at
+// that point (MUSCL_Scheme.cpp / MHM_Scheme.cpp / Godunov_Scheme.cpp loop
+// ranges, with the harness's zero-initialised scratch): slot 5 (U_D) is the
+// Y reconstruction for rows [ng-1, N-1), else the X stage's U_L (columns
+// [il0, M-1), il0 = ng-1 for MHM and 1 otherwise; MHM-predicted), else 0;
+// slot 6 (U_U) the Y reconstruction for rows [0, N-2), else the X stage's
+// U_R (columns [0, M-2)), else 0; MHM then predicts each slot in its row
+// range from the fluxes of both.  Returns whether the branch fires at (i, j)
+// and the value it stores.
+template <int SCH, int LIM>
+__device__ bool pvrs_stray_source(const double *__restrict__ U, long long P, int pitch, int M, int N, int ng,
+                                  double g, double dt, double dx, double dy, int i, int j, double *value)
+{
+    auto cell = [&](int ii, int jj, double v[4]) {
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            v[k] = U[k * P + (long long)jj * pitch + ii];
+    };
+    const int il0 = (SCH == MHM) ? ng - 1 : 1;
+    const bool x5 = i >= il0 && i < M - 1, x6 = i < M - 2;
+    const bool y5 = j >= ng - 1 && j < N - 1, y6 = j < N - 2;
+    double s5[4] = {0.0, 0.0, 0.0, 0.0}, s6[4] = {0.0, 0.0, 0.0, 0.0};
+    if (!y5 || !y6)
+    {
+        // the X stage's U_L and U_R at (i, j): MUSCL_Scheme.cpp:30-60 / MHM_Scheme.cpp:28-96
+        double a[4], b[4], c[4], d[4];
+        if (x5 || x6)
+            cell(i, j, b);
+        if (x5)
+        {
+            cell(i - 1, j, a);
+            cell(i + 1, j, c);
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                s5[k] = (SCH == GODUNOV) ? b[k] : b[k] + half_slope<LIM>(b[k], a[k], c[k], b[k]);
+        }
+        if (x6)
+        {
+            cell(i + 1, j, c);
+            cell(i + 2, j, d);
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                s6[k] = (SCH == GODUNOV) ? c[k] : c[k] - half_slope<LIM>(d[k], c[k], c[k], b[k]);
+        }
+        if (SCH == MHM)
+        {
+            double FL[4], FR[4];
+            flux_x(s5, g, FL);
+            flux_x(s6, g, FR);
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+            {
+                double dd = 0.5 * (FL[k] - FR[k]) * dt / dx;
+                if (x5)
+                    s5[k] = s5[k] + dd;
+                if (x6)
+                    s6[k] = s6[k] + dd;
+            }
+        }
+    }
+    if (y5 || y6)
+    {
+        // the Y stage: MUSCL_Scheme.cpp:91-121 / MHM_Scheme.cpp:98-183
+        double a[4], b[4], c[4], d[4];
+        cell(i, j, b);
+        cell(i, j + 1, c);
+        if (y5)
+        {
+            cell(i, j - 1, a);
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                s5[k] = (SCH == GODUNOV) ? b[k] : b[k] + half_slope<LIM>(b[k], a[k], c[k], b[k]);
+        }
+        if (y6)
+        {
+            cell(i, j + 2, d);
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                s6[k] = (SCH == GODUNOV) ? c[k] : c[k] - half_slope<LIM>(d[k], c[k], c[k], b[k]);
+        }
+    }
+    if (SCH == MHM)
+    {
+        double FL[4], FR[4];
+        flux_y(s5, g, FL);
+        flux_y(s6, g, FR);
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+        {
+            double dd = 0.5 * (FL[k] - FR[k]) * dt / dy;
+            if (y5)
+                s5[k] = s5[k] + dd;
+            if (y6)
+                s6[k] = s6[k] + dd;
+        }
+    }
+    double G[4], stray = 0.0;
+    if (!(pvrs_y(s5, s6, g, G, &stray) & 8))
+        return false;
+    *value = stray;
+    return true;
+}
+
 // One X face: states from four cells, MHM predictor, Riemann solver.
 template <int SCH, int RIE, int LIM>
 __device__ __forceinline__ void x_face(const double c0[4], const double c1[4], const double c2[4], const double c3[4],

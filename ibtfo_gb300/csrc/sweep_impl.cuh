@@ -334,6 +334,21 @@ __device__ __forceinline__ void sweep_tile64(SweepSmem64<TX, TY> &s, const GridD
             double stray = 0.0;
             int keep = FASTPHYS ? y_face_fast<double, SCH, RIE, LIM>(c0, c1, c2, c3, K, hy2, f, &stray)
                                 : y_face<SCH, RIE, LIM>(c0, c1, c2, c3, gam, dt, g.dy, f, &stray);
+            if constexpr (RIE == PVRS)
+            {
+                // the reference's PVRS stray store from cell 7 c' + 2 into this face's
+                // energy flux (physics.cuh, pvrs_stray_source)
+                const long long lin = (long long)g.M * (j0 - 1 + r) + (i0 + c);
+                const long long src = 7 * lin + 2;
+                double sv;
+                if (i0 + c < g.M && src < (long long)g.M * g.N &&
+                    pvrs_stray_source<SCH, LIM>(U, P, pitch, g.M, g.N, g.ng, gam, dt, g.dx, g.dy,
+                                                (int)(src % g.M), (int)(src / g.M), &sv))
+                {
+                    f[3] = sv;
+                    keep &= ~8;
+                }
+            }
 #pragma unroll
             for (int k = 0; k < 4; k++)
                 s.sG[k][r][c] = f[k];

@@ -79,8 +79,8 @@ def run_steps(case, n):
 
 
 # fixtures where the PVRS Y-solver branch at PVRS/Riemann_solver.cpp:547-550
-# fires: its stray store lands in another cell's flux slot, which the GPU path
-# does not reproduce (the local effect of the branch is reproduced)
+# fires: its stray store lands in another cell's flux slot; the sweep
+# reproduces it (physics.cuh, pvrs_stray_source)
 PVRS_STRAY = {"quaddown_MUSCL_PVRS_minmod", "quaddown_MHM_PVRS_minmod"}
 
 
@@ -89,8 +89,6 @@ PVRS_STRAY = {"quaddown_MUSCL_PVRS_minmod", "quaddown_MHM_PVRS_minmod"}
 def test_gpu_matches_reference_fixture(name, precision):
     fx = load(name)
     cfg = fx["config"]
-    if name in PVRS_STRAY:
-        pytest.xfail("PVRS :547-550 stray store into a remote flux slot is not reproduced")
     if precision == "fp64_fast" and not np.isfinite(fx["u_old"]).all():
         pytest.skip("reference output holds NaN/inf: where NaN first appears depends on last-bit rounding")
     with make_case(cfg, precision) as c:
