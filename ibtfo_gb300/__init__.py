@@ -147,6 +147,7 @@ SIGNATURES = {
     "ibtfo_get_state": (C.c_int, [_P, _DP, _DP]),
     "ibtfo_put_state": (C.c_int, [_P, _DP]),
     "ibtfo_step_host": (C.c_int, [_P, _DP, _DP, C.POINTER(Progress)]),
+    "ibtfo_step_host_bytes": (C.c_int, [_P, C.c_int, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
     "ibtfo_advance": (C.c_int, [_P, C.c_int]),
     "ibtfo_enqueue_sweep": (C.c_int, [_P]),
     "ibtfo_enqueue_boundary": (C.c_int, [_P]),
@@ -367,6 +368,12 @@ class Case:
         _check(lib().ibtfo_step_host(self.h, C.cast(C.c_void_p(in_ptr), _DP), C.cast(C.c_void_p(out_ptr), _DP),
                                      C.byref(p)))
         return p.as_dict()
+
+    def step_host_bytes(self, in_place=True):
+        """(host-to-device, device-to-host) bytes of one step_host_ptr call."""
+        a, b = C.c_longlong(), C.c_longlong()
+        _check(lib().ibtfo_step_host_bytes(self.h, 1 if in_place else 0, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     # ---------------------------------------------------------- stepping
     def set_stream(self, stream_ptr: int | None):

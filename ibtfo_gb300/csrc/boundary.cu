@@ -454,13 +454,15 @@ void launch_aos_to_cur_rows(const double *aos, double *b0, double *b1, const Dev
 
 __global__ void snapshot_rows_to_aos_kernel(const double *b0, const double *b1, const DevState *__restrict__ st,
                                             const uint8_t *__restrict__ type, double *__restrict__ aos, GridDesc g,
-                                            int r0, int r1)
+                                            int r0, int r1, int c0, int c1)
 {
-    long long c = (long long)r0 * g.M + (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= (long long)r1 * g.M)
+    const int w = c1 - c0;
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= (long long)(r1 - r0) * w)
         return;
     const int cur = st->step_cur;
-    int j = (int)(c / g.M), i = (int)(c - (long long)j * g.M);
+    int j = r0 + (int)(q / w), i = c0 + (int)(q % w);
+    long long c = (long long)j * g.M + i;
     long long o = (long long)j * g.pitch + i;
     const double *src = (type[o] == CELL_FLUID) ? (cur ? b0 : b1) : (cur ? b1 : b0);
     for (int k = 0; k < 4; k++)
@@ -468,12 +470,50 @@ __global__ void snapshot_rows_to_aos_kernel(const double *b0, const double *b1, 
 }
 
 void launch_snapshot_to_aos_rows(const double *b0, const double *b1, const DevState *st, const uint8_t *type,
-                                 double *aos, const GridDesc &g, int r0, int r1, cudaStream_t s)
+                                 double *aos, const GridDesc &g, int r0, int r1, int c0, int c1, cudaStream_t s)
 {
-    long long n = (long long)(r1 - r0) * g.M;
-    if (n <= 0)
+    long long n = (long long)(r1 - r0) * (c1 - c0);
+    if (r1 <= r0 || c1 <= c0)
         return;
-    snapshot_rows_to_aos_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(b0, b1, st, type, aos, g, r0, r1);
+    snapshot_rows_to_aos_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(b0, b1, st, type, aos, g, r0, r1, c0,
+                                                                           c1);
+    count_launch();
+}
+
+// the domain ring (rows below and above the interior, then the columns left
+// and right of it) from the current buffer into the host-layout array
+__global__ void ring_to_aos_kernel(const double *b0, const double *b1, const DevState *__restrict__ st,
+                                   double *__restrict__ aos, GridDesc g)
+{
+    const long long nrow = 2LL * g.ng * g.M, ncol = 2LL * g.ng * g.n_y;
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nrow + ncol)
+        return;
+    int i, j;
+    if (q < nrow)
+    {
+        const int r = (int)(q / g.M);
+        i = (int)(q - (long long)r * g.M);
+        j = (r < g.ng) ? r : g.n_y + r;
+    }
+    else
+    {
+        const long long qq = q - nrow;
+        const int r = (int)(qq / (2 * g.ng)), s = (int)(qq - (long long)r * 2 * g.ng);
+        j = g.ng + r;
+        i = (s < g.ng) ? s : g.n_x + s;
+    }
+    const double *src = st->cur ? b1 : b0;
+    const long long o = (long long)j * g.pitch + i, c = (long long)j * g.M + i;
+    for (int k = 0; k < 4; k++)
+        aos[c * 4 + k] = state_ld(src, k, o, g);
+}
+
+void launch_ring_to_aos(const double *b0, const double *b1, const DevState *st, double *aos, const GridDesc &g,
+                        cudaStream_t s)
+{
+    const long long n = 2LL * g.ng * g.M + 2LL * g.ng * g.n_y;
+    ring_to_aos_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(b0, b1, st, aos, g);
     count_launch();
 }
 

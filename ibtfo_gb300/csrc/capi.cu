@@ -142,7 +142,8 @@ struct ibtfo_case
     std::vector<int> band_rows;   // NBANDS + 1 array-row offsets of the host-to-device chunks
     std::vector<int> out_rows;    // NBANDS + 1 array-row offsets of the device-to-host chunks
     std::vector<int> band_tiles;  // NBANDS + 1 offsets into the active-tile list
-    std::vector<long long> post_idx; // cells the boundary pass writes (ghost cells, then the domain ring)
+    std::vector<int> fluid_cols;  // 2 NBANDS: columns [c0, c1) holding the fluid cells of each band
+    std::vector<long long> post_idx; // ghost cells (the boundary pass writes them and the domain ring)
     long long *d_post_idx = nullptr;
     double *d_post = nullptr, *h_post = nullptr; // their values after the step (device, pinned host)
     cudaStream_t h2d = nullptr, d2h = nullptr, sw[2] = {nullptr, nullptr};
@@ -177,8 +178,6 @@ static void drop_graphs(ibtfo_case *c)
 // array row that band's stencil reads (two rows above its tiles), so band k
 // can start once chunks 0..k are on the device.
 static const int NBANDS = 8;
-// bench.py counts this many device-to-host bytes for each progress read
-static_assert(sizeof(DevState) == 112, "DevState size changed: update the byte count of a progress read");
 static void make_bands(ibtfo_case *c, const std::vector<unsigned> &tiles)
 {
     const GridDesc &g = c->g;
@@ -186,6 +185,7 @@ static void make_bands(ibtfo_case *c, const std::vector<unsigned> &tiles)
     c->band_rows.assign(NBANDS + 1, 0);
     c->out_rows.assign(NBANDS + 1, 0);
     c->band_tiles.assign(NBANDS + 1, 0);
+    c->fluid_cols.assign(2 * NBANDS, 0);
     size_t t = 0;
     for (int k = 1; k <= NBANDS; k++)
     {
@@ -198,21 +198,50 @@ static void make_bands(ibtfo_case *c, const std::vector<unsigned> &tiles)
             t++;
         c->band_tiles[k] = (k == NBANDS) ? (int)tiles.size() : (int)t;
     }
+    // the columns of each band's active tiles (tiles without fluid cells are not listed)
+    for (int k = 0; k < NBANDS; k++)
+    {
+        int lo = g.M, hi = 0;
+        for (int q = c->band_tiles[k]; q < c->band_tiles[k + 1]; q++)
+        {
+            const int tx = (int)(tiles[q] & 0xFFFFu);
+            lo = std::min(lo, g.ng + tx * TILE_X);
+            hi = std::max(hi, std::min(g.ng + g.n_x, g.ng + (tx + 1) * TILE_X));
+        }
+        c->fluid_cols[2 * k] = lo < hi ? lo : 0;
+        c->fluid_cols[2 * k + 1] = lo < hi ? hi : 0;
+    }
 }
 
-// the cells a boundary pass writes: the ghost list, then every cell outside
-// the interior (the domain ring)
+// the interior cells a boundary pass writes: the ghost list (the domain
+// ring, the rest of what it writes, goes back by strided copies)
 static void make_post_cells(ibtfo_case *c, const std::vector<GhostRec> &gl)
 {
     const GridDesc &g = c->g;
     c->post_idx.clear();
     for (const GhostRec &r : gl)
         c->post_idx.push_back((long long)g.M * r.j + r.i);
-    for (int j = 0; j < g.N; j++)
-        for (int i = 0; i < g.M; i++)
-            if (i < g.ng || i >= g.n_x + g.ng || j < g.ng || j >= g.n_y + g.ng)
-                c->post_idx.push_back((long long)g.M * j + i);
     std::sort(c->post_idx.begin(), c->post_idx.end()); // the host writes them in address order
+}
+
+// the domain ring of the current state into u_out: two runs of whole rows
+// and two strided runs of the side columns
+static ibtfo_status ring_to_host(ibtfo_case *c, double *u_out)
+{
+    const GridDesc &g = c->g;
+    const size_t row = sizeof(double) * 4 * (size_t)g.M, cell = sizeof(double) * 4;
+    launch_ring_to_aos(c->buf[0], c->buf[1], c->st, c->staging, g, c->stream);
+    CK(cudaEventRecord(c->ev_done, c->stream));
+    CK(cudaStreamWaitEvent(c->d2h, c->ev_done, 0));
+    const size_t top = (size_t)(g.ng + g.n_y) * g.M * 4, side = (size_t)g.ng * g.M * 4;
+    CK(cudaMemcpyAsync(u_out, c->staging, row * g.ng, cudaMemcpyDeviceToHost, c->d2h));
+    CK(cudaMemcpyAsync(u_out + top, c->staging + top, row * g.ng, cudaMemcpyDeviceToHost, c->d2h));
+    CK(cudaMemcpy2DAsync(u_out + side, row, c->staging + side, row, cell * g.ng, g.n_y, cudaMemcpyDeviceToHost,
+                         c->d2h));
+    const size_t right = side + (size_t)(g.ng + g.n_x) * 4;
+    CK(cudaMemcpy2DAsync(u_out + right, row, c->staging + right, row, cell * g.ng, g.n_y, cudaMemcpyDeviceToHost,
+                         c->d2h));
+    return IBTFO_OK;
 }
 
 // Case buffers come from the device's stream-ordered pool; freed memory stays
@@ -1336,11 +1365,16 @@ static ibtfo_status step_host_plain(ibtfo_case *c, const double *u_in, double *u
 // compute.  After the last band the boundary pass writes the ghost cells and
 // the domain ring; those cells alone are gathered, copied and scattered
 // into u_out on the host.  Every copy of u_in lands before any write to
-// u_out, so u_out may be u_in.
+// u_out, so u_out may be u_in.  In place (u_out == u_in) the host array
+// already holds every cell the step leaves alone (solid cells are never
+// written; ghost cells and the domain ring come with the boundary-pass
+// cells), so each band copies back only the interior rows of the columns
+// its fluid cells occupy.
 static ibtfo_status step_host_banded(ibtfo_case *c, const double *u_in, double *u_out)
 {
     const GridDesc &g = c->g;
     const size_t row = sizeof(double) * 4 * (size_t)g.M;
+    const bool inplace = (u_out == u_in);
     for (int k = 0; k < NBANDS; k++)
     {
         const int r0 = c->band_rows[k], r1 = c->band_rows[k + 1];
@@ -1366,13 +1400,21 @@ static ibtfo_status step_host_banded(ibtfo_case *c, const double *u_in, double *
             c->sweep(a, dim3(t1 - t0), dim3(TILE_X * TILE_Y), s);
             count_launch();
         }
-        const int o0 = c->out_rows[k], o1 = c->out_rows[k + 1];
-        launch_snapshot_to_aos_rows(c->buf[0], c->buf[1], c->st, c->type, c->staging, g, o0, o1, s);
+        int o0 = c->out_rows[k], o1 = c->out_rows[k + 1], x0 = 0, x1 = g.M;
+        if (inplace)
+        {
+            o0 = std::max(o0, g.ng);
+            o1 = std::min(o1, g.ng + g.n_y);
+            x0 = c->fluid_cols[2 * k];
+            x1 = c->fluid_cols[2 * k + 1];
+        }
+        launch_snapshot_to_aos_rows(c->buf[0], c->buf[1], c->st, c->type, c->staging, g, o0, o1, x0, x1, s);
         CK(cudaEventRecord(c->ev_out[k], s));
         CK(cudaStreamWaitEvent(c->d2h, c->ev_out[k], 0));
-        if (o1 > o0)
-            CK(cudaMemcpyAsync(u_out + (size_t)o0 * 4 * g.M, c->staging + (size_t)o0 * 4 * g.M, row * (o1 - o0),
-                               cudaMemcpyDeviceToHost, c->d2h));
+        if (o1 > o0 && x1 > x0)
+            CK(cudaMemcpy2DAsync(u_out + ((size_t)o0 * g.M + x0) * 4, row, c->staging + ((size_t)o0 * g.M + x0) * 4,
+                                 row, sizeof(double) * 4 * (size_t)(x1 - x0), (size_t)(o1 - o0),
+                                 cudaMemcpyDeviceToHost, c->d2h));
     }
     for (int q = 0; q < 2; q++)
     {
@@ -1382,12 +1424,43 @@ static ibtfo_status step_host_banded(ibtfo_case *c, const double *u_in, double *
     enqueue_boundary(c);
     const int n = (int)c->post_idx.size();
     launch_gather_cells(c->buf[0], c->buf[1], c->st, c->d_post_idx, n, c->d_post, g, c->stream);
-    CK(cudaEventRecord(c->ev_done, c->stream));
-    CK(cudaStreamWaitEvent(c->d2h, c->ev_done, 0));
+    ibtfo_status rs = ring_to_host(c, u_out); // records ev_done behind the gather
+    if (rs != IBTFO_OK)
+        return rs;
     if (n)
         CK(cudaMemcpyAsync(c->h_post, c->d_post, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, c->d2h));
     CK(cudaEventRecord(c->ev_done, c->d2h));
     CK(cudaStreamWaitEvent(c->stream, c->ev_done, 0));
+    return IBTFO_OK;
+}
+
+ibtfo_status ibtfo_step_host_bytes(const ibtfo_case *c, int in_place, long long *h2d, long long *d2h)
+{
+    if (!c || !h2d || !d2h)
+        return fail(IBTFO_EINVAL, "null argument");
+    if (!c->geometry)
+        return fail(IBTFO_ESTATE, "ibtfo_setup_geometry has not run");
+    const GridDesc &g = c->g;
+    const long long cell = sizeof(double) * 4;
+    *h2d = cell * g.M * g.N;
+    const bool banded = !c->ccm && c->cfg.time_advance == IBTFO_TIME_SINGLESTEP;
+    long long out = cell * g.M * g.N;
+    if (banded)
+    {
+        out = cell * ((long long)c->post_idx.size() + 2LL * g.ng * g.M + 2LL * g.ng * g.n_y);
+        for (int k = 0; k < NBANDS; k++)
+        {
+            if (!in_place)
+            {
+                out += cell * (long long)(c->out_rows[k + 1] - c->out_rows[k]) * g.M;
+                continue;
+            }
+            const int o0 = std::max(c->out_rows[k], g.ng), o1 = std::min(c->out_rows[k + 1], g.ng + g.n_y);
+            if (o1 > o0)
+                out += cell * (long long)(o1 - o0) * (c->fluid_cols[2 * k + 1] - c->fluid_cols[2 * k]);
+        }
+    }
+    *d2h = out + (long long)sizeof(DevState); // the loop state read for the progress
     return IBTFO_OK;
 }
 

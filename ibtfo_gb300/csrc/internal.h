@@ -212,11 +212,15 @@ void launch_aos_to_cur_rows(const double *aos, double *b0, double *b1, const Dev
                             int r1, cudaStream_t s);
 void launch_cur_to_aos_rows(const double *b0, const double *b1, const DevState *st, double *aos, const GridDesc &g,
                             int r0, int r1, cudaStream_t s);
-// rows [r0, r1) of a step in flight (before its boundary pass): fluid cells
-// from the step's output buffer, the rest from its input (st->step_cur)
+// rows [r0, r1), columns [c0, c1) of a step in flight (before its boundary
+// pass): fluid cells from the step's output buffer, the rest from its input
+// (st->step_cur)
 void launch_snapshot_to_aos_rows(const double *b0, const double *b1, const DevState *st, const uint8_t *type,
-                                 double *aos, const GridDesc &g, int r0, int r1, cudaStream_t s);
-// the cells a boundary pass writes (linear indices M*j + i), gathered from the
+                                 double *aos, const GridDesc &g, int r0, int r1, int c0, int c1, cudaStream_t s);
+// the domain ring of the current buffer into the host-layout array
+void launch_ring_to_aos(const double *b0, const double *b1, const DevState *st, double *aos, const GridDesc &g,
+                        cudaStream_t s);
+// cells given by linear indices M*j + i (the ghost list), gathered from the
 // current buffer into out[q*4 + k]
 void launch_gather_cells(const double *b0, const double *b1, const DevState *st, const long long *idx, int n,
                          double *out, const GridDesc &g, cudaStream_t s);

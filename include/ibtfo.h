@@ -206,6 +206,10 @@ ibtfo_status ibtfo_put_state(ibtfo_case *c, const double *u_old);
  * the sweep start once their stencil is on the device): from page-locked
  * host memory the copies run concurrently with the kernels. */
 ibtfo_status ibtfo_step_host(ibtfo_case *c, const double *u_in, double *u_out, ibtfo_progress *p);
+/* Bytes one ibtfo_step_host call moves each way.  In place (u_out == u_in)
+ * only the cells a step can change go back: the interior rows of the
+ * columns holding fluid cells, plus the ghost cells and the domain ring. */
+ibtfo_status ibtfo_step_host_bytes(const ibtfo_case *c, int in_place, long long *h2d, long long *d2h);
 
 /* Queues `nsteps` iterations of the reference loop body (Sod.cpp:154-177:
  * TimeAdvance, Boundary, Global_Boundary, ComputeDt, CaculateMass,
