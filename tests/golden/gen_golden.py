@@ -144,6 +144,15 @@ def fixtures():
                    base("refincline", 48, 48, (0, 0), (1, 1), 0.3, 0.3, "MUSCL", "HLL", "minmod", b, "refincline",
                         plugin_params={"angle": 30.0, "AxisD": 0.4, "rho_L": 1, "u_L": 0, "v_L": 0, "p_L": 1,
                                        "rho_R": 0.125, "u_R": 0, "v_R": 0, "p_R": 0.1}), 10))
+    # VanLeer beyond MUSCL + HLL, and more scheme x solver x ghost-fluid pairings
+    # (the reference's VanLeer macro turns these to NaN within a few steps: 2 and 3 steps keep most values finite)
+    fx.append(("quad_MHM_HLL_VanLeer", base("quadrants", 32, 24, (0, 0), (1, 0.75), 0.3, 1.0, "MHM", "HLL", "VanLeer"), 2))
+    fx.append(("channel_MUSCL_HLL_VanLeer_IDWBaseGFM",
+               base("channel", 64, 32, (0, 0), (2, 1), 0.45, 0.2, "MUSCL", "HLL", "VanLeer", "IDWBaseGFM"), 3))
+    fx.append(("channel_Godunov_SW_minmod_HBCGFM",
+               base("channel", 64, 32, (0, 0), (2, 1), 0.45, 0.2, "Godunov", "StegerWarming", "minmod", "HBCGFM"), 10))
+    fx.append(("channel_MHM_PVRS_minmod_LinearBaseGFM",
+               base("channel", 64, 32, (0, 0), (2, 1), 0.3, 0.2, "MHM", "PVRS", "minmod", "LinearBaseGFM"), 10))
     # Scheme = Lax (Lax_Scheme.cpp): four-state problem, Sod tube to t_end, ghost-fluid channel
     fx.append(("quad_Lax", base("quadrants", 32, 24, (0, 0), (1, 0.75), 0.3, 1.0, "Lax"), 10))
     fx.append(("sodtube_Lax", base("sod_x", 80, 20, (0, 0), (1, 0.25), 0.5, 0.2, "Lax"), 1000))
