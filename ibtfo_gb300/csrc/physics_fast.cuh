@@ -196,10 +196,12 @@ __device__ __forceinline__ bool hll_fast(const T UL[4], const T UR[4], const Gas
     }
     else
     {
-        const T inv = rcp_t(S_R - S_L), srsl = S_R * S_L;
+        // (S_R F_L - S_L F_R + S_R S_L (U_R - U_L)) / (S_R - S_L) with the three weights formed once
+        const T inv = rcp_t(S_R - S_L);
+        const T wl = S_R * inv, wr = -S_L * inv, wu = wl * S_L;
 #pragma unroll
         for (int k = 0; k < 4; k++)
-            F[k] = (S_R * FL[k] - S_L * FR[k] + srsl * (UR[k] - UL[k])) * inv;
+            F[k] = fma_t(wl, FL[k], fma_t(wr, FR[k], wu * (UR[k] - UL[k])));
     }
     return true;
 }

@@ -202,6 +202,24 @@ __device__ __forceinline__ void block_reduce_finalize(CellStats cs, DevState *st
     block_commit_finalize<NT>(a, u, v, m, n, st, partial, g, step_accounting, set_start, nblocks, bid);
 }
 
+// max(m, x) for m >= 0 as fmax gives it (NaN and negative x leave m), with
+// the compare on the integer pipe: non-negative doubles order like their bits
+__device__ __forceinline__ double max_nonneg(double m, double x)
+{
+    const long long bm = __double_as_longlong(m), bx = __double_as_longlong(x);
+    return (bx > bm && bx <= 0x7ff0000000000000LL) ? x : m;
+}
+
+// any of four values NaN, tested on the integer pipe
+__device__ __forceinline__ int any_nan4(const double v[4])
+{
+    const long long inf = 0x7ff0000000000000LL, mask = 0x7fffffffffffffffLL;
+    return ((__double_as_longlong(v[0]) & mask) > inf || (__double_as_longlong(v[1]) & mask) > inf ||
+            (__double_as_longlong(v[2]) & mask) > inf || (__double_as_longlong(v[3]) & mask) > inf)
+               ? 1
+               : 0;
+}
+
 // CFL and mass contributions of one fluid cell of the new state
 // (ComputeDt.cpp:38-45, CaculateMass.cpp:36)
 __device__ __forceinline__ void cell_stats(const double v[4], double gam, double dx, double dy, CellStats &cs)
@@ -210,11 +228,11 @@ __device__ __forceinline__ void cell_stats(const double v[4], double gam, double
     double u = v[1] / v[0];
     double w = v[2] / v[0];
     double p = (gam - 1) * (v[3] - 0.5 * rho * (u * u + w * w));
-    cs.a2max = fmax(cs.a2max, gam * p / rho); // pow(gam p / rho, 0.5) taken once per block
-    cs.umax = fmax(cs.umax, fabs(u));
-    cs.vmax = fmax(cs.vmax, fabs(w));
+    cs.a2max = max_nonneg(cs.a2max, gam * p / rho); // pow(gam p / rho, 0.5) taken once per block
+    cs.umax = max_nonneg(cs.umax, fabs(u));
+    cs.vmax = max_nonneg(cs.vmax, fabs(w));
     cs.mass += v[0] * dx * dy;
-    cs.nans += (isnan(v[0]) || isnan(v[1]) || isnan(v[2]) || isnan(v[3])) ? 1 : 0;
+    cs.nans += any_nan4(v);
 }
 
 // the same statistics with a shared reciprocal (fp64_fast)
@@ -224,11 +242,11 @@ __device__ __forceinline__ void cell_stats_fast(const double v[4], const GasCons
     const double ir = rcp_t(v[0]);
     const double u = v[1] * ir, w = v[2] * ir;
     const double p = K.gm1 * fma(-0.5, fma(v[1], u, v[2] * w), v[3]);
-    cs.a2max = fmax(cs.a2max, K.g * ir * p);
-    cs.umax = fmax(cs.umax, fabs(u));
-    cs.vmax = fmax(cs.vmax, fabs(w));
+    cs.a2max = max_nonneg(cs.a2max, K.g * ir * p);
+    cs.umax = max_nonneg(cs.umax, fabs(u));
+    cs.vmax = max_nonneg(cs.vmax, fabs(w));
     cs.mass += v[0] * dxdy;
-    cs.nans += (isnan(v[0]) || isnan(v[1]) || isnan(v[2]) || isnan(v[3])) ? 1 : 0;
+    cs.nans += any_nan4(v);
 }
 
 // shared memory of one FP64 tile: the tile plus two halo cells each side,
