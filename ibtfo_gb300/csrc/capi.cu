@@ -355,9 +355,11 @@ ibtfo_status ibtfo_create(const ibtfo_config *cfg, ibtfo_case **out)
         k.boundary < 0 || k.boundary > 6 || k.global_boundary < 0 || k.global_boundary > 1 || k.precision < 0 ||
         k.precision > 2 || k.time_advance < 0 || k.time_advance > 1)
         return fail(IBTFO_EINVAL, "unknown scheme/riemann/limiter/boundary/global_boundary/precision/time key");
-    if ((k.scheme == IBTFO_SCHEME_LAX || k.time_advance == IBTFO_TIME_RK2) &&
+    if (k.scheme == IBTFO_SCHEME_LAX &&
         (k.precision == IBTFO_PRECISION_FP32_COMPENSATED || k.boundary == IBTFO_BOUNDARY_CCM))
-        return fail(IBTFO_EINVAL, "Scheme = Lax and Time = RK2 run in the FP64 precisions without cut cells");
+        return fail(IBTFO_EINVAL, "Scheme = Lax runs in the FP64 precisions without cut cells");
+    if (k.time_advance == IBTFO_TIME_RK2 && k.boundary == IBTFO_BOUNDARY_CCM)
+        return fail(IBTFO_EINVAL, "Time = RK2 runs without cut cells");
     if (k.precision == IBTFO_PRECISION_FP32_COMPENSATED && k.riemann == IBTFO_RIEMANN_PVRS)
         return fail(IBTFO_EINVAL, "PVRS is available in the FP64 precisions only");
     if (k.boundary == IBTFO_BOUNDARY_CCM && k.riemann == IBTFO_RIEMANN_PVRS)

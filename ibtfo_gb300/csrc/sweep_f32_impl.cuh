@@ -42,6 +42,18 @@ __device__ __forceinline__ void two_float_acc(float &h, float &l, float oh, floa
     l = l + ol + err;
 }
 
+// (h, l) = ((h, l) + (oh, ol)) / 2 for the second RK2 stage: TwoSum of the
+// hi parts, the halving is exact, then renormalisation
+__device__ __forceinline__ void two_float_average(float &h, float &l, float oh, float ol)
+{
+    two_float_acc(h, l, oh, ol);
+    h *= 0.5f;
+    l *= 0.5f;
+    const float s = h + l;
+    l = l - (s - h);
+    h = s;
+}
+
 // per-thread statistics in FP32; the mass as a compensated (hi, lo) pair
 struct CellStats32
 {
@@ -61,10 +73,13 @@ struct SweepSmem32
 
 // Advance the tile whose first interior cell is (i0, j0) from U into V (float
 // planes: 0-3 hi, 4-7 lo) and accumulate the statistics of the updated cells.
+// Time = RK2: stage 1 gathers no statistics; stage 2 stores the average of
+// the advanced state and the pair the output buffer holds (the state at the
+// start of the step).
 template <int SCH, int RIE, int LIM, int TX, int TY, int NT>
 __device__ __forceinline__ void sweep_tile32(SweepSmem32<TX, TY> &s, const GridDesc &g, const float *__restrict__ U,
                                              float *__restrict__ V, const uint8_t *__restrict__ type, int i0, int j0,
-                                             double dt, CellStats32 &cs)
+                                             double dt, CellStats32 &cs, int stage = 0)
 {
     constexpr int WX = TX + 4, WY = TY + 4;
     const long long P = g.plane;
@@ -199,12 +214,20 @@ __device__ __forceinline__ void sweep_tile32(SweepSmem32<TX, TY> &s, const GridD
                     lo[3] = 0.0f;
                 }
             }
+            if (stage == 2)
+            {
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    two_float_average(hi[k], lo[k], V[k * P + o], V[(4 + k) * P + o]);
+            }
 #pragma unroll
             for (int k = 0; k < 4; k++)
             {
                 V[k * P + o] = hi[k];
                 V[(4 + k) * P + o] = lo[k];
             }
+            if (stage == 1)
+                continue;
             // CFL statistics (ComputeDt.cpp:38-45) from the hi parts
             const float ir = rcp_t(hi[0]);
             const float u = hi[1] * ir, w = hi[2] * ir;
@@ -223,8 +246,15 @@ __device__ __forceinline__ void sweep_tile32(SweepSmem32<TX, TY> &s, const GridD
 // this part), then block_commit_finalize.
 template <int NT>
 __device__ __forceinline__ void block_reduce_finalize32(CellStats32 cs, DevState *st, double *partial,
-                                                        const GridDesc &g, unsigned nblocks, unsigned bid)
+                                                        const GridDesc &g, unsigned nblocks, unsigned bid,
+                                                        bool first_stage = false)
 {
+    if (first_stage)
+    {
+        __syncthreads(); // every thread of the block has stored its cells
+        block_commit_finalize<NT>(0, 0, 0, 0, 0, st, partial, g, false, false, nblocks, bid, true);
+        return;
+    }
     __shared__ float red[5][NT / 32];
     __shared__ int rnan[NT / 32];
 #pragma unroll
@@ -293,8 +323,8 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y, 6) sweep_f32_kernel(const Swee
     const int i0 = g.ng + (int)(tile & 0xFFFFu) * TILE_X;
     const int j0 = g.ng + (int)(tile >> 16) * TILE_Y;
     CellStats32 cs;
-    sweep_tile32<SCH, RIE, LIM, TILE_X, TILE_Y, NT>(s, g, U, V, a.type, i0, j0, dt, cs);
-    block_reduce_finalize32<NT>(cs, st, a.partial, g, a.nblocks ? a.nblocks : gridDim.x, bid);
+    sweep_tile32<SCH, RIE, LIM, TILE_X, TILE_Y, NT>(s, g, U, V, a.type, i0, j0, dt, cs, a.stage);
+    block_reduce_finalize32<NT>(cs, st, a.partial, g, a.nblocks ? a.nblocks : gridDim.x, bid, a.stage == 1);
 }
 
 template <int SCH, int RIE, int LIM>

@@ -44,8 +44,8 @@ enum { IBTFO_SCHEME_MUSCL = 0, IBTFO_SCHEME_MHM = 1, IBTFO_SCHEME_GODUNOV = 2, I
  * method, U1 = U0 + dt L(U0) with its Boundary and Global_Boundary passes,
  * then 0.5 (U0 + U1 + dt L(U1)) on fluid cells, both stages with the dt of
  * the step (the two-stage method Src/Base/TimeAdvance/RK2/RK2.cpp describes;
- * that file itself does not compile).  FP64 precisions, not with cut cells
- * or in batches. */
+ * that file itself does not compile); in the FP32 form the average is taken
+ * on the (hi, lo) pairs.  Not with cut cells or in batches. */
 enum { IBTFO_TIME_SINGLESTEP = 0, IBTFO_TIME_RK2 = 1 };
 /* HLLC is the reference's HLLC directory, whose solver is HLL (including the
  * Y-face slot reuse); HLLC_TORO is a contact-restoring HLLC with no
