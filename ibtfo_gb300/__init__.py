@@ -222,6 +222,7 @@ REF_SIGNATURES = {
     "ibtfo_ref_Global_Boundary": (None, [_I, _I, _I, _D, _DP, _DP, _I, _I]),
     "ibtfo_ref_ComputeDt": (None, [_D, _D, _I, _I, _I, _D, _D, _DP, _DP, _DP, _I, _I]),
     "ibtfo_ref_CaculateMass": (None, [_D, _D, _I, _I, _I, _DP, _DP, _DP, _I, _I]),
+    "ibtfo_ref_WriteData": (None, [_D, _D, _D, _D, _I, _I, _I, _I, _D, _D, _DP, _DP, _I, _I]),
     "ibtfo_ref_update_self": (None, [_DP]),
     "ibtfo_ref_update_device": (None, [_DP]),
     "ibtfo_ref_release": (None, [_DP]),

@@ -939,7 +939,13 @@ ibtfo_status ibtfo_case_bytes(const ibtfo_config *k, long long *resident, long l
 
 // ---------------------------------------------------------------- output
 
-ibtfo_status ibtfo_write_vtk(ibtfo_case *c, const char *path, int binary)
+// the VTK file of the current state; the TIME field is the state's loop time
+// unless `time` is given (the reference's WriteData takes it from its caller)
+static ibtfo_status write_vtk(ibtfo_case *c, const char *path, int binary, const double *time);
+
+ibtfo_status ibtfo_write_vtk(ibtfo_case *c, const char *path, int binary) { return write_vtk(c, path, binary, nullptr); }
+
+static ibtfo_status write_vtk(ibtfo_case *c, const char *path, int binary, const double *time)
 {
     if (!c || !path)
         return fail(IBTFO_EINVAL, "null argument");
@@ -958,7 +964,8 @@ ibtfo_status ibtfo_write_vtk(ibtfo_case *c, const char *path, int binary)
     cudaFreeAsync(d, c->stream);
     CK(cudaStreamSynchronize(c->stream));
     const ibtfo_config &k = c->cfg;
-    if (write_vtk_file(path, g, k.lo_x, k.lo_y, k.hi_x - k.lo_x, k.hi_y - k.lo_y, s.now_t, h.data(), binary))
+    if (write_vtk_file(path, g, k.lo_x, k.lo_y, k.hi_x - k.lo_x, k.hi_y - k.lo_y, time ? *time : s.now_t, h.data(),
+                       binary))
         return fail(IBTFO_EINVAL, std::string("cannot write ") + path);
     return IBTFO_OK;
 }
@@ -1644,6 +1651,7 @@ int case_batch_view(ibtfo_case *c, SweepArgs *sa, FillArgs *fa, int *scheme, int
 }
 
 cudaStream_t case_stream(const ibtfo_case *c) { return c->stream; }
+int case_write_vtk_at(ibtfo_case *c, const char *path, double now_t) { return write_vtk(c, path, 0, &now_t); }
 int case_time_advance(const ibtfo_case *c) { return c->cfg.time_advance; }
 int case_device(const ibtfo_case *c) { return c->device; }
 

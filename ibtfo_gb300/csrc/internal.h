@@ -330,6 +330,7 @@ int case_batch_view(ibtfo_case *c, SweepArgs *s, FillArgs *f, int *scheme, int *
                     int *precision, int *has_state);
 cudaStream_t case_stream(const ibtfo_case *c);
 int case_time_advance(const ibtfo_case *c);
+int case_write_vtk_at(ibtfo_case *c, const char *path, double now_t); // ASCII, TIME field = now_t
 int case_device(const ibtfo_case *c);
 double case_gamma(const ibtfo_case *c);
 void set_last_error(const char *msg);

@@ -5,6 +5,7 @@
 // mirror is a present table: the XYCOORD pointer of the first geometry call
 // names a case, its U_OLD pointer is bound at the first state call, and every
 // later call with those pointers works on the resident device state.
+#include <cstdio>
 #include <cstring>
 #include <iterator>
 #include <map>
@@ -336,6 +337,43 @@ void ibtfo_ref_CaculateMass(double Psy_L, double Psy_H, int N_x, int N_y, int nu
     if (set_status(ibtfo_get_progress(e->cs, &p)) != IBTFO_OK)
         return;
     MASS_DEVICE[device] = p.mass;
+}
+
+void ibtfo_ref_WriteData(double lo_x, double lo_y, double Psy_L, double Psy_H, int N_x, int N_y, int num_ghost_cell,
+                         int iter, double now_t, double gamma, double *U_OLD, double *XYCOORD, int ndevices,
+                         int device)
+{
+    std::lock_guard<std::mutex> lock(g_mu);
+    (void)lo_x;
+    (void)lo_y;
+    (void)Psy_L;
+    (void)Psy_H;
+    (void)N_x;
+    (void)N_y;
+    (void)num_ghost_cell;
+    if (!one_device(ndevices, device))
+        return;
+    Entry *e = by_xy(XYCOORD);
+    if (!e || !e->cs)
+    {
+        set_status(IBTFO_ESTATE, "WriteData before Level_Set");
+        return;
+    }
+    if (!e->state && bind_state(e, U_OLD, nullptr, gamma) != IBTFO_OK)
+        return;
+    // WriteData.cpp:20-27
+    FILE *visit = fopen("result.visit", "a");
+    if (!visit)
+    {
+        set_status(IBTFO_EINVAL, "cannot open result.visit");
+        return;
+    }
+    if (iter == 0 && device == 0)
+        fprintf(visit, "!NBLOCKS %d\n", ndevices);
+    const std::string name = "dat_" + std::to_string(device) + "_" + std::to_string(iter) + ".vtk";
+    fprintf(visit, "%s\n", name.c_str());
+    fclose(visit);
+    set_status(ibtfo::case_write_vtk_at(e->cs, name.c_str(), now_t));
 }
 
 void ibtfo_ref_update_self(double *U)

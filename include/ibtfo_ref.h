@@ -66,6 +66,14 @@ void ibtfo_ref_ComputeDt(double Psy_L, double Psy_H, int N_x, int N_y, int num_g
 void ibtfo_ref_CaculateMass(double Psy_L, double Psy_H, int N_x, int N_y, int num_ghost_cell, double *U_OLD,
                             double *XYCOORD, double *MASS_DEVICE, int ndevices, int device);
 
+/* Src/Utils/WriteData.H (WriteData.cpp:5-247): appends dat_<device>_<iter>.vtk
+ * to result.visit (with the "!NBLOCKS 1" line at iter 0) and writes that file
+ * in the reference's ASCII layout from the resident state; U_OLD is not
+ * copied back. */
+void ibtfo_ref_WriteData(double lo_x, double lo_y, double Psy_L, double Psy_H, int N_x, int N_y, int num_ghost_cell,
+                         int iter, double now_t, double gamma, double *U_OLD, double *XYCOORD, int ndevices,
+                         int device);
+
 /* `acc update self` / `acc update device` of a registered U_OLD or U_NEW */
 void ibtfo_ref_update_self(double *U);
 void ibtfo_ref_update_device(double *U);

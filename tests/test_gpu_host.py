@@ -35,8 +35,10 @@ def rel_linf(a, b):
 @pytest.mark.parametrize("name", ["refincline_MUSCL_HLL_minmod_IDWBaseGFM", "channel_MUSCL_HLLC_minmod_BCGFM",
                                   "channel_MUSCL_HLLC_minmod_LinearBaseGFM", "sodtube_MUSCL_HLL_minmod",
                                   "refsod_MUSCL_HLL_minmod"])
-def test_reference_driver_sequence_through_shim(name):
-    """Test/InclineSod/InclineSod.cpp:97-189 call by call through ibtfo_ref_*."""
+def test_reference_driver_sequence_through_shim(name, tmp_path, monkeypatch):
+    """Test/InclineSod/InclineSod.cpp:97-189 call by call through ibtfo_ref_*,
+    with WriteData before the loop and after it (Sod.cpp:139-141, :186)."""
+    monkeypatch.chdir(tmp_path)
     fx = load(name)
     c = fx["config"]
     L = ib.lib()
@@ -69,6 +71,8 @@ def test_reference_driver_sequence_through_shim(name):
     assert L.ibtfo_ref_status() == 0, L.ibtfo_last_error()
     dt = dt_buf[0]
     assert np.isclose(dt, fx["dts"][0], rtol=RTOL, atol=0)
+    L.ibtfo_ref_WriteData(c["lo_x"], c["lo_y"], PL, PH, nx, ny, ng, 0, 0.0, g, _p(U_OLD), _p(XY), 1, 0)
+    assert L.ibtfo_ref_status() == 0, L.ibtfo_last_error()
     now_t, it, dts, ms = 0.0, 0, [], []
     while now_t < c["Psy_time"] and it < fx["iters"]:
         L.ibtfo_ref_TimeAdvance(PL, PH, nx, ny, ng, g, dt, _p(U_OLD), _p(U_TMP), _p(U_NEW), _p(XY), _p(SCH), 1, 0)
@@ -91,6 +95,18 @@ def test_reference_driver_sequence_through_shim(name):
     assert np.array_equal(np.isfinite(U_OLD), np.isfinite(fx["u_old"]))
     assert rel_linf(U_OLD, fx["u_old"]) <= RTOL
     assert rel_linf(U_NEW, fx["u_new"]) <= RTOL
+    L.ibtfo_ref_WriteData(c["lo_x"], c["lo_y"], PL, PH, nx, ny, ng, it, now_t, g, _p(U_OLD), _p(XY), 1, 0)
+    assert L.ibtfo_ref_status() == 0, L.ibtfo_last_error()
+    assert (tmp_path / "result.visit").read_text().split() == ["!NBLOCKS", "1", "dat_0_0.vtk", f"dat_0_{it}.vtk"]
+    lines = (tmp_path / f"dat_0_{it}.vtk").read_text().split("\n")
+    assert abs(float(lines[10].split()[0]) - now_t) < 1e-6
+    k = lines.index("SCALARS density float  ") + 2
+    rho = np.array([float(x) for x in lines[k:k + nx * ny]])
+    u = U_OLD.reshape(N, M, 4)[ng:-ng, ng:-ng]
+    t = XY.reshape(N, M, 6)[ng:-ng, ng:-ng, 5]
+    want = np.where((t == 0) | (t == 3), np.maximum(u[..., 0], 1e-6), -1.0).reshape(-1)
+    fin = np.isfinite(want)
+    assert np.all(np.abs(rho[fin] - want[fin]) <= 5.1e-7 + 2e-7 * np.abs(want[fin]))
     L.ibtfo_ref_release(_p(XY))
 
 
