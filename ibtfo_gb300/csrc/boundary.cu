@@ -221,9 +221,15 @@ __device__ void fill_ring(const FillArgs &a, const View &v, double *dst, long lo
 __device__ __forceinline__ void fill_block(const FillArgs &a, int vb, int do_ghosts, int do_ring)
 {
     DevState *st = a.st;
-    if (!a.init_mode && !st->fill_pending)
-        return;
-    const int cur = st->cur;
+    int cur;
+    if (a.pre_flip)
+        cur = st->step_cur ^ 1; // the buffer the step in flight writes
+    else
+    {
+        if (!a.init_mode && !st->fill_pending)
+            return;
+        cur = st->cur;
+    }
     View v;
     v.next = cur ? a.buf1 : a.buf0;
     v.prev = cur ? a.buf0 : a.buf1;
@@ -235,10 +241,10 @@ __device__ __forceinline__ void fill_block(const FillArgs &a, int vb, int do_gho
     v.n_x = a.g.n_x;
     v.n_y = a.g.n_y;
     double *dst = cur ? a.buf1 : a.buf0;
-    const int gblocks = do_ghosts ? (a.nghost + 255) / 256 : 0;
+    const int gblocks = do_ghosts ? (a.nghost - a.ghost0 + 255) / 256 : 0;
     if (vb < gblocks)
     {
-        int t = vb * 256 + threadIdx.x;
+        int t = a.ghost0 + vb * 256 + threadIdx.x;
         if (t < a.nghost)
             fill_ghost(a, v, dst, a.ghosts[t]);
         return;
@@ -254,6 +260,20 @@ __device__ __forceinline__ void fill_block(const FillArgs &a, int vb, int do_gho
 __global__ void __launch_bounds__(256) fill_kernel(const FillArgs a)
 {
     fill_block(a, blockIdx.x, a.do_ghosts, a.do_ring);
+}
+
+void launch_fill_ghosts(const FillArgs &a, int g0, int g1, cudaStream_t s)
+{
+    if (g1 <= g0)
+        return;
+    FillArgs b = a;
+    b.pre_flip = 1;
+    b.ghost0 = g0;
+    b.nghost = g1; // records [ghost0, nghost)
+    b.do_ghosts = 1;
+    b.do_ring = 0;
+    fill_kernel<<<(g1 - g0 + 255) / 256, 256, 0, s>>>(b);
+    count_launch();
 }
 
 void launch_fill(const FillArgs &a, cudaStream_t s)
@@ -464,7 +484,9 @@ __global__ void snapshot_rows_to_aos_kernel(const double *b0, const double *b1, 
     int j = r0 + (int)(q / w), i = c0 + (int)(q % w);
     long long c = (long long)j * g.M + i;
     long long o = (long long)j * g.pitch + i;
-    const double *src = (type[o] == CELL_FLUID) ? (cur ? b0 : b1) : (cur ? b1 : b0);
+    const bool out = type[o] == CELL_FLUID ||
+                     (type[o] == CELL_GHOST && i >= g.ng && i < g.ng + g.n_x && j >= g.ng && j < g.ng + g.n_y);
+    const double *src = out ? (cur ? b0 : b1) : (cur ? b1 : b0);
     for (int k = 0; k < 4; k++)
         aos[c * 4 + k] = state_ld(src, k, o, g);
 }
@@ -517,28 +539,6 @@ void launch_ring_to_aos(const double *b0, const double *b1, const DevState *st, 
     count_launch();
 }
 
-__global__ void gather_cells_kernel(const double *b0, const double *b1, const DevState *__restrict__ st,
-                                    const long long *__restrict__ idx, int n, double *__restrict__ out, GridDesc g)
-{
-    int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= n)
-        return;
-    const double *src = st->cur ? b1 : b0;
-    long long c = idx[q];
-    int j = (int)(c / g.M), i = (int)(c - (long long)j * g.M);
-    long long o = (long long)j * g.pitch + i;
-    for (int k = 0; k < 4; k++)
-        out[(long long)q * 4 + k] = state_ld(src, k, o, g);
-}
-
-void launch_gather_cells(const double *b0, const double *b1, const DevState *st, const long long *idx, int n,
-                         double *out, const GridDesc &g, cudaStream_t s)
-{
-    if (n <= 0)
-        return;
-    gather_cells_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(b0, b1, st, idx, n, out, g);
-    count_launch();
-}
 
 void launch_cur_to_aos_rows(const double *b0, const double *b1, const DevState *st, double *aos, const GridDesc &g,
                             int r0, int r1, cudaStream_t s)

@@ -143,11 +143,11 @@ struct ibtfo_case
     std::vector<int> out_rows;    // NBANDS + 1 array-row offsets of the device-to-host chunks
     std::vector<int> band_tiles;  // NBANDS + 1 offsets into the active-tile list
     std::vector<int> fluid_cols;  // 2 NBANDS: columns [c0, c1) holding the fluid cells of each band
-    std::vector<long long> post_idx; // ghost cells (the boundary pass writes them and the domain ring)
-    long long *d_post_idx = nullptr;
-    double *d_post = nullptr, *h_post = nullptr; // their values after the step (device, pinned host)
-    cudaStream_t h2d = nullptr, d2h = nullptr, sw[2] = {nullptr, nullptr};
-    cudaEvent_t ev_in[8] = {}, ev_conv[8] = {}, ev_out[8] = {}, ev_sw[2] = {}, ev_done = nullptr;
+    std::vector<int> band_ghosts; // NBANDS + 1 offsets into the ghost list (rows of each band)
+    std::vector<int> ghost_ready; // NBANDS: the last band whose fluid cells the band's ghost fills read
+    cudaStream_t h2d = nullptr, d2h = nullptr, sw[2] = {nullptr, nullptr}, fin = nullptr;
+    cudaEvent_t ev_in[8] = {}, ev_conv[8] = {}, ev_out[8] = {}, ev_swept[8] = {}, ev_sw[2] = {}, ev_fin = nullptr,
+                ev_done = nullptr;
     // the banded step captured as a CUDA graph for one pair of page-locked host arrays
     cudaGraphExec_t host_graph = nullptr;
     const double *host_graph_in = nullptr;
@@ -213,15 +213,42 @@ static void make_bands(ibtfo_case *c, const std::vector<unsigned> &tiles)
     }
 }
 
-// the interior cells a boundary pass writes: the ghost list (the domain
-// ring, the rest of what it writes, goes back by strided copies)
-static void make_post_cells(ibtfo_case *c, const std::vector<GhostRec> &gl)
+// Ghost records by band: the records of each band's rows (the list is in
+// row order), the last band whose fluid cells their fills read (the image
+// and extra points' bracket rows), and the columns they add to the band's
+// copy box.
+static void make_ghost_bands(ibtfo_case *c, const std::vector<GhostRec> &gl)
 {
     const GridDesc &g = c->g;
-    c->post_idx.clear();
-    for (const GhostRec &r : gl)
-        c->post_idx.push_back((long long)g.M * r.j + r.i);
-    std::sort(c->post_idx.begin(), c->post_idx.end()); // the host writes them in address order
+    auto band_of_row = [&](int j) {
+        int k = 0;
+        while (k + 1 < NBANDS && j >= c->out_rows[k + 1])
+            k++;
+        return k;
+    };
+    c->band_ghosts.assign(NBANDS + 1, (int)gl.size());
+    c->ghost_ready.assign(NBANDS, 0);
+    size_t t = 0;
+    for (int k = 0; k < NBANDS; k++)
+    {
+        c->band_ghosts[k] = (int)t;
+        int ready = k;
+        while (t < gl.size() && gl[t].j < c->out_rows[k + 1])
+        {
+            const GhostRec &r = gl[t];
+            ready = std::max(ready, band_of_row(std::min(g.N - 1, r.idy + 1)));
+            if (c->cfg.boundary == IBTFO_BOUNDARY_BCGFM || c->cfg.boundary == IBTFO_BOUNDARY_HBCGFM)
+                ready = std::max(ready, band_of_row(std::min(g.N - 1, r.idy2 + 1)));
+            int &lo = c->fluid_cols[2 * k], &hi = c->fluid_cols[2 * k + 1];
+            if (lo >= hi)
+                lo = r.i, hi = r.i + 1;
+            else
+                lo = std::min(lo, r.i), hi = std::max(hi, r.i + 1);
+            t++;
+        }
+        c->ghost_ready[k] = ready;
+    }
+    c->band_ghosts[NBANDS] = (int)gl.size();
 }
 
 // the domain ring of the current state into u_out: two runs of whole rows
@@ -306,27 +333,25 @@ ibtfo_status ibtfo_destroy(ibtfo_case *c)
         cudaStreamSynchronize(c->stream);
     drop_graphs(c);
     vtk_writer_destroy(c->vtk, c->own ? c->own : c->stream);
-    for (cudaStream_t s : {c->h2d, c->d2h, c->sw[0], c->sw[1]})
+    for (cudaStream_t s : {c->h2d, c->d2h, c->sw[0], c->sw[1], c->fin})
         if (s)
         {
             cudaStreamSynchronize(s);
             cudaStreamDestroy(s);
         }
     for (int k = 0; k < NBANDS; k++)
-        for (cudaEvent_t e : {c->ev_in[k], c->ev_conv[k], c->ev_out[k]})
+        for (cudaEvent_t e : {c->ev_in[k], c->ev_conv[k], c->ev_out[k], c->ev_swept[k]})
             if (e)
                 cudaEventDestroy(e);
-    for (cudaEvent_t e : {c->ev_sw[0], c->ev_sw[1], c->ev_done})
+    for (cudaEvent_t e : {c->ev_sw[0], c->ev_sw[1], c->ev_fin, c->ev_done})
         if (e)
             cudaEventDestroy(e);
-    if (c->h_post)
-        cudaFreeHost(c->h_post);
     // stream-ordered frees: the memory returns to the device pool without a
     // device-wide synchronisation (other cases keep running)
     cudaStream_t fs = c->own ? c->own : c->stream;
     void *bufs[] = {c->buf[0], c->buf[1], c->ic, c->staging, c->phi, c->nx, c->ny, c->type, c->ghosts,
                     c->st, c->partial, c->ring_ic, c->tiles, c->alpha, c->ax, c->ay, c->mix_ex, c->mix_part,
-                    c->mix_links, c->mix_e, c->d_post_idx, c->d_post};
+                    c->mix_links, c->mix_e};
     for (void *p : bufs)
         if (p)
             cudaFreeAsync(p, fs);
@@ -497,15 +522,7 @@ static ibtfo_status geometry_from_phi(ibtfo_case *c)
                                           c->stream) != cudaSuccess ||
                           cudaStreamSynchronize(c->stream) != cudaSuccess))
             rc = 5;
-        make_post_cells(c, gl);
-        if (c->d_post_idx)
-            cudaFreeAsync(c->d_post_idx, c->stream);
-        if (c->d_post)
-            cudaFreeAsync(c->d_post, c->stream);
-        if (c->h_post)
-            cudaFreeHost(c->h_post);
-        c->d_post_idx = nullptr;
-        c->d_post = c->h_post = nullptr; // allocated by the first ibtfo_step_host
+        make_ghost_bands(c, gl);
     }
     if (rc == 2)
         return fail(IBTFO_ENOMEM, "geometry allocation failed");
@@ -1298,36 +1315,22 @@ ibtfo_status ibtfo_step(ibtfo_case *c, ibtfo_progress *p)
     return IBTFO_OK;
 }
 
-// streams, events and buffers of ibtfo_step_host, created on first use
+// streams and events of ibtfo_step_host, created on first use
 static cudaError_t ensure_pipeline(ibtfo_case *c)
 {
     cudaError_t e = cudaSuccess;
     if (!c->ev_done)
     {
-        for (cudaStream_t *s : {&c->h2d, &c->d2h, &c->sw[0], &c->sw[1]})
+        for (cudaStream_t *s : {&c->h2d, &c->d2h, &c->sw[0], &c->sw[1], &c->fin})
             if (e == cudaSuccess)
                 e = cudaStreamCreateWithFlags(s, cudaStreamNonBlocking);
         for (int k = 0; k < NBANDS && e == cudaSuccess; k++)
-            for (cudaEvent_t *v : {&c->ev_in[k], &c->ev_conv[k], &c->ev_out[k]})
+            for (cudaEvent_t *v : {&c->ev_in[k], &c->ev_conv[k], &c->ev_out[k], &c->ev_swept[k]})
                 if (e == cudaSuccess)
                     e = cudaEventCreateWithFlags(v, cudaEventDisableTiming);
-        for (cudaEvent_t *v : {&c->ev_sw[0], &c->ev_sw[1], &c->ev_done})
+        for (cudaEvent_t *v : {&c->ev_sw[0], &c->ev_sw[1], &c->ev_fin, &c->ev_done})
             if (e == cudaSuccess)
                 e = cudaEventCreateWithFlags(v, cudaEventDisableTiming);
-    }
-    const size_t n = c->post_idx.size();
-    if (e == cudaSuccess && n && !c->d_post_idx)
-    {
-        e = cudaMallocAsync(&c->d_post_idx, sizeof(long long) * n, c->stream);
-        if (e == cudaSuccess)
-            e = cudaMallocAsync(&c->d_post, sizeof(double) * 4 * n, c->stream);
-        if (e == cudaSuccess)
-            e = cudaMallocHost(&c->h_post, sizeof(double) * 4 * n);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(c->d_post_idx, c->post_idx.data(), sizeof(long long) * n, cudaMemcpyHostToDevice,
-                                c->stream);
-        if (e == cudaSuccess)
-            e = cudaStreamSynchronize(c->stream);
     }
     return e;
 }
@@ -1366,19 +1369,18 @@ static ibtfo_status step_host_plain(ibtfo_case *c, const double *u_in, double *u
 
 // The banded pipeline.  Row chunk k goes host -> device on one copy stream;
 // the case's stream converts it into the current state buffer; band k of the
-// sweep (the tiles of tile rows [k*nty/8, (k+1)*nty/8), which read array
-// rows up to the end of chunk k) runs on one of two sweep streams, so that
-// consecutive bands overlap on the SMs; right behind it the band's rows are
-// converted back (fluid cells from the step's output, other cells from its
-// input) and go device -> host on the second copy stream while later bands
-// compute.  After the last band the boundary pass writes the ghost cells and
-// the domain ring; those cells alone are gathered, copied and scattered
-// into u_out on the host.  Every copy of u_in lands before any write to
-// u_out, so u_out may be u_in.  In place (u_out == u_in) the host array
-// already holds every cell the step leaves alone (solid cells are never
-// written; ghost cells and the domain ring come with the boundary-pass
-// cells), so each band copies back only the interior rows of the columns
-// its fluid cells occupy.
+// sweep (the tiles of its tile rows, which read array rows up to the end of
+// chunk k) runs on one of two sweep streams, so that consecutive bands
+// overlap on the SMs.  A finishing stream then fills the ghost cells of band
+// k's rows (once every band their image points read has been swept),
+// converts the band's rows back (fluid and ghost cells from the step's
+// output, other cells from its input) and hands them to the second copy
+// stream, while later bands compute.  After the last band the domain edges
+// are filled and go back by two row copies and two strided column copies.
+// Every copy of u_in lands before any write to u_out, so u_out may be u_in.
+// In place (u_out == u_in) the host array already holds every cell the step
+// leaves alone (solid cells are never written), so each band copies back
+// only its interior rows over the columns of its fluid and ghost cells.
 static ibtfo_status step_host_banded(ibtfo_case *c, const double *u_in, double *u_out)
 {
     const GridDesc &g = c->g;
@@ -1394,6 +1396,32 @@ static ibtfo_status step_host_banded(ibtfo_case *c, const double *u_in, double *
     }
     SweepArgs a = sweep_args(c, 0);
     a.nblocks = c->ntiles;
+    FillArgs f = fill_args(c);
+    const bool gfm = c->cfg.boundary != IBTFO_BOUNDARY_REGULAR;
+    auto finish = [&](int k) -> ibtfo_status {
+        // band k's ghost cells, its rows back to the host layout, and their copy
+        for (int b = 0; b <= c->ghost_ready[k]; b++)
+            CK(cudaStreamWaitEvent(c->fin, c->ev_swept[b], 0));
+        if (gfm)
+            launch_fill_ghosts(f, c->band_ghosts[k], c->band_ghosts[k + 1], c->fin);
+        int o0 = c->out_rows[k], o1 = c->out_rows[k + 1], x0 = 0, x1 = g.M;
+        if (inplace)
+        {
+            o0 = std::max(o0, g.ng);
+            o1 = std::min(o1, g.ng + g.n_y);
+            x0 = c->fluid_cols[2 * k];
+            x1 = c->fluid_cols[2 * k + 1];
+        }
+        launch_snapshot_to_aos_rows(c->buf[0], c->buf[1], c->st, c->type, c->staging, g, o0, o1, x0, x1, c->fin);
+        CK(cudaEventRecord(c->ev_out[k], c->fin));
+        CK(cudaStreamWaitEvent(c->d2h, c->ev_out[k], 0));
+        if (o1 > o0 && x1 > x0)
+            CK(cudaMemcpy2DAsync(u_out + ((size_t)o0 * g.M + x0) * 4, row, c->staging + ((size_t)o0 * g.M + x0) * 4,
+                                 row, sizeof(double) * 4 * (size_t)(x1 - x0), (size_t)(o1 - o0),
+                                 cudaMemcpyDeviceToHost, c->d2h));
+        return IBTFO_OK;
+    };
+    int next = 0; // the next band to finish
     for (int k = 0; k < NBANDS; k++)
     {
         CK(cudaStreamWaitEvent(c->stream, c->ev_in[k], 0));
@@ -1409,35 +1437,35 @@ static ibtfo_status step_host_banded(ibtfo_case *c, const double *u_in, double *
             c->sweep(a, dim3(t1 - t0), dim3(TILE_X * TILE_Y), s);
             count_launch();
         }
-        int o0 = c->out_rows[k], o1 = c->out_rows[k + 1], x0 = 0, x1 = g.M;
-        if (inplace)
+        CK(cudaEventRecord(c->ev_swept[k], s));
+        for (; next < NBANDS && c->ghost_ready[next] <= k; next++)
         {
-            o0 = std::max(o0, g.ng);
-            o1 = std::min(o1, g.ng + g.n_y);
-            x0 = c->fluid_cols[2 * k];
-            x1 = c->fluid_cols[2 * k + 1];
+            ibtfo_status st = finish(next);
+            if (st != IBTFO_OK)
+                return st;
         }
-        launch_snapshot_to_aos_rows(c->buf[0], c->buf[1], c->st, c->type, c->staging, g, o0, o1, x0, x1, s);
-        CK(cudaEventRecord(c->ev_out[k], s));
-        CK(cudaStreamWaitEvent(c->d2h, c->ev_out[k], 0));
-        if (o1 > o0 && x1 > x0)
-            CK(cudaMemcpy2DAsync(u_out + ((size_t)o0 * g.M + x0) * 4, row, c->staging + ((size_t)o0 * g.M + x0) * 4,
-                                 row, sizeof(double) * 4 * (size_t)(x1 - x0), (size_t)(o1 - o0),
-                                 cudaMemcpyDeviceToHost, c->d2h));
     }
+    for (; next < NBANDS; next++)
+    {
+        ibtfo_status st = finish(next);
+        if (st != IBTFO_OK)
+            return st;
+    }
+    // the domain edges once every band and every ghost cell is done (periodic
+    // edges copy interior cells, ghost cells included)
     for (int q = 0; q < 2; q++)
     {
         CK(cudaEventRecord(c->ev_sw[q], c->sw[q]));
         CK(cudaStreamWaitEvent(c->stream, c->ev_sw[q], 0));
     }
-    enqueue_boundary(c);
-    const int n = (int)c->post_idx.size();
-    launch_gather_cells(c->buf[0], c->buf[1], c->st, c->d_post_idx, n, c->d_post, g, c->stream);
-    ibtfo_status rs = ring_to_host(c, u_out); // records ev_done behind the gather
+    CK(cudaEventRecord(c->ev_fin, c->fin));
+    CK(cudaStreamWaitEvent(c->stream, c->ev_fin, 0));
+    f.do_ghosts = 0;
+    f.do_ring = 1;
+    launch_fill(f, c->stream);
+    ibtfo_status rs = ring_to_host(c, u_out);
     if (rs != IBTFO_OK)
         return rs;
-    if (n)
-        CK(cudaMemcpyAsync(c->h_post, c->d_post, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, c->d2h));
     CK(cudaEventRecord(c->ev_done, c->d2h));
     CK(cudaStreamWaitEvent(c->stream, c->ev_done, 0));
     return IBTFO_OK;
@@ -1456,7 +1484,7 @@ ibtfo_status ibtfo_step_host_bytes(const ibtfo_case *c, int in_place, long long 
     long long out = cell * g.M * g.N;
     if (banded)
     {
-        out = cell * ((long long)c->post_idx.size() + 2LL * g.ng * g.M + 2LL * g.ng * g.n_y);
+        out = cell * (2LL * g.ng * g.M + 2LL * g.ng * g.n_y); // the domain ring
         for (int k = 0; k < NBANDS; k++)
         {
             if (!in_place)
@@ -1503,7 +1531,7 @@ ibtfo_status ibtfo_step_host(ibtfo_case *c, const double *u_in, double *u_out, i
         long long before = g_launches.load();
         CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
         cudaEventRecord(c->ev_done, c->stream);
-        for (cudaStream_t s : {c->h2d, c->d2h, c->sw[0], c->sw[1]})
+        for (cudaStream_t s : {c->h2d, c->d2h, c->sw[0], c->sw[1], c->fin})
             cudaStreamWaitEvent(s, c->ev_done, 0);
         st = step_host_banded(c, u_in, u_out);
         c->host_graph_launches = g_launches.load() - before;
@@ -1529,7 +1557,7 @@ ibtfo_status ibtfo_step_host(ibtfo_case *c, const double *u_in, double *u_out, i
     {
         // every helper stream starts after what is already queued on the case's stream
         CK(cudaEventRecord(c->ev_done, c->stream));
-        for (cudaStream_t s : {c->h2d, c->d2h, c->sw[0], c->sw[1]})
+        for (cudaStream_t s : {c->h2d, c->d2h, c->sw[0], c->sw[1], c->fin})
             CK(cudaStreamWaitEvent(s, c->ev_done, 0));
         st = banded ? step_host_banded(c, u_in, u_out) : step_host_plain(c, u_in, u_out);
         if (st != IBTFO_OK)
@@ -1537,23 +1565,7 @@ ibtfo_status ibtfo_step_host(ibtfo_case *c, const double *u_in, double *u_out, i
     }
     CK(cudaGetLastError());
     ibtfo_progress q;
-    st = ibtfo_get_progress(c, p ? p : &q); // waits for the copies
-    if (st != IBTFO_OK)
-        return st;
-    if (banded)
-    {
-        const size_t n = c->post_idx.size();
-        for (size_t t = 0; t < n; t++)
-        {
-            double *d = u_out + c->post_idx[t] * 4;
-            const double *v = c->h_post + t * 4;
-            d[0] = v[0];
-            d[1] = v[1];
-            d[2] = v[2];
-            d[3] = v[3];
-        }
-    }
-    return IBTFO_OK;
+    return ibtfo_get_progress(c, p ? p : &q); // waits for the copies
 }
 
 ibtfo_status ibtfo_run(ibtfo_case *c, int stop_on_nan, ibtfo_progress *p)

@@ -134,6 +134,8 @@ struct FillArgs
     int do_ring;     // run the domain-edge (Global_Boundary) pass
     int init_mode;   // initial Boundary call: fill without requiring a completed step
     const double *ring_ic; // Regular: initial values feeding the corner columns [2][2*ng][4]
+    int pre_flip;    // a step in flight: its output buffer is the one st->step_cur does not name
+    int ghost0;      // the ghost records this launch fills start here
 };
 
 struct ReduceArgs
@@ -204,6 +206,8 @@ constexpr int TILE_Y = 8;
 
 SweepLaunch sweep_launcher(int scheme, int riemann, int limiter, int precision);
 void launch_fill(const FillArgs &a, cudaStream_t s);
+// ghost records [g0, g1) of a step in flight (FillArgs.pre_flip)
+void launch_fill_ghosts(const FillArgs &a, int g0, int g1, cudaStream_t s);
 void launch_reduce(const ReduceArgs &a, int nblocks_max, cudaStream_t s);
 void launch_aos_to_soa(const double *aos, double *soa, const GridDesc &g, cudaStream_t s);
 void launch_soa_to_aos(const double *soa, double *aos, const GridDesc &g, cudaStream_t s);
@@ -212,18 +216,15 @@ void launch_aos_to_cur_rows(const double *aos, double *b0, double *b1, const Dev
                             int r1, cudaStream_t s);
 void launch_cur_to_aos_rows(const double *b0, const double *b1, const DevState *st, double *aos, const GridDesc &g,
                             int r0, int r1, cudaStream_t s);
-// rows [r0, r1), columns [c0, c1) of a step in flight (before its boundary
-// pass): fluid cells from the step's output buffer, the rest from its input
-// (st->step_cur)
+// rows [r0, r1), columns [c0, c1) of a step in flight: fluid and ghost-fluid
+// cells from the step's output buffer (the ghost cells of these rows are
+// filled by then), the rest from its input (st->step_cur)
 void launch_snapshot_to_aos_rows(const double *b0, const double *b1, const DevState *st, const uint8_t *type,
                                  double *aos, const GridDesc &g, int r0, int r1, int c0, int c1, cudaStream_t s);
 // the domain ring of the current buffer into the host-layout array
 void launch_ring_to_aos(const double *b0, const double *b1, const DevState *st, double *aos, const GridDesc &g,
                         cudaStream_t s);
-// cells given by linear indices M*j + i (the ghost list), gathered from the
-// current buffer into out[q*4 + k]
-void launch_gather_cells(const double *b0, const double *b1, const DevState *st, const long long *idx, int n,
-                         double *out, const GridDesc &g, cudaStream_t s);
+
 
 // ---------------------------------------------------------------- batches
 //
