@@ -171,8 +171,8 @@ int fill_blocks(const FillArgs &f, int phase)
     const bool gfm = f.bc != BC_REGULAR;
     const bool split = gfm && f.gb == GB_PERIODIC;
     const long long nring = 2LL * f.g.ng * f.g.n_x + 2LL * f.g.ng * f.g.N;
-    const int rblocks = (int)((nring + 255) / 256);
-    const int gblocks = (f.nghost + 255) / 256;
+    const int rblocks = (int)((nring + FILL_THREADS - 1) / FILL_THREADS);
+    const int gblocks = (f.nghost + FILL_THREADS - 1) / FILL_THREADS;
     if (phase == 0)
         return (gfm ? gblocks : 0) + (split ? 0 : rblocks);
     return split ? rblocks : 0;

@@ -216,7 +216,7 @@ __device__ void fill_ring(const FillArgs &a, const View &v, double *dst, long lo
         state_st(dst, k, o, out[k], a.g);
 }
 
-// one 256-thread block of a case's boundary pass: blocks [0, gblocks) fill
+// one FILL_THREADS block of a case's boundary pass: blocks [0, gblocks) fill
 // the ghost list, the rest the domain edges
 __device__ __forceinline__ void fill_block(const FillArgs &a, int vb, int do_ghosts, int do_ring)
 {
@@ -241,23 +241,23 @@ __device__ __forceinline__ void fill_block(const FillArgs &a, int vb, int do_gho
     v.n_x = a.g.n_x;
     v.n_y = a.g.n_y;
     double *dst = cur ? a.buf1 : a.buf0;
-    const int gblocks = do_ghosts ? (a.nghost - a.ghost0 + 255) / 256 : 0;
+    const int gblocks = do_ghosts ? (a.nghost - a.ghost0 + FILL_THREADS - 1) / FILL_THREADS : 0;
     if (vb < gblocks)
     {
-        int t = a.ghost0 + vb * 256 + threadIdx.x;
+        int t = a.ghost0 + vb * FILL_THREADS + threadIdx.x;
         if (t < a.nghost)
             fill_ghost(a, v, dst, a.ghosts[t]);
         return;
     }
     if (!do_ring)
         return;
-    long long q = (long long)(vb - gblocks) * 256 + threadIdx.x;
+    long long q = (long long)(vb - gblocks) * FILL_THREADS + threadIdx.x;
     long long nring = 2LL * a.g.ng * a.g.n_x + 2LL * a.g.ng * a.g.N;
     if (q < nring)
         fill_ring(a, v, dst, q);
 }
 
-__global__ void __launch_bounds__(256) fill_kernel(const FillArgs a)
+__global__ void __launch_bounds__(FILL_THREADS) fill_kernel(const FillArgs a)
 {
     fill_block(a, blockIdx.x, a.do_ghosts, a.do_ring);
 }
@@ -272,18 +272,18 @@ void launch_fill_ghosts(const FillArgs &a, int g0, int g1, cudaStream_t s)
     b.nghost = g1; // records [ghost0, nghost)
     b.do_ghosts = 1;
     b.do_ring = 0;
-    fill_kernel<<<(g1 - g0 + 255) / 256, 256, 0, s>>>(b);
+    fill_kernel<<<(g1 - g0 + FILL_THREADS - 1) / FILL_THREADS, FILL_THREADS, 0, s>>>(b);
     count_launch();
 }
 
 void launch_fill(const FillArgs &a, cudaStream_t s)
 {
-    int gblocks = a.do_ghosts ? (a.nghost + 255) / 256 : 0;
+    int gblocks = a.do_ghosts ? (a.nghost + FILL_THREADS - 1) / FILL_THREADS : 0;
     long long nring = 2LL * a.g.ng * a.g.n_x + 2LL * a.g.ng * a.g.N;
-    int rblocks = a.do_ring ? (int)((nring + 255) / 256) : 0;
+    int rblocks = a.do_ring ? (int)((nring + FILL_THREADS - 1) / FILL_THREADS) : 0;
     if (gblocks + rblocks == 0)
         return;
-    fill_kernel<<<gblocks + rblocks, 256, 0, s>>>(a);
+    fill_kernel<<<gblocks + rblocks, FILL_THREADS, 0, s>>>(a);
     count_launch();
 }
 
@@ -291,7 +291,7 @@ void launch_fill(const FillArgs &a, cudaStream_t s)
 // list (ghost-fluid variants) and domain edges; phase 1: the domain edges of
 // periodic ghost-fluid cases, which copy interior cells filled in phase 0.
 // The (slot, block) table lists only blocks with work; persistent CTAs walk it.
-__global__ void __launch_bounds__(256) batch_fill_kernel(const BatchHeader *__restrict__ h, int phase)
+__global__ void __launch_bounds__(FILL_THREADS) batch_fill_kernel(const BatchHeader *__restrict__ h, int phase)
 {
     const int n = h->nfill[phase];
     const int2 *tab = h->fill[phase];
@@ -310,7 +310,7 @@ __global__ void __launch_bounds__(256) batch_fill_kernel(const BatchHeader *__re
 
 void launch_batch_fill(const BatchHeader *h, int phase, int grid, cudaStream_t s)
 {
-    batch_fill_kernel<<<grid, 256, 0, s>>>(h, phase);
+    batch_fill_kernel<<<grid, FILL_THREADS, 0, s>>>(h, phase);
     count_launch();
 }
 

@@ -269,6 +269,10 @@ enum BatchShape { SHAPE_32x8 = 0, SHAPE_32x16 = 1, SHAPE_64x8 = 2, SHAPE_COUNT =
 constexpr int shape_tx(int shape) { return shape == SHAPE_64x8 ? 64 : 32; }
 constexpr int shape_ty(int shape) { return shape == SHAPE_32x16 ? 16 : 8; }
 constexpr int BATCH_THREADS = 256;
+// threads of a boundary-pass block: the ghost fill is FP64-heavy and its
+// records are few (about one per wall cell), so small blocks spread them
+// over every SM
+constexpr int FILL_THREADS = 64;
 
 struct BatchKernel
 {
