@@ -17,7 +17,7 @@ template <int SCH, int RIE, int LIM, int PREC, int TX, int TY>
 __global__ void __launch_bounds__(BATCH_THREADS) batch_sweep_kernel(const BatchHeader *__restrict__ h)
 {
     constexpr int NT = BATCH_THREADS;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     const int ntiles = h->ntiles;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x)
     {

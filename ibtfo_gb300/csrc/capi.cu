@@ -121,6 +121,8 @@ struct ibtfo_case
     DevState *st = nullptr;
     double *partial = nullptr;
     double *ring_ic = nullptr; // [2][2*ng][4]
+    int tma = 0;                // tensor maps of buf[0], buf[1] below are valid
+    CUtensorMap tmap[2];
     unsigned *tiles = nullptr; // active sweep tiles
     int ntiles = 0;
     // cut cells (BC_CCM): volume fractions, apertures, small-cell mixing lists
@@ -269,6 +271,47 @@ static ibtfo_status ring_to_host(ibtfo_case *c, double *u_out)
     CK(cudaMemcpy2DAsync(u_out + right, row, c->staging + right, row, cell * g.ng, g.n_y, cudaMemcpyDeviceToHost,
                          c->d2h));
     return IBTFO_OK;
+}
+
+// Tensor maps of the two state buffers for the sweeps' bulk tensor copies:
+// (column, row, plane) with the row pitch and plane stride of the buffers,
+// box = a 32x8 tile plus its two-cell halo over the four planes (FP64, or
+// the FP32 form's hi planes).  A box starts at column i0 - 2 = 32 k + ng - 2,
+// so the copies need ng == 2 for their 16-byte start alignment; other
+// ghost widths keep the element-wise staging.  0 when not available.
+static int make_state_tmaps(ibtfo_case *c)
+{
+    const GridDesc &g = c->g;
+    if (g.ng != 2)
+        return 0;
+    typedef CUresult (*EncodeTiled)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                     const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                     CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    static EncodeTiled encode = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            encode = reinterpret_cast<EncodeTiled>(fn);
+        cudaGetLastError();
+    });
+    if (!encode)
+        return 0;
+    const bool f32 = g.f32 != 0;
+    const cuuint64_t elem = f32 ? sizeof(float) : sizeof(double);
+    const cuuint64_t dims[3] = {(cuuint64_t)g.M, (cuuint64_t)g.N, 4};
+    const cuuint64_t strides[2] = {(cuuint64_t)g.pitch * elem, (cuuint64_t)g.plane * elem};
+    const cuuint32_t box[3] = {TILE_X + 4, TILE_Y + 4, 4};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    for (int b = 0; b < 2; b++)
+        if (encode(&c->tmap[b], f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, c->buf[b],
+                   dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return 0;
+    return 1;
 }
 
 // Case buffers come from the device's stream-ordered pool; freed memory stays
@@ -454,6 +497,7 @@ ibtfo_status ibtfo_create(const ibtfo_config *cfg, ibtfo_case **out)
         return s;
     }
     c->stream = c->own;
+    c->tma = make_state_tmaps(c);
     *out = c;
     return IBTFO_OK;
 }
@@ -643,6 +687,9 @@ static FillArgs fill_args(ibtfo_case *c)
 static SweepArgs sweep_args(ibtfo_case *c, int guard)
 {
     SweepArgs a{};
+    a.tma = c->tma;
+    a.tmap[0] = c->tmap[0];
+    a.tmap[1] = c->tmap[1];
     a.g = c->g;
     a.buf0 = c->buf[0];
     a.buf1 = c->buf[1];

@@ -49,7 +49,7 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) ccm_sweep_kernel(const CcmArgs
 {
     using T = typename std::conditional<PREC == 2, float, double>::type;
     constexpr int TX = TILE_X, TY = TILE_Y, NT = TX * TY, WX = TX + 4, WY = TY + 4;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     auto &s = *reinterpret_cast<CcmSmem<T, TX, TY> *>(smem_raw);
 
     const SweepArgs &a = ca.s;

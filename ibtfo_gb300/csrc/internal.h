@@ -3,6 +3,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <cuda.h> // CUtensorMap (the tensor maps are encoded through the runtime's driver entry point)
 #include <cuda_runtime.h>
 #include <string>
 #include <vector>
@@ -39,7 +40,7 @@ struct DevState
     double last_amax, last_umax, last_vmax; // maxima behind the latest dt
 };
 
-enum { STATUS_NAN = 1 };
+enum { STATUS_NAN = 1, STATUS_STALL = 2 }; // STALL: a bounded wait of a kernel gave up
 
 // One ghost-fluid cell (interior cell of type 2) with everything its fill
 // needs, computed once at set-up (reference Scheme_Index).
@@ -118,6 +119,8 @@ struct SweepArgs
     int stage;               // 0: one step; Time = RK2: 1 the first stage, 2 the second stage and average
     int tile0;               // a step split over several launches: first tile of this launch
     int nblocks;             // ... and the tiles of the whole step (0: one launch, its grid)
+    int tma;                 // stage tiles with the tensor maps below (else element-wise loads)
+    CUtensorMap tmap[2];     // buf0 / buf1 as (column, row, plane) tensors, box = tile + halo, 4 planes
 };
 
 struct FillArgs

@@ -76,10 +76,14 @@ struct SweepSmem32
 // Time = RK2: stage 1 gathers no statistics; stage 2 stores the average of
 // the advanced state and the pair the output buffer holds (the state at the
 // start of the step).
+// With `tmap` the tile and halo (hi planes) are staged by one bulk tensor
+// copy (column i0 - 2 must be a multiple of 4); a copy that does not
+// complete within the bounded wait sets STATUS_STALL and the tile is skipped.
 template <int SCH, int RIE, int LIM, int TX, int TY, int NT>
 __device__ __forceinline__ void sweep_tile32(SweepSmem32<TX, TY> &s, const GridDesc &g, const float *__restrict__ U,
                                              float *__restrict__ V, const uint8_t *__restrict__ type, int i0, int j0,
-                                             double dt, CellStats32 &cs, int stage = 0)
+                                             double dt, CellStats32 &cs, int stage = 0,
+                                             const CUtensorMap *tmap = nullptr, int *status = nullptr)
 {
     constexpr int WX = TX + 4, WY = TY + 4;
     const long long P = g.plane;
@@ -94,8 +98,27 @@ __device__ __forceinline__ void sweep_tile32(SweepSmem32<TX, TY> &s, const GridD
         s.sC[3] = 0.5f * s.sC[1];
     }
 
+    if (tmap)
+    {
+        __shared__ uint64_t bar;
+        if (tid == 0)
+            mbar_init(&bar, 1);
+        __syncthreads();
+        if (tid == 0)
+        {
+            mbar_expect_tx(&bar, (unsigned)sizeof(s.sU));
+            tma_load_3d(&s.sU[0][0][0], tmap, i0 - 2, j0 - 2, 0, &bar);
+        }
+        if (!__syncthreads_and(mbar_wait(&bar, 0)))
+        {
+            if (tid == 0 && status)
+                atomicOr(status, STATUS_STALL);
+            return;
+        }
+    }
     // stage the tile and its halo: one index computation per cell, four planes
-    for (int q = tid; q < WX * WY; q += NT)
+    else
+        for (int q = tid; q < WX * WY; q += NT)
     {
         const int ly = q / WX, lx = q - ly * WX;
         const int gi = i0 - 2 + lx, gj = j0 - 2 + ly;
@@ -302,10 +325,10 @@ __device__ __forceinline__ void block_reduce_finalize32(CellStats32 cs, DevState
 
 // one case: one CTA per active tile
 template <int SCH, int RIE, int LIM>
-__global__ void __launch_bounds__(TILE_X *TILE_Y, 6) sweep_f32_kernel(const SweepArgs a)
+__global__ void __launch_bounds__(TILE_X *TILE_Y, 6) sweep_f32_kernel(const __grid_constant__ SweepArgs a)
 {
     constexpr int NT = TILE_X * TILE_Y;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     auto &s = *reinterpret_cast<SweepSmem32<TILE_X, TILE_Y> *>(smem_raw);
 
     const GridDesc &g = a.g;
@@ -323,7 +346,8 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y, 6) sweep_f32_kernel(const Swee
     const int i0 = g.ng + (int)(tile & 0xFFFFu) * TILE_X;
     const int j0 = g.ng + (int)(tile >> 16) * TILE_Y;
     CellStats32 cs;
-    sweep_tile32<SCH, RIE, LIM, TILE_X, TILE_Y, NT>(s, g, U, V, a.type, i0, j0, dt, cs, a.stage);
+    sweep_tile32<SCH, RIE, LIM, TILE_X, TILE_Y, NT>(s, g, U, V, a.type, i0, j0, dt, cs, a.stage,
+                                                    a.tma ? &a.tmap[cur] : nullptr, &st->status);
     block_reduce_finalize32<NT>(cs, st, a.partial, g, a.nblocks ? a.nblocks : gridDim.x, bid, a.stage == 1);
 }
 

@@ -21,6 +21,7 @@
 #include "internal.h"
 #include "physics.cuh"
 #include "physics_fast.cuh"
+#include "tma.cuh"
 
 namespace ibtfo {
 
@@ -266,10 +267,15 @@ struct SweepSmem64
 // accumulate the statistics of the updated cells.  All NT threads call it.
 // stage 2 (the second RK2 stage) stores 0.5 (V + the advanced state) instead,
 // V holding the state at the start of the step; stage 1 gathers no statistics.
+// With `tmap` the tile and halo are staged by one bulk tensor copy (the box
+// starts at column i0 - 2, which must be a multiple of 2); a copy that does
+// not complete within the bounded wait sets STATUS_STALL in *status and the
+// tile is skipped.
 template <int SCH, int RIE, int LIM, int FAST, int TX, int TY, int NT>
 __device__ __forceinline__ void sweep_tile64(SweepSmem64<TX, TY> &s, const GridDesc &g, const double *__restrict__ U,
                                              double *__restrict__ V, const uint8_t *__restrict__ type, int i0, int j0,
-                                             double dt, CellStats &cs, int stage = 0)
+                                             double dt, CellStats &cs, int stage = 0,
+                                             const CUtensorMap *tmap = nullptr, int *status = nullptr)
 {
     constexpr int WX = TX + 4, WY = TY + 4;
     const long long P = g.plane;
@@ -284,9 +290,28 @@ __device__ __forceinline__ void sweep_tile64(SweepSmem64<TX, TY> &s, const GridD
         s.sC[3] = 0.5 * s.sC[1];
     }
 
+    if (tmap)
+    {
+        __shared__ uint64_t bar;
+        if (tid == 0)
+            mbar_init(&bar, 1);
+        __syncthreads();
+        if (tid == 0)
+        {
+            mbar_expect_tx(&bar, (unsigned)sizeof(s.sU));
+            tma_load_3d(&s.sU[0][0][0], tmap, i0 - 2, j0 - 2, 0, &bar);
+        }
+        if (!__syncthreads_and(mbar_wait(&bar, 0)))
+        {
+            if (tid == 0 && status)
+                atomicOr(status, STATUS_STALL);
+            return;
+        }
+    }
     // stage the tile and its halo (always inside the padded array: ng >= 2),
     // one index computation per cell for the four planes
-    for (int q = tid; q < WX * WY; q += NT)
+    else
+        for (int q = tid; q < WX * WY; q += NT)
     {
         const int ly = q / WX, lx = q - ly * WX;
         const int gi = i0 - 2 + lx, gj = j0 - 2 + ly;
@@ -446,10 +471,10 @@ __device__ __forceinline__ void sweep_tile64(SweepSmem64<TX, TY> &s, const GridD
 template <int SCH, int RIE, int LIM, int FAST>
 // fp64_fast with HLL or Steger-Warming fits 64 registers: 4 CTAs per SM
 __global__ void __launch_bounds__(TILE_X *TILE_Y, (FAST && (RIE == HLL || RIE == SW)) ? 4 : 1)
-    sweep_kernel(const SweepArgs a)
+    sweep_kernel(const __grid_constant__ SweepArgs a)
 {
     constexpr int NT = TILE_X * TILE_Y;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     auto &s = *reinterpret_cast<SweepSmem64<TILE_X, TILE_Y> *>(smem_raw);
 
     const GridDesc &g = a.g;
@@ -471,7 +496,8 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y, (FAST && (RIE == HLL || RIE ==
     const int i0 = g.ng + (int)(tile & 0xFFFFu) * TILE_X;
     const int j0 = g.ng + (int)(tile >> 16) * TILE_Y;
     CellStats cs;
-    sweep_tile64<SCH, RIE, LIM, FAST, TILE_X, TILE_Y, NT>(s, g, U, V, a.type, i0, j0, dt, cs, a.stage);
+    sweep_tile64<SCH, RIE, LIM, FAST, TILE_X, TILE_Y, NT>(s, g, U, V, a.type, i0, j0, dt, cs, a.stage,
+                                                          a.tma ? &a.tmap[cur] : nullptr, &st->status);
     block_reduce_finalize<NT>(cs, st, a.partial, g, true, false, a.nblocks ? a.nblocks : gridDim.x, bid,
                               a.stage == 1);
 }

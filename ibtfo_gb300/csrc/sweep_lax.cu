@@ -29,7 +29,7 @@ struct LaxSmem
 __global__ void __launch_bounds__(TILE_X *TILE_Y) lax_kernel(const SweepArgs a)
 {
     constexpr int NT = TILE_X * TILE_Y;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     auto &s = *reinterpret_cast<LaxSmem *>(smem_raw);
 
     const GridDesc &g = a.g;
