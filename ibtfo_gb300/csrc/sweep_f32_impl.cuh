@@ -78,7 +78,8 @@ struct SweepSmem32
 // start of the step).
 // With `tmap` the tile and halo (hi planes) are staged by one bulk tensor
 // copy (column i0 - 2 must be a multiple of 4); a copy that does not
-// complete within the bounded wait sets STATUS_STALL and the tile is skipped.
+// complete within the bounded wait sets STATUS_STALL and the tile is staged
+// element-wise.
 template <int SCH, int RIE, int LIM, int TX, int TY, int NT>
 __device__ __forceinline__ void sweep_tile32(SweepSmem32<TX, TY> &s, const GridDesc &g, const float *__restrict__ U,
                                              float *__restrict__ V, const uint8_t *__restrict__ type, int i0, int j0,
@@ -98,6 +99,7 @@ __device__ __forceinline__ void sweep_tile32(SweepSmem32<TX, TY> &s, const GridD
         s.sC[3] = 0.5f * s.sC[1];
     }
 
+    bool staged = false;
     if (tmap)
     {
         __shared__ uint64_t bar;
@@ -109,15 +111,12 @@ __device__ __forceinline__ void sweep_tile32(SweepSmem32<TX, TY> &s, const GridD
             mbar_expect_tx(&bar, (unsigned)sizeof(s.sU));
             tma_load_3d(&s.sU[0][0][0], tmap, i0 - 2, j0 - 2, 0, &bar);
         }
-        if (!__syncthreads_and(mbar_wait(&bar, 0)))
-        {
-            if (tid == 0 && status)
-                atomicOr(status, STATUS_STALL);
-            return;
-        }
+        staged = __syncthreads_and(mbar_wait(&bar, 0));
+        if (!staged && tid == 0 && status)
+            atomicOr(status, STATUS_STALL); // stage element-wise instead (a late copy brings the same values)
     }
     // stage the tile and its halo: one index computation per cell, four planes
-    else
+    if (!staged)
         for (int q = tid; q < WX * WY; q += NT)
     {
         const int ly = q / WX, lx = q - ly * WX;

@@ -270,7 +270,7 @@ struct SweepSmem64
 // With `tmap` the tile and halo are staged by one bulk tensor copy (the box
 // starts at column i0 - 2, which must be a multiple of 2); a copy that does
 // not complete within the bounded wait sets STATUS_STALL in *status and the
-// tile is skipped.
+// tile is staged element-wise.
 template <int SCH, int RIE, int LIM, int FAST, int TX, int TY, int NT>
 __device__ __forceinline__ void sweep_tile64(SweepSmem64<TX, TY> &s, const GridDesc &g, const double *__restrict__ U,
                                              double *__restrict__ V, const uint8_t *__restrict__ type, int i0, int j0,
@@ -290,6 +290,7 @@ __device__ __forceinline__ void sweep_tile64(SweepSmem64<TX, TY> &s, const GridD
         s.sC[3] = 0.5 * s.sC[1];
     }
 
+    bool staged = false;
     if (tmap)
     {
         __shared__ uint64_t bar;
@@ -301,16 +302,13 @@ __device__ __forceinline__ void sweep_tile64(SweepSmem64<TX, TY> &s, const GridD
             mbar_expect_tx(&bar, (unsigned)sizeof(s.sU));
             tma_load_3d(&s.sU[0][0][0], tmap, i0 - 2, j0 - 2, 0, &bar);
         }
-        if (!__syncthreads_and(mbar_wait(&bar, 0)))
-        {
-            if (tid == 0 && status)
-                atomicOr(status, STATUS_STALL);
-            return;
-        }
+        staged = __syncthreads_and(mbar_wait(&bar, 0));
+        if (!staged && tid == 0 && status)
+            atomicOr(status, STATUS_STALL); // stage element-wise instead (a late copy brings the same values)
     }
     // stage the tile and its halo (always inside the padded array: ng >= 2),
     // one index computation per cell for the four planes
-    else
+    if (!staged)
         for (int q = tid; q < WX * WY; q += NT)
     {
         const int ly = q / WX, lx = q - ly * WX;
