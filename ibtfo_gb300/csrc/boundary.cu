@@ -433,19 +433,52 @@ void launch_soa_to_aos(const double *soa, double *aos, const GridDesc &g, cudaSt
 
 // the same conversions over rows [r0, r1), with the current buffer taken from
 // the device state when the kernel runs (so a step queued before it counts)
-__global__ void aos_to_cur_rows_kernel(const double *__restrict__ aos, double *b0, double *b1, DevState *st,
-                                       GridDesc g, int r0, int r1)
+struct BoxArgs
 {
-    long long c = (long long)r0 * g.M + (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r0 == 0 && c == 0)
+    HostBoxes bx;
+    long long start[6]; // cells before each box
+};
+
+__global__ void aos_to_cur_boxes_kernel(const double *__restrict__ aos, double *b0, double *b1, DevState *st,
+                                        GridDesc g, const BoxArgs a, int first, int both)
+{
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (first && q == 0)
         st->step_cur = st->cur; // read by the snapshot conversions of this step
-    if (c >= (long long)r1 * g.M)
+    if (q >= a.start[a.bx.n])
         return;
+    int b = 0;
+    while (q >= a.start[b + 1])
+        b++;
+    const int w = a.bx.c1[b] - a.bx.c0[b];
+    const long long r = q - a.start[b];
+    const int j = a.bx.r0[b] + (int)(r / w), i = a.bx.c0[b] + (int)(r % w);
+    const long long c = (long long)j * g.M + i, o = (long long)j * g.pitch + i;
     double *soa = st->cur ? b1 : b0;
-    int j = (int)(c / g.M), i = (int)(c - (long long)j * g.M);
-    long long o = (long long)j * g.pitch + i;
+    double *other = st->cur ? b0 : b1;
     for (int k = 0; k < 4; k++)
-        state_st(soa, k, o, aos[c * 4 + k], g);
+    {
+        const double v = aos[c * 4 + k];
+        state_st(soa, k, o, v, g);
+        if (both)
+            state_st(other, k, o, v, g);
+    }
+}
+
+void launch_aos_to_cur_boxes(const double *aos, double *b0, double *b1, const DevState *st, const GridDesc &g,
+                             const HostBoxes &bx, bool first, bool both, cudaStream_t s)
+{
+    BoxArgs a;
+    a.bx = bx;
+    a.start[0] = 0;
+    for (int b = 0; b < bx.n; b++)
+        a.start[b + 1] = a.start[b] + (long long)(bx.r1[b] - bx.r0[b]) * (bx.c1[b] - bx.c0[b]);
+    const long long n = a.start[bx.n];
+    if (n <= 0)
+        return;
+    aos_to_cur_boxes_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(aos, b0, b1, const_cast<DevState *>(st), g,
+                                                                        a, first ? 1 : 0, both ? 1 : 0);
+    count_launch();
 }
 
 __global__ void cur_rows_to_aos_kernel(const double *b0, const double *b1, const DevState *__restrict__ st,
@@ -459,17 +492,6 @@ __global__ void cur_rows_to_aos_kernel(const double *b0, const double *b1, const
     long long o = (long long)j * g.pitch + i;
     for (int k = 0; k < 4; k++)
         aos[c * 4 + k] = state_ld(soa, k, o, g);
-}
-
-void launch_aos_to_cur_rows(const double *aos, double *b0, double *b1, const DevState *st, const GridDesc &g, int r0,
-                            int r1, cudaStream_t s)
-{
-    long long n = (long long)(r1 - r0) * g.M;
-    if (n <= 0)
-        return;
-    aos_to_cur_rows_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(aos, b0, b1, const_cast<DevState *>(st), g,
-                                                                      r0, r1);
-    count_launch();
 }
 
 __global__ void snapshot_rows_to_aos_kernel(const double *b0, const double *b1, const DevState *__restrict__ st,

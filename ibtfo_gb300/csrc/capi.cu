@@ -6,6 +6,7 @@
 // device, ibtfo_advance queues any number of steps without a host round trip;
 // chunks of steps are captured once into a CUDA graph and replayed.
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -105,6 +106,9 @@ static void set_derived_constants(GridDesc &g)
     g.idyf = (float)g.idy;
 }
 
+static constexpr int NBANDS = 8; // row bands of ibtfo_step_host
+static constexpr int NSW = 2;    // streams the bands' sweeps alternate on
+
 struct ibtfo_case
 {
     ibtfo_config cfg;
@@ -145,17 +149,31 @@ struct ibtfo_case
     std::vector<int> out_rows;    // NBANDS + 1 array-row offsets of the device-to-host chunks
     std::vector<int> band_tiles;  // NBANDS + 1 offsets into the active-tile list
     std::vector<int> fluid_cols;  // 2 NBANDS: columns [c0, c1) holding the fluid cells of each band
+    std::vector<HostBoxes> in_boxes; // NBANDS: the cells of each chunk an in-place step reads
+    // the host array of the last in-place ibtfo_step_host: the cells outside
+    // in_boxes hold in both state buffers what they hold there
+    const double *mirror_in = nullptr;
     std::vector<int> band_ghosts; // NBANDS + 1 offsets into the ghost list (rows of each band)
     std::vector<int> ghost_ready; // NBANDS: the last band whose fluid cells the band's ghost fills read
-    cudaStream_t h2d = nullptr, d2h = nullptr, sw[2] = {nullptr, nullptr}, fin = nullptr;
-    cudaEvent_t ev_in[8] = {}, ev_conv[8] = {}, ev_out[8] = {}, ev_swept[8] = {}, ev_sw[2] = {}, ev_fin = nullptr,
-                ev_done = nullptr;
+    cudaStream_t h2d = nullptr, d2h = nullptr, sw[NSW] = {}, fin = nullptr;
+    cudaEvent_t ev_in[NBANDS] = {}, ev_conv[NBANDS] = {}, ev_out[NBANDS] = {}, ev_swept[NBANDS] = {},
+                ev_sw[NSW] = {}, ev_fin = nullptr, ev_done = nullptr;
     // the banded step captured as a CUDA graph for one pair of page-locked host arrays
     cudaGraphExec_t host_graph = nullptr;
     const double *host_graph_in = nullptr;
     double *host_graph_out = nullptr;
     long long host_graph_launches = 0;
 };
+
+// the streams of ibtfo_step_host besides the case's own
+static std::array<cudaStream_t, 3 + NSW> helper_streams(const ibtfo_case *c)
+{
+    std::array<cudaStream_t, 3 + NSW> a;
+    a[0] = c->h2d, a[1] = c->d2h, a[2] = c->fin;
+    for (int q = 0; q < NSW; q++)
+        a[3 + q] = c->sw[q];
+    return a;
+}
 
 // graphs embed the case's kernel arguments and buffers: dropped whenever those change
 static void drop_graphs(ibtfo_case *c)
@@ -179,7 +197,6 @@ static void drop_graphs(ibtfo_case *c)
 // row lies in [k*nty/NB, (k+1)*nty/NB); its transfer chunk ends at the last
 // array row that band's stencil reads (two rows above its tiles), so band k
 // can start once chunks 0..k are on the device.
-static const int NBANDS = 8;
 static void make_bands(ibtfo_case *c, const std::vector<unsigned> &tiles)
 {
     const GridDesc &g = c->g;
@@ -251,6 +268,81 @@ static void make_ghost_bands(ibtfo_case *c, const std::vector<GhostRec> &gl)
         c->ghost_ready[k] = ready;
     }
     c->band_ghosts[NBANDS] = (int)gl.size();
+}
+
+// Copy-in boxes of an in-place ibtfo_step_host, per transfer chunk: the
+// cells some part of the step reads or copies back.  Those are the staged
+// box of every active tile (the tile and two cells around it: the widest
+// reconstruction stencil), the band's copy-back columns (fluid and ghost
+// cells, whose rows' other cells go back from the input), and the domain
+// edge: 2 ng rows and columns at each side, the ring and the cells its fill
+// copies.  Per chunk: whole edge rows, and over the other rows the union of
+// their columns with the two edge strips (at most five boxes).  Solid cells
+// away from the fluid and the edge are neither read nor written by a step.
+static void make_in_boxes(ibtfo_case *c, const std::vector<unsigned> &tiles)
+{
+    const GridDesc &g = c->g;
+    std::vector<int> lo(g.N, g.M), hi(g.N, 0);
+    auto add = [&](int j0, int j1, int i0, int i1) {
+        j0 = std::max(j0, 0);
+        j1 = std::min(j1, g.N);
+        i0 = std::max(i0, 0);
+        i1 = std::min(i1, g.M);
+        if (i0 >= i1)
+            return;
+        for (int j = j0; j < j1; j++)
+        {
+            lo[j] = std::min(lo[j], i0);
+            hi[j] = std::max(hi[j], i1);
+        }
+    };
+    const int halo = std::max(2, g.ng);
+    for (unsigned t : tiles)
+    {
+        const int i0 = g.ng + (int)(t & 0xFFFFu) * TILE_X, j0 = g.ng + (int)(t >> 16) * TILE_Y;
+        add(j0 - halo, j0 + TILE_Y + halo, i0 - halo, i0 + TILE_X + halo);
+    }
+    for (int k = 0; k < NBANDS; k++)
+        add(std::max(c->out_rows[k], g.ng), std::min(c->out_rows[k + 1], g.ng + g.n_y), c->fluid_cols[2 * k],
+            c->fluid_cols[2 * k + 1]);
+    const int e = 2 * g.ng, bottom = std::max(e, g.N - e);
+    c->in_boxes.assign(NBANDS, HostBoxes{});
+    for (int k = 0; k < NBANDS; k++)
+    {
+        HostBoxes &b = c->in_boxes[k];
+        auto push = [&](int r0, int r1, int c0, int c1) {
+            if (r1 > r0 && c1 > c0)
+            {
+                b.r0[b.n] = r0, b.r1[b.n] = r1, b.c0[b.n] = c0, b.c1[b.n] = c1;
+                b.n++;
+            }
+        };
+        const int r0 = c->band_rows[k], r1 = c->band_rows[k + 1];
+        push(r0, std::min(r1, e), 0, g.M);
+        const int a = std::max(r0, e), z = std::min(r1, bottom);
+        if (a < z)
+        {
+            int clo = g.M, chi = 0;
+            for (int j = a; j < z; j++)
+                if (lo[j] < hi[j])
+                    clo = std::min(clo, lo[j]), chi = std::max(chi, hi[j]);
+            // [0, e), [clo, chi), [M - e, M) in column order, overlaps merged
+            int iv[3][2] = {{0, e}, {clo, chi}, {g.M - e, g.M}};
+            int n = 0, m[3][2];
+            for (auto &v : iv)
+            {
+                if (v[0] >= v[1])
+                    continue;
+                if (n && v[0] <= m[n - 1][1])
+                    m[n - 1][1] = std::max(m[n - 1][1], v[1]);
+                else
+                    m[n][0] = v[0], m[n][1] = v[1], n++;
+            }
+            for (int q = 0; q < n; q++)
+                push(a, z, m[q][0], m[q][1]);
+        }
+        push(std::max(r0, bottom), r1, 0, g.M);
+    }
 }
 
 // the domain ring of the current state into u_out: two runs of whole rows
@@ -376,7 +468,7 @@ ibtfo_status ibtfo_destroy(ibtfo_case *c)
         cudaStreamSynchronize(c->stream);
     drop_graphs(c);
     vtk_writer_destroy(c->vtk, c->own ? c->own : c->stream);
-    for (cudaStream_t s : {c->h2d, c->d2h, c->sw[0], c->sw[1], c->fin})
+    for (cudaStream_t s : helper_streams(c))
         if (s)
         {
             cudaStreamSynchronize(s);
@@ -386,7 +478,10 @@ ibtfo_status ibtfo_destroy(ibtfo_case *c)
         for (cudaEvent_t e : {c->ev_in[k], c->ev_conv[k], c->ev_out[k], c->ev_swept[k]})
             if (e)
                 cudaEventDestroy(e);
-    for (cudaEvent_t e : {c->ev_sw[0], c->ev_sw[1], c->ev_fin, c->ev_done})
+    for (cudaEvent_t e : c->ev_sw)
+        if (e)
+            cudaEventDestroy(e);
+    for (cudaEvent_t e : {c->ev_fin, c->ev_done})
         if (e)
             cudaEventDestroy(e);
     // stream-ordered frees: the memory returns to the device pool without a
@@ -567,6 +662,8 @@ static ibtfo_status geometry_from_phi(ibtfo_case *c)
                           cudaStreamSynchronize(c->stream) != cudaSuccess))
             rc = 5;
         make_ghost_bands(c, gl);
+        make_in_boxes(c, tile_list);
+        c->mirror_in = nullptr;
     }
     if (rc == 2)
         return fail(IBTFO_ENOMEM, "geometry allocation failed");
@@ -808,6 +905,7 @@ ibtfo_status ibtfo_set_state(ibtfo_case *c, const double *u0)
 // Boundary call and the initial ComputeDt / CaculateMass (InclineSod.cpp:105-120)
 static ibtfo_status finish_initial_state(ibtfo_case *c)
 {
+    c->mirror_in = nullptr;
     const GridDesc &g = c->g;
     CK(cudaMemcpyAsync(c->buf[1], c->buf[0], sizeof(double) * 4 * (size_t)g.plane, cudaMemcpyDeviceToDevice,
                        c->stream));
@@ -854,7 +952,11 @@ ibtfo_status ibtfo_put_state(ibtfo_case *c, const double *u)
     CK(cudaStreamSynchronize(c->stream));
     CK(ensure_staging(c));
     CK(cudaMemcpyAsync(c->staging, u, sizeof(double) * 4 * (size_t)g.M * g.N, cudaMemcpyHostToDevice, c->stream));
+    // both buffers: a step leaves solid cells as they are (the reference copies
+    // U_NEW into U_OLD for fluid cells only, IDWBaseGFM/GFM_Bound.cpp:24-35)
     launch_aos_to_soa(c->staging, c->buf[s.cur], g, c->stream);
+    launch_aos_to_soa(c->staging, c->buf[s.cur ^ 1], g, c->stream);
+    c->mirror_in = nullptr;
     CK(cudaGetLastError());
     return IBTFO_OK;
 }
@@ -1176,6 +1278,7 @@ ibtfo_status ibtfo_load_checkpoint(ibtfo_case *c, const char *path)
         return fail(IBTFO_EINVAL, std::string(path) + " is truncated");
     CK(cudaMemcpyAsync(c->buf[0], u.data(), bytes, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(c->buf[1], u.data(), bytes, cudaMemcpyHostToDevice, c->stream));
+    c->mirror_in = nullptr;
     if (h.has_ic)
     {
         CK(cudaMemcpyAsync(c->ic, ic.data(), bytes, cudaMemcpyHostToDevice, c->stream));
@@ -1368,18 +1471,42 @@ static cudaError_t ensure_pipeline(ibtfo_case *c)
     cudaError_t e = cudaSuccess;
     if (!c->ev_done)
     {
-        for (cudaStream_t *s : {&c->h2d, &c->d2h, &c->sw[0], &c->sw[1], &c->fin})
+        for (cudaStream_t *s : {&c->h2d, &c->d2h, &c->fin})
             if (e == cudaSuccess)
                 e = cudaStreamCreateWithFlags(s, cudaStreamNonBlocking);
+        for (cudaStream_t &s : c->sw)
+            if (e == cudaSuccess)
+                e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
         for (int k = 0; k < NBANDS && e == cudaSuccess; k++)
             for (cudaEvent_t *v : {&c->ev_in[k], &c->ev_conv[k], &c->ev_out[k], &c->ev_swept[k]})
                 if (e == cudaSuccess)
                     e = cudaEventCreateWithFlags(v, cudaEventDisableTiming);
-        for (cudaEvent_t *v : {&c->ev_sw[0], &c->ev_sw[1], &c->ev_fin, &c->ev_done})
+        for (cudaEvent_t &v : c->ev_sw)
+            if (e == cudaSuccess)
+                e = cudaEventCreateWithFlags(&v, cudaEventDisableTiming);
+        for (cudaEvent_t *v : {&c->ev_fin, &c->ev_done})
             if (e == cudaSuccess)
                 e = cudaEventCreateWithFlags(v, cudaEventDisableTiming);
     }
     return e;
+}
+
+// The cells of transfer chunk k an ibtfo_step_host copies in: every row, or
+// (boxes) the in-place copy-in boxes.  They go into both state buffers: a
+// step leaves solid cells as they are (the reference copies U_NEW into U_OLD
+// for fluid cells only, e.g. IDWBaseGFM/GFM_Bound.cpp:24-35), which with two
+// alternating buffers needs them in both.
+static HostBoxes chunk_boxes(const ibtfo_case *c, int k, bool boxes)
+{
+    if (boxes)
+        return c->in_boxes[k];
+    HostBoxes b{};
+    if (c->band_rows[k + 1] > c->band_rows[k])
+    {
+        b.n = 1;
+        b.r0[0] = c->band_rows[k], b.r1[0] = c->band_rows[k + 1], b.c0[0] = 0, b.c1[0] = c->g.M;
+    }
+    return b;
 }
 
 // The step when the banded pipeline does not apply (cut cells, RK2): the
@@ -1396,7 +1523,8 @@ static ibtfo_status step_host_plain(ibtfo_case *c, const double *u_in, double *u
                                cudaMemcpyHostToDevice, c->h2d));
         CK(cudaEventRecord(c->ev_in[k], c->h2d));
         CK(cudaStreamWaitEvent(c->stream, c->ev_in[k], 0));
-        launch_aos_to_cur_rows(c->staging, c->buf[0], c->buf[1], c->st, g, r0, r1, c->stream);
+        launch_aos_to_cur_boxes(c->staging, c->buf[0], c->buf[1], c->st, g, chunk_boxes(c, k, false), k == 0, true,
+                                c->stream);
     }
     enqueue_step(c, 0);
     for (int k = 0; k < NBANDS; k++)
@@ -1427,18 +1555,26 @@ static ibtfo_status step_host_plain(ibtfo_case *c, const double *u_in, double *u
 // Every copy of u_in lands before any write to u_out, so u_out may be u_in.
 // In place (u_out == u_in) the host array already holds every cell the step
 // leaves alone (solid cells are never written), so each band copies back
-// only its interior rows over the columns of its fluid and ghost cells.
-static ibtfo_status step_host_banded(ibtfo_case *c, const double *u_in, double *u_out)
+// only its interior rows over the columns of its fluid and ghost cells, and
+// (boxes) copies in only the cells some part of the step reads.
+static ibtfo_status step_host_banded(ibtfo_case *c, const double *u_in, double *u_out, bool boxes)
 {
     const GridDesc &g = c->g;
-    const size_t row = sizeof(double) * 4 * (size_t)g.M;
+    const size_t row = sizeof(double) * 4 * (size_t)g.M, cell = sizeof(double) * 4;
     const bool inplace = (u_out == u_in);
     for (int k = 0; k < NBANDS; k++)
     {
-        const int r0 = c->band_rows[k], r1 = c->band_rows[k + 1];
-        if (r1 > r0)
-            CK(cudaMemcpyAsync(c->staging + (size_t)r0 * 4 * g.M, u_in + (size_t)r0 * 4 * g.M, row * (r1 - r0),
-                               cudaMemcpyHostToDevice, c->h2d));
+        const HostBoxes b = chunk_boxes(c, k, boxes);
+        for (int q = 0; q < b.n; q++)
+        {
+            const size_t o = ((size_t)b.r0[q] * g.M + b.c0[q]) * 4;
+            if (b.c0[q] == 0 && b.c1[q] == g.M)
+                CK(cudaMemcpyAsync(c->staging + o, u_in + o, row * (b.r1[q] - b.r0[q]), cudaMemcpyHostToDevice,
+                                   c->h2d));
+            else
+                CK(cudaMemcpy2DAsync(c->staging + o, row, u_in + o, row, cell * (b.c1[q] - b.c0[q]),
+                                     (size_t)(b.r1[q] - b.r0[q]), cudaMemcpyHostToDevice, c->h2d));
+        }
         CK(cudaEventRecord(c->ev_in[k], c->h2d));
     }
     SweepArgs a = sweep_args(c, 0);
@@ -1472,10 +1608,10 @@ static ibtfo_status step_host_banded(ibtfo_case *c, const double *u_in, double *
     for (int k = 0; k < NBANDS; k++)
     {
         CK(cudaStreamWaitEvent(c->stream, c->ev_in[k], 0));
-        launch_aos_to_cur_rows(c->staging, c->buf[0], c->buf[1], c->st, g, c->band_rows[k], c->band_rows[k + 1],
-                               c->stream);
+        launch_aos_to_cur_boxes(c->staging, c->buf[0], c->buf[1], c->st, g, chunk_boxes(c, k, boxes), k == 0, true,
+                                c->stream);
         CK(cudaEventRecord(c->ev_conv[k], c->stream));
-        cudaStream_t s = c->sw[k & 1];
+        cudaStream_t s = c->sw[k % NSW];
         CK(cudaStreamWaitEvent(s, c->ev_conv[k], 0));
         const int t0 = c->band_tiles[k], t1 = c->band_tiles[k + 1];
         if (t1 > t0)
@@ -1500,7 +1636,7 @@ static ibtfo_status step_host_banded(ibtfo_case *c, const double *u_in, double *
     }
     // the domain edges once every band and every ghost cell is done (periodic
     // edges copy interior cells, ghost cells included)
-    for (int q = 0; q < 2; q++)
+    for (int q = 0; q < NSW; q++)
     {
         CK(cudaEventRecord(c->ev_sw[q], c->sw[q]));
         CK(cudaStreamWaitEvent(c->stream, c->ev_sw[q], 0));
@@ -1518,6 +1654,11 @@ static ibtfo_status step_host_banded(ibtfo_case *c, const double *u_in, double *
     return IBTFO_OK;
 }
 
+// The PVRS solvers read, for a Y face, the state of cell 7 c + 2 (the
+// reference's stray scratch store): anywhere in the array, so their in-place
+// steps copy every row in.
+static bool boxes_apply(const ibtfo_case *c) { return c->cfg.riemann != IBTFO_RIEMANN_PVRS; }
+
 ibtfo_status ibtfo_step_host_bytes(const ibtfo_case *c, int in_place, long long *h2d, long long *d2h)
 {
     if (!c || !h2d || !d2h)
@@ -1528,6 +1669,16 @@ ibtfo_status ibtfo_step_host_bytes(const ibtfo_case *c, int in_place, long long 
     const long long cell = sizeof(double) * 4;
     *h2d = cell * g.M * g.N;
     const bool banded = !c->ccm && c->cfg.time_advance == IBTFO_TIME_SINGLESTEP;
+    if (banded && in_place && boxes_apply(c))
+    {
+        *h2d = 0;
+        for (int k = 0; k < NBANDS; k++)
+        {
+            const HostBoxes &b = c->in_boxes[k];
+            for (int q = 0; q < b.n; q++)
+                *h2d += cell * (long long)(b.r1[q] - b.r0[q]) * (b.c1[q] - b.c0[q]);
+        }
+    }
     long long out = cell * g.M * g.N;
     if (banded)
     {
@@ -1569,6 +1720,27 @@ ibtfo_status ibtfo_step_host(ibtfo_case *c, const double *u_in, double *u_out, i
         cudaGetLastError();
     }
     ibtfo_status st = IBTFO_OK;
+    bool boxes = false;
+    if (banded && u_in == u_out && boxes_apply(c))
+    {
+        if (c->mirror_in != u_in)
+        {
+            // the first in-place step on this array since the device state was
+            // last written from elsewhere: every row in, so that the cells
+            // later steps do not copy agree with the array
+            CK(cudaEventRecord(c->ev_done, c->stream));
+            for (cudaStream_t s : helper_streams(c))
+                CK(cudaStreamWaitEvent(s, c->ev_done, 0));
+            st = step_host_banded(c, u_in, u_out, false);
+            if (st != IBTFO_OK)
+                return st;
+            CK(cudaGetLastError());
+            c->mirror_in = u_in;
+            ibtfo_progress q;
+            return ibtfo_get_progress(c, p ? p : &q);
+        }
+        boxes = true;
+    }
     if (graph && (c->host_graph_in != u_in || c->host_graph_out != u_out || !c->host_graph))
     {
         if (c->host_graph)
@@ -1578,9 +1750,9 @@ ibtfo_status ibtfo_step_host(ibtfo_case *c, const double *u_in, double *u_out, i
         long long before = g_launches.load();
         CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
         cudaEventRecord(c->ev_done, c->stream);
-        for (cudaStream_t s : {c->h2d, c->d2h, c->sw[0], c->sw[1], c->fin})
+        for (cudaStream_t s : helper_streams(c))
             cudaStreamWaitEvent(s, c->ev_done, 0);
-        st = step_host_banded(c, u_in, u_out);
+        st = step_host_banded(c, u_in, u_out, boxes);
         c->host_graph_launches = g_launches.load() - before;
         g_launches.store(before); // counted when replayed
         cudaError_t e = cudaStreamEndCapture(c->stream, &gr);
@@ -1604,9 +1776,9 @@ ibtfo_status ibtfo_step_host(ibtfo_case *c, const double *u_in, double *u_out, i
     {
         // every helper stream starts after what is already queued on the case's stream
         CK(cudaEventRecord(c->ev_done, c->stream));
-        for (cudaStream_t s : {c->h2d, c->d2h, c->sw[0], c->sw[1], c->fin})
+        for (cudaStream_t s : helper_streams(c))
             CK(cudaStreamWaitEvent(s, c->ev_done, 0));
-        st = banded ? step_host_banded(c, u_in, u_out) : step_host_plain(c, u_in, u_out);
+        st = banded ? step_host_banded(c, u_in, u_out, boxes) : step_host_plain(c, u_in, u_out);
         if (st != IBTFO_OK)
             return st;
     }

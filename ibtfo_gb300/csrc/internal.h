@@ -215,10 +215,19 @@ void launch_reduce(const ReduceArgs &a, int nblocks_max, cudaStream_t s);
 void launch_aos_to_soa(const double *aos, double *soa, const GridDesc &g, cudaStream_t s);
 void launch_soa_to_aos(const double *soa, double *aos, const GridDesc &g, cudaStream_t s);
 // rows [r0, r1) of the current state buffer (picked on the device by st->cur)
-void launch_aos_to_cur_rows(const double *aos, double *b0, double *b1, const DevState *st, const GridDesc &g, int r0,
-                            int r1, cudaStream_t s);
 void launch_cur_to_aos_rows(const double *b0, const double *b1, const DevState *st, double *aos, const GridDesc &g,
                             int r0, int r1, cudaStream_t s);
+// up to five boxes of array rows [r0, r1) x columns [c0, c1) of one transfer chunk
+struct HostBoxes
+{
+    int n;
+    int r0[5], r1[5], c0[5], c1[5];
+};
+// the boxes from the host-layout array into the current state buffer (and,
+// with `both`, into the other buffer too); `first` records st->cur as the
+// step's input buffer (st->step_cur)
+void launch_aos_to_cur_boxes(const double *aos, double *b0, double *b1, const DevState *st, const GridDesc &g,
+                             const HostBoxes &bx, bool first, bool both, cudaStream_t s);
 // rows [r0, r1), columns [c0, c1) of a step in flight: fluid and ghost-fluid
 // cells from the step's output buffer (the ghost cells of these rows are
 // filled by then), the rest from its input (st->step_cur)

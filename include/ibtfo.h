@@ -204,11 +204,20 @@ ibtfo_status ibtfo_put_state(ibtfo_case *c, const double *u_old);
  * result and fills `p` (may be NULL).  The transfers go in row chunks on two
  * copy streams, overlapped with the layout conversion and the sweep (rows of
  * the sweep start once their stencil is on the device): from page-locked
- * host memory the copies run concurrently with the kernels. */
+ * host memory the copies run concurrently with the kernels.
+ * In place (u_out == u_in) a step copies back only the cells it can change,
+ * and from the second call on the same array (with no ibtfo_set_state,
+ * ibtfo_put_state, ibtfo_init_x_split or ibtfo_load_checkpoint in between)
+ * copies in only the cells it reads: the fluid cells with two cells around
+ * them, the ghost cells and the domain edge (PVRS solvers: every row).  The
+ * result in the array is the same; the device copy of the cells no step
+ * reads (solid cells away from the fluid) keeps the values the array held
+ * at the first call. */
 ibtfo_status ibtfo_step_host(ibtfo_case *c, const double *u_in, double *u_out, ibtfo_progress *p);
-/* Bytes one ibtfo_step_host call moves each way.  In place (u_out == u_in)
- * only the cells a step can change go back: the interior rows of the
- * columns holding fluid cells, plus the ghost cells and the domain ring. */
+/* Bytes one ibtfo_step_host call moves each way (in place: a call after the
+ * first on the same array).  In place only the cells a step can change go
+ * back: the interior rows of the columns holding fluid cells, plus the ghost
+ * cells and the domain ring. */
 ibtfo_status ibtfo_step_host_bytes(const ibtfo_case *c, int in_place, long long *h2d, long long *d2h);
 
 /* Queues `nsteps` iterations of the reference loop body (Sod.cpp:154-177:

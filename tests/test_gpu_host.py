@@ -212,7 +212,8 @@ def test_pinned_buffers_move_the_same_bytes_as_pageable_ones(precision):
 
 
 @pytest.mark.parametrize("kind,precision", [("channel", "fp64_fast"), ("channel", "fp64"), ("channel", "fp32c"),
-                                            ("channel_rk2", "fp64_fast"), ("ccm", "fp32c"), ("sod", "fp64")])
+                                            ("channel_rk2", "fp64_fast"), ("channel_pvrs", "fp64"), ("ccm", "fp32c"),
+                                            ("sod", "fp64")])
 @pytest.mark.parametrize("in_place,pinned", [(True, True), (False, True), (True, False)])
 def test_step_host_equals_put_step_get(kind, precision, in_place, pinned):
     """ibtfo_step_host (row-chunked copies overlapped with the banded sweep,
@@ -225,6 +226,8 @@ def test_step_host_equals_put_step_get(kind, precision, in_place, pinned):
         g = w.grid
         phi = _c.channel_phi(g)
         kw = dict(precision=precision, time="RK2" if kind.endswith("rk2") else "SingleStep")
+        if kind.endswith("pvrs"):
+            kw["riemann"] = "PVRS"
 
         def make():
             c = ib.Case.from_workload(w, **kw)
@@ -276,3 +279,79 @@ def test_step_host_equals_put_step_get(kind, precision, in_place, pinned):
     for (ur, pr), (ug, pg) in zip(ref, got):
         assert np.array_equal(ur, ug, equal_nan=True)
         assert pr == pg
+
+
+def test_step_host_in_place_copies_in_only_what_the_step_reads():
+    """In place, the calls after the first copy in only the cells a step
+    reads (the fluid cells and two cells around them, the ghost cells, the
+    domain edge).  A value the caller writes into a solid cell away from the
+    fluid stays in the array and changes nothing else: the array after three
+    more steps equals put + step + get of the modified array."""
+    from ibtfo_gb300 import cases as _c
+    w = _c.inclined_channel(512, 256)
+    g = w.grid
+    phi = _c.channel_phi(g)
+
+    def make():
+        c = ib.Case.from_workload(w, precision="fp64_fast")
+        c.setup_geometry(phi)
+        c.set_state(_c.channel_init(g, c.cell_types(), w.gamma))
+        return c
+
+    n = g.M * g.N * 4
+    pin = ib.PinnedBuffer(n)
+    try:
+        with make() as b:
+            full_in, _ = b.step_host_bytes(in_place=False)
+            box_in, _ = b.step_host_bytes(in_place=True)
+            assert box_in < 0.6 * full_in, (box_in, full_in)
+            types = b.cell_types().reshape(g.N, g.M)
+            j, i = g.N // 2, 2 * g.ng + 1  # solid, far from the channel and from the domain edge
+            assert (types[j, g.ng: i + 40] == 1).all()
+            b.get_state_ptr(pin.ptr)
+            b.step_host_ptr(pin.ptr, pin.ptr)  # first call on the array: every row in
+            b.step_host_ptr(pin.ptr, pin.ptr)
+            u = pin.array.reshape(g.N, g.M, 4)
+            u[j, i] = (7.0, 0.5, -0.25, 30.0)
+            start = pin.array.copy()
+            for _ in range(3):
+                p = b.step_host_ptr(pin.ptr, pin.ptr)
+            got = pin.array.copy()
+        with make() as a:
+            ua = a.get_state()
+            for k in range(5):
+                if k == 2:
+                    assert np.array_equal(np.delete(ua.reshape(-1, 4), j * g.M + i, axis=0),
+                                          np.delete(start.reshape(-1, 4), j * g.M + i, axis=0))
+                    ua = start  # the same state with the modified solid cell
+                a.put_state_ptr(ua.ctypes.data)
+                a.step()
+                ua = a.get_state()
+            pa = a.progress()
+        assert np.array_equal(got, ua, equal_nan=True)
+        assert tuple(got.reshape(g.N, g.M, 4)[j, i]) == (7.0, 0.5, -0.25, 30.0)
+        assert p["mass"] == pa["mass"] and p["dt"] == pa["dt"]
+    finally:
+        pin.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+def test_put_state_solid_cells_stay_through_steps(precision):
+    """A step copies U_NEW into U_OLD for fluid cells only
+    (IDWBaseGFM/GFM_Bound.cpp:24-35): a solid cell written by ibtfo_put_state
+    keeps its value through the following steps."""
+    from ibtfo_gb300 import cases as _c
+    w = _c.inclined_channel(256, 128)
+    g = w.grid
+    with ib.Case.from_workload(w, precision=precision) as c:
+        c.setup_geometry(_c.channel_phi(g))
+        c.set_state(_c.channel_init(g, c.cell_types(), w.gamma))
+        c.advance(3)
+        u = c.get_state().reshape(g.N, g.M, 4)
+        j, i = g.N // 2, 2 * g.ng + 1
+        assert c.cell_types().reshape(g.N, g.M)[j, i] == 1
+        u[j, i] = (7.0, 0.5, -0.25, 30.0)
+        c.put_state(u.reshape(-1))
+        for _ in range(3):
+            c.advance(1)
+            assert tuple(c.get_state().reshape(g.N, g.M, 4)[j, i]) == (7.0, 0.5, -0.25, 30.0)
