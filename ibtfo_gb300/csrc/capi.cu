@@ -24,15 +24,17 @@ namespace ibtfo {
 SweepLaunch sweep_launcher_muscl(int riemann, int limiter);
 SweepLaunch sweep_launcher_mhm(int riemann, int limiter);
 SweepLaunch sweep_launcher_godunov(int riemann, int limiter);
-SweepLaunch sweep_launcher_muscl_fast(int riemann, int limiter);
-SweepLaunch sweep_launcher_mhm_fast(int riemann, int limiter);
-SweepLaunch sweep_launcher_godunov_fast(int riemann, int limiter);
+SweepLaunch sweep_launcher_muscl_fast(int riemann, int limiter, int ty);
+SweepLaunch sweep_launcher_mhm_fast(int riemann, int limiter, int ty);
+SweepLaunch sweep_launcher_godunov_fast(int riemann, int limiter, int ty);
 SweepLaunch sweep_launcher_muscl_f32(int riemann, int limiter);
 SweepLaunch sweep_launcher_mhm_f32(int riemann, int limiter);
 SweepLaunch sweep_launcher_godunov_f32(int riemann, int limiter);
 SweepLaunch sweep_launcher_lax();
 
-SweepLaunch sweep_launcher(int scheme, int riemann, int limiter, int precision)
+// the sweep of a case's configuration over TILE_X x ty tiles (ty = TILE_Y
+// or, for the fp64_fast sweeps without PVRS, FAST_TILE_Y)
+SweepLaunch sweep_launcher(int scheme, int riemann, int limiter, int precision, int ty)
 {
     const int r = (riemann == HLLC) ? HLL : riemann; // HLLC/Riemann_solver.cpp is HLL
     const bool fast = (precision == IBTFO_PRECISION_FP64_FAST);
@@ -49,9 +51,9 @@ SweepLaunch sweep_launcher(int scheme, int riemann, int limiter, int precision)
     }
     switch (scheme)
     {
-    case MHM: return fast ? sweep_launcher_mhm_fast(r, limiter) : sweep_launcher_mhm(r, limiter);
-    case GODUNOV: return fast ? sweep_launcher_godunov_fast(r, limiter) : sweep_launcher_godunov(r, limiter);
-    default: return fast ? sweep_launcher_muscl_fast(r, limiter) : sweep_launcher_muscl(r, limiter);
+    case MHM: return fast ? sweep_launcher_mhm_fast(r, limiter, ty) : sweep_launcher_mhm(r, limiter);
+    case GODUNOV: return fast ? sweep_launcher_godunov_fast(r, limiter, ty) : sweep_launcher_godunov(r, limiter);
+    default: return fast ? sweep_launcher_muscl_fast(r, limiter, ty) : sweep_launcher_muscl(r, limiter);
     }
 }
 
@@ -126,9 +128,16 @@ struct ibtfo_case
     double *partial = nullptr;
     double *ring_ic = nullptr; // [2][2*ng][4]
     int tma = 0;                // tensor maps of buf[0], buf[1] below are valid
-    CUtensorMap tmap[2];
-    unsigned *tiles = nullptr; // active sweep tiles
+    CUtensorMap tmap[2];        // boxes of TILE_X x tile_y cells and their halo
+    CUtensorMap tmap8[2];       // boxes of TILE_X x TILE_Y cells (the host step's bands)
+    unsigned *tiles = nullptr;  // active sweep tiles (TILE_X x tile_y)
     int ntiles = 0;
+    // the host step's bands sweep TILE_X x TILE_Y tiles (shorter CTAs fill and
+    // drain the band pipeline faster): their list when tile_y differs, and
+    // the launcher for them
+    unsigned *tiles8 = nullptr;
+    int ntiles8 = 0;
+    SweepLaunch sweep8 = nullptr;
     // cut cells (BC_CCM): volume fractions, apertures, small-cell mixing lists
     double *alpha = nullptr, *ax = nullptr, *ay = nullptr;
     MixExchange *mix_ex = nullptr;
@@ -140,6 +149,7 @@ struct ibtfo_case
     int nblocks = 0;
     bool geometry = false, state = false;
     SweepLaunch sweep = nullptr;
+    int tile_y = TILE_Y; // rows of the sweep's tiles (TILE_X columns)
     cudaGraphExec_t graph = nullptr;
     int graph_steps = 0;
     long long graph_launches = 0; // kernel launches in one replay of the graph
@@ -200,7 +210,8 @@ static void drop_graphs(ibtfo_case *c)
 static void make_bands(ibtfo_case *c, const std::vector<unsigned> &tiles)
 {
     const GridDesc &g = c->g;
-    const int nty = (g.n_y + TILE_Y - 1) / TILE_Y;
+    const int TY = TILE_Y;
+    const int nty = (g.n_y + TY - 1) / TY;
     c->band_rows.assign(NBANDS + 1, 0);
     c->out_rows.assign(NBANDS + 1, 0);
     c->band_tiles.assign(NBANDS + 1, 0);
@@ -211,8 +222,8 @@ static void make_bands(ibtfo_case *c, const std::vector<unsigned> &tiles)
         // the first and the last band half as tall as the others: the
         // pipeline waits for the first chunk alone and drains the last one alone
         const int tb = (k == NBANDS) ? nty : (int)((long long)(2 * k - 1) * nty / (2 * NBANDS - 2));
-        c->band_rows[k] = (k == NBANDS) ? g.N : std::min(g.N, g.ng + tb * TILE_Y + 2);
-        c->out_rows[k] = (k == NBANDS) ? g.N : std::min(g.N, g.ng + tb * TILE_Y);
+        c->band_rows[k] = (k == NBANDS) ? g.N : std::min(g.N, g.ng + tb * TY + 2);
+        c->out_rows[k] = (k == NBANDS) ? g.N : std::min(g.N, g.ng + tb * TY);
         while (t < tiles.size() && (int)(tiles[t] >> 16) < tb)
             t++;
         c->band_tiles[k] = (k == NBANDS) ? (int)tiles.size() : (int)t;
@@ -396,13 +407,17 @@ static int make_state_tmaps(ibtfo_case *c)
     const cuuint64_t elem = f32 ? sizeof(float) : sizeof(double);
     const cuuint64_t dims[3] = {(cuuint64_t)g.M, (cuuint64_t)g.N, 4};
     const cuuint64_t strides[2] = {(cuuint64_t)g.pitch * elem, (cuuint64_t)g.plane * elem};
-    const cuuint32_t box[3] = {TILE_X + 4, TILE_Y + 4, 4};
     const cuuint32_t estr[3] = {1, 1, 1};
-    for (int b = 0; b < 2; b++)
-        if (encode(&c->tmap[b], f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, c->buf[b],
-                   dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                   CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-            return 0;
+    for (int h = 0; h < 2; h++)
+    {
+        const cuuint32_t box[3] = {TILE_X + 4, (cuuint32_t)(h ? TILE_Y : c->tile_y) + 4, 4};
+        CUtensorMap *maps = h ? c->tmap8 : c->tmap;
+        for (int b = 0; b < 2; b++)
+            if (encode(&maps[b], f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3,
+                       c->buf[b], dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                       CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+                return 0;
+    }
     return 1;
 }
 
@@ -488,7 +503,7 @@ ibtfo_status ibtfo_destroy(ibtfo_case *c)
     // device-wide synchronisation (other cases keep running)
     cudaStream_t fs = c->own ? c->own : c->stream;
     void *bufs[] = {c->buf[0], c->buf[1], c->ic, c->staging, c->phi, c->nx, c->ny, c->type, c->ghosts,
-                    c->st, c->partial, c->ring_ic, c->tiles, c->alpha, c->ax, c->ay, c->mix_ex, c->mix_part,
+                    c->st, c->partial, c->ring_ic, c->tiles, c->tiles8, c->alpha, c->ax, c->ay, c->mix_ex, c->mix_part,
                     c->mix_links, c->mix_e};
     for (void *p : bufs)
         if (p)
@@ -551,7 +566,14 @@ ibtfo_status ibtfo_create(const ibtfo_config *cfg, ibtfo_case **out)
     g.f32 = (k.precision == IBTFO_PRECISION_FP32_COMPENSATED) ? 1 : 0;
     set_derived_constants(g);
     c->nblocks = ((k.n_x + TILE_X - 1) / TILE_X) * ((k.n_y + TILE_Y - 1) / TILE_Y);
-    c->sweep = sweep_launcher(k.scheme, k.riemann, k.limiter, k.precision);
+    // rows per tile: the fp64_fast sweeps run 32 x FAST_TILE_Y tiles except
+    // with PVRS; Lax, the strict and FP32 forms and the cut-cell kernels 32x8
+    c->tile_y = (k.precision == IBTFO_PRECISION_FP64_FAST && k.scheme != IBTFO_SCHEME_LAX &&
+                 k.boundary != IBTFO_BOUNDARY_CCM && k.riemann != IBTFO_RIEMANN_PVRS)
+                    ? FAST_TILE_Y
+                    : TILE_Y;
+    c->sweep = sweep_launcher(k.scheme, k.riemann, k.limiter, k.precision, c->tile_y);
+    c->sweep8 = c->tile_y == TILE_Y ? c->sweep : sweep_launcher(k.scheme, k.riemann, k.limiter, k.precision, TILE_Y);
     if (k.boundary == IBTFO_BOUNDARY_CCM)
         c->ccm = ccm_launcher(k.scheme, k.riemann, k.limiter, k.precision);
 
@@ -652,7 +674,18 @@ static ibtfo_status geometry_from_phi(ibtfo_case *c)
         rc = setup_geometry(g, c->cfg.boundary, c->phi, c->nx, c->ny, c->type, &c->ghosts, &c->nghost, c->stream);
     std::vector<unsigned> tile_list;
     if (rc == 0)
-        rc = active_tiles(g, c->type, &c->tiles, &c->ntiles, c->stream, &tile_list);
+        rc = active_tiles(g, c->type, TILE_Y, &c->tiles8, &c->ntiles8, c->stream, &tile_list);
+    if (rc == 0 && c->tile_y != TILE_Y)
+        rc = active_tiles(g, c->type, c->tile_y, &c->tiles, &c->ntiles, c->stream);
+    else if (rc == 0)
+    {
+        std::swap(c->tiles, c->tiles8); // one list: the sweep's, tiles8 left empty
+        if (c->tiles8)
+            cudaFreeAsync(c->tiles8, c->stream);
+        c->tiles8 = nullptr;
+        c->ntiles = c->ntiles8;
+        c->ntiles8 = 0;
+    }
     if (rc == 0)
     {
         make_bands(c, tile_list);
@@ -833,7 +866,7 @@ static void enqueue_advance(ibtfo_case *c, int guard)
         a.alpha = c->alpha;
         a.ax = c->ax;
         a.ay = c->ay;
-        c->ccm(a, dim3(c->ntiles), dim3(TILE_X * TILE_Y), c->stream);
+        c->ccm(a, dim3(c->ntiles), dim3(TILE_X * TILE_Y), c->stream); // cut-cell cases: 32x8 tiles
         count_launch();
         MixArgs m{};
         m.g = c->g;
@@ -1577,8 +1610,15 @@ static ibtfo_status step_host_banded(ibtfo_case *c, const double *u_in, double *
         }
         CK(cudaEventRecord(c->ev_in[k], c->h2d));
     }
+    // the bands sweep TILE_X x TILE_Y tiles
     SweepArgs a = sweep_args(c, 0);
-    a.nblocks = c->ntiles;
+    if (c->tiles8)
+    {
+        a.tiles = c->tiles8;
+        a.tmap[0] = c->tmap8[0];
+        a.tmap[1] = c->tmap8[1];
+    }
+    a.nblocks = c->tiles8 ? c->ntiles8 : c->ntiles;
     FillArgs f = fill_args(c);
     const bool gfm = c->cfg.boundary != IBTFO_BOUNDARY_REGULAR;
     auto finish = [&](int k) -> ibtfo_status {
@@ -1617,7 +1657,7 @@ static ibtfo_status step_host_banded(ibtfo_case *c, const double *u_in, double *
         if (t1 > t0)
         {
             a.tile0 = t0;
-            c->sweep(a, dim3(t1 - t0), dim3(TILE_X * TILE_Y), s);
+            c->sweep8(a, dim3(t1 - t0), dim3(TILE_X * TILE_Y), s);
             count_launch();
         }
         CK(cudaEventRecord(c->ev_swept[k], s));

@@ -292,11 +292,11 @@ int active_tile_list(const GridDesc &g, const uint8_t *d_type, int tx, int ty, s
     return 0;
 }
 
-int active_tiles(const GridDesc &g, const uint8_t *d_type, unsigned **d_tiles, int *ntiles, cudaStream_t s,
+int active_tiles(const GridDesc &g, const uint8_t *d_type, int ty, unsigned **d_tiles, int *ntiles, cudaStream_t s,
                  std::vector<unsigned> *host_list)
 {
     std::vector<unsigned> list;
-    int rc = active_tile_list(g, d_type, TILE_X, TILE_Y, list, s);
+    int rc = active_tile_list(g, d_type, TILE_X, ty, list, s);
     if (rc)
         return rc;
     if (host_list)

@@ -206,6 +206,11 @@ typedef void (*SweepLaunch)(const SweepArgs &, dim3 grid, dim3 block, cudaStream
 // sweep tile (interior cells per CTA)
 constexpr int TILE_X = 32;
 constexpr int TILE_Y = 8;
+// Rows of the fp64_fast sweep's tiles (not with the PVRS solvers, whose 158
+// registers leave room for one 32x8 tile per SM at most): a 32x16 tile solves
+// 2.16 faces per cell where a 32x8 tile solves 2.28, and stages 1.41 cells
+// per cell, not 1.69.  Every sweep CTA has TILE_X x TILE_Y threads.
+constexpr int FAST_TILE_Y = 16;
 
 SweepLaunch sweep_launcher(int scheme, int riemann, int limiter, int precision);
 void launch_fill(const FillArgs &a, cudaStream_t s);
@@ -319,7 +324,8 @@ int vtk_writer_wait(VtkWriter *w, std::string *why);
 void vtk_writer_destroy(VtkWriter *w, cudaStream_t s);
 
 // geometry set-up (geometry.cu)
-int active_tiles(const GridDesc &g, const uint8_t *d_type, unsigned **d_tiles, int *ntiles, cudaStream_t s,
+// the tiles of TILE_X x ty cells holding fluid cells, on the device and (host_list) on the host
+int active_tiles(const GridDesc &g, const uint8_t *d_type, int ty, unsigned **d_tiles, int *ntiles, cudaStream_t s,
                  std::vector<unsigned> *host_list = nullptr);
 // host list of the tx x ty tiles holding at least one fluid cell (bx | by << 16);
 // 0, or 2 (allocation) / 5 (CUDA error)

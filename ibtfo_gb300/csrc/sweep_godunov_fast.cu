@@ -1,19 +1,28 @@
-// Instantiations of the fused sweep for Scheme=GODUNOV, fp64_fast (compiled with contraction).
+// Instantiations of the fused sweep for Scheme=GODUNOV, fp64_fast (compiled with contraction):
+// 32x16 tiles (FAST_TILE_Y rows) or 32x8, 32x8 with the PVRS solvers.
 // One translation unit per scheme and precision so the library builds in parallel.
 #include "sweep_impl.cuh"
 
 namespace ibtfo {
 
-SweepLaunch sweep_launcher_godunov_fast(int riemann, int limiter)
+template <int TY>
+static SweepLaunch select(int riemann, bool vl)
 {
-    const bool vl = (limiter == VANLEER);
     switch (riemann)
     {
     case PVRS: return vl ? &launch_sweep<GODUNOV, PVRS, VANLEER, 1> : &launch_sweep<GODUNOV, PVRS, MINMOD, 1>;
-    case SW: return vl ? &launch_sweep<GODUNOV, SW, VANLEER, 1> : &launch_sweep<GODUNOV, SW, MINMOD, 1>;
-    case HLLCT: return vl ? &launch_sweep<GODUNOV, HLLCT, VANLEER, 1> : &launch_sweep<GODUNOV, HLLCT, MINMOD, 1>;
-    default: return vl ? &launch_sweep<GODUNOV, HLL, VANLEER, 1> : &launch_sweep<GODUNOV, HLL, MINMOD, 1>;
+    case SW: return vl ? prepared_sweep_launcher<GODUNOV, SW, VANLEER, 1, TY>() : prepared_sweep_launcher<GODUNOV, SW, MINMOD, 1, TY>();
+    case HLLCT: return vl ? prepared_sweep_launcher<GODUNOV, HLLCT, VANLEER, 1, TY>() : prepared_sweep_launcher<GODUNOV, HLLCT, MINMOD, 1, TY>();
+    default: return vl ? prepared_sweep_launcher<GODUNOV, HLL, VANLEER, 1, TY>() : prepared_sweep_launcher<GODUNOV, HLL, MINMOD, 1, TY>();
     }
+}
+
+SweepLaunch sweep_launcher_godunov_fast(int riemann, int limiter, int ty)
+{
+    const bool vl = (limiter == VANLEER);
+    if (ty == TILE_Y || riemann == PVRS)
+        return select<TILE_Y>(riemann, vl);
+    return select<FAST_TILE_Y>(riemann, vl);
 }
 
 } // namespace ibtfo

@@ -84,7 +84,10 @@ def test_batch_equals_alone(precision, shape):
         prog = b.progress()
         b.synchronize()
         for k, c in enumerate(cs):
-            same((c.get_state(), c.progress()), ref[k], exact_mass=(shape == "32x8"))
+            # the mass sum is bit for bit where the batch's tiles are the case
+            # path's (32x16 for fp64_fast, 32x8 for the FP32 form)
+            same((c.get_state(), c.progress()), ref[k],
+                 exact_mass=(shape == ("32x16" if precision == "fp64_fast" else "32x8")))
             assert prog[k][0]["iter"] == ref[k][1]["iter"]
             assert ref[k][1]["nan_cells"] == 0
     # the short case stopped at its own t_end; the others ran every step

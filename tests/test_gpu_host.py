@@ -22,6 +22,14 @@ def _p(a):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
 
+def same_progress(a, b):
+    """Loop scalars equal; the mass to 1e-14 relative: fp64_fast sums it over
+    32x16 tiles in ibtfo_step and over the 32x8 tiles of the host step's row
+    bands, an order that changes its last bits."""
+    assert {k: v for k, v in a.items() if k != "mass"} == {k: v for k, v in b.items() if k != "mass"}
+    assert abs(a["mass"] - b["mass"]) <= 1e-14 * abs(b["mass"]), (a["mass"], b["mass"])
+
+
 def rel_linf(a, b):
     a, b = a.reshape(-1, 4), b.reshape(-1, 4)
     worst = 0.0
@@ -218,8 +226,8 @@ def test_pinned_buffers_move_the_same_bytes_as_pageable_ones(precision):
 def test_step_host_equals_put_step_get(kind, precision, in_place, pinned):
     """ibtfo_step_host (row-chunked copies overlapped with the banded sweep,
     replayed as a CUDA graph for page-locked arrays) leaves the same state,
-    progress and output bytes as ibtfo_put_state + ibtfo_step +
-    ibtfo_get_state, step after step."""
+    output bytes and loop scalars (the mass to its summation order) as
+    ibtfo_put_state + ibtfo_step + ibtfo_get_state, step after step."""
     from ibtfo_gb300 import cases as _c
     if kind.startswith("channel"):
         w = _c.inclined_channel(512, 256)
@@ -278,7 +286,7 @@ def test_step_host_equals_put_step_get(kind, precision, in_place, pinned):
         assert np.array_equal(b.get_state(), got[-1][0], equal_nan=True)
     for (ur, pr), (ug, pg) in zip(ref, got):
         assert np.array_equal(ur, ug, equal_nan=True)
-        assert pr == pg
+        same_progress(pr, pg)
 
 
 def test_step_host_in_place_copies_in_only_what_the_step_reads():
@@ -330,7 +338,7 @@ def test_step_host_in_place_copies_in_only_what_the_step_reads():
             pa = a.progress()
         assert np.array_equal(got, ua, equal_nan=True)
         assert tuple(got.reshape(g.N, g.M, 4)[j, i]) == (7.0, 0.5, -0.25, 30.0)
-        assert p["mass"] == pa["mass"] and p["dt"] == pa["dt"]
+        same_progress(p, pa)
     finally:
         pin.close()
 
