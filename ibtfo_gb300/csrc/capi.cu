@@ -27,9 +27,9 @@ SweepLaunch sweep_launcher_godunov(int riemann, int limiter);
 SweepLaunch sweep_launcher_muscl_fast(int riemann, int limiter, int ty);
 SweepLaunch sweep_launcher_mhm_fast(int riemann, int limiter, int ty);
 SweepLaunch sweep_launcher_godunov_fast(int riemann, int limiter, int ty);
-SweepLaunch sweep_launcher_muscl_f32(int riemann, int limiter);
-SweepLaunch sweep_launcher_mhm_f32(int riemann, int limiter);
-SweepLaunch sweep_launcher_godunov_f32(int riemann, int limiter);
+SweepLaunch sweep_launcher_muscl_f32(int riemann, int limiter, int ty);
+SweepLaunch sweep_launcher_mhm_f32(int riemann, int limiter, int ty);
+SweepLaunch sweep_launcher_godunov_f32(int riemann, int limiter, int ty);
 SweepLaunch sweep_launcher_lax();
 
 // the sweep of a case's configuration over TILE_X x ty tiles (ty = TILE_Y
@@ -44,9 +44,9 @@ SweepLaunch sweep_launcher(int scheme, int riemann, int limiter, int precision, 
     {
         switch (scheme)
         {
-        case MHM: return sweep_launcher_mhm_f32(r, limiter);
-        case GODUNOV: return sweep_launcher_godunov_f32(r, limiter);
-        default: return sweep_launcher_muscl_f32(r, limiter);
+        case MHM: return sweep_launcher_mhm_f32(r, limiter, ty);
+        case GODUNOV: return sweep_launcher_godunov_f32(r, limiter, ty);
+        default: return sweep_launcher_muscl_f32(r, limiter, ty);
         }
     }
     switch (scheme)
@@ -566,10 +566,10 @@ ibtfo_status ibtfo_create(const ibtfo_config *cfg, ibtfo_case **out)
     g.f32 = (k.precision == IBTFO_PRECISION_FP32_COMPENSATED) ? 1 : 0;
     set_derived_constants(g);
     c->nblocks = ((k.n_x + TILE_X - 1) / TILE_X) * ((k.n_y + TILE_Y - 1) / TILE_Y);
-    // rows per tile: the fp64_fast sweeps run 32 x FAST_TILE_Y tiles except
-    // with PVRS; Lax, the strict and FP32 forms and the cut-cell kernels 32x8
-    c->tile_y = (k.precision == IBTFO_PRECISION_FP64_FAST && k.scheme != IBTFO_SCHEME_LAX &&
-                 k.boundary != IBTFO_BOUNDARY_CCM && k.riemann != IBTFO_RIEMANN_PVRS)
+    // rows per tile: the fp64_fast and FP32 sweeps run 32 x FAST_TILE_Y tiles
+    // except with PVRS; Lax, the strict form and the cut-cell kernels 32x8
+    c->tile_y = ((k.precision == IBTFO_PRECISION_FP64_FAST || k.precision == IBTFO_PRECISION_FP32_COMPENSATED) &&
+                 k.scheme != IBTFO_SCHEME_LAX && k.boundary != IBTFO_BOUNDARY_CCM && k.riemann != IBTFO_RIEMANN_PVRS)
                     ? FAST_TILE_Y
                     : TILE_Y;
     c->sweep = sweep_launcher(k.scheme, k.riemann, k.limiter, k.precision, c->tile_y);

@@ -322,13 +322,15 @@ __device__ __forceinline__ void block_reduce_finalize32(CellStats32 cs, DevState
     block_commit_finalize<NT>(amax, umax, vmax, mass, n, st, partial, g, true, false, nblocks, bid);
 }
 
-// one case: one CTA per active tile
-template <int SCH, int RIE, int LIM>
-__global__ void __launch_bounds__(TILE_X *TILE_Y, 6) sweep_f32_kernel(const __grid_constant__ SweepArgs a)
+// one case: one 256-thread CTA per active tile of TILE_X x TY cells (32x8:
+// 40 registers, 6 CTAs per SM; 32x16: 5 CTAs per SM)
+template <int SCH, int RIE, int LIM, int TY>
+__global__ void __launch_bounds__(TILE_X *TILE_Y, TY == TILE_Y ? 6 : 5)
+    sweep_f32_kernel(const __grid_constant__ SweepArgs a)
 {
     constexpr int NT = TILE_X * TILE_Y;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    auto &s = *reinterpret_cast<SweepSmem32<TILE_X, TILE_Y> *>(smem_raw);
+    auto &s = *reinterpret_cast<SweepSmem32<TILE_X, TY> *>(smem_raw);
 
     const GridDesc &g = a.g;
     DevState *st = a.st;
@@ -343,17 +345,30 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y, 6) sweep_f32_kernel(const __gr
     const unsigned bid = a.tile0 + blockIdx.x;
     const unsigned tile = a.tiles[bid];
     const int i0 = g.ng + (int)(tile & 0xFFFFu) * TILE_X;
-    const int j0 = g.ng + (int)(tile >> 16) * TILE_Y;
+    const int j0 = g.ng + (int)(tile >> 16) * TY;
     CellStats32 cs;
-    sweep_tile32<SCH, RIE, LIM, TILE_X, TILE_Y, NT>(s, g, U, V, a.type, i0, j0, dt, cs, a.stage,
-                                                    a.tma ? &a.tmap[cur] : nullptr, &st->status);
+    sweep_tile32<SCH, RIE, LIM, TILE_X, TY, NT>(s, g, U, V, a.type, i0, j0, dt, cs, a.stage,
+                                                a.tma ? &a.tmap[cur] : nullptr, &st->status);
     block_reduce_finalize32<NT>(cs, st, a.partial, g, a.nblocks ? a.nblocks : gridDim.x, bid, a.stage == 1);
 }
 
-template <int SCH, int RIE, int LIM>
+template <int SCH, int RIE, int LIM, int TY>
 void launch_sweep_f32(const SweepArgs &a, dim3 grid, dim3 block, cudaStream_t s)
 {
-    sweep_f32_kernel<SCH, RIE, LIM><<<grid, block, sizeof(SweepSmem32<TILE_X, TILE_Y>), s>>>(a);
+    sweep_f32_kernel<SCH, RIE, LIM, TY><<<grid, block, sizeof(SweepSmem32<TILE_X, TY>), s>>>(a);
+}
+
+// the launchers of one scheme over TILE_X x TY tiles (nullptr: PVRS, FP64 precisions only)
+template <int SCH, int TY>
+SweepLaunch select_f32(int riemann, bool vl)
+{
+    if (riemann == SW)
+        return vl ? &launch_sweep_f32<SCH, SW, VANLEER, TY> : &launch_sweep_f32<SCH, SW, MINMOD, TY>;
+    if (riemann == HLLCT)
+        return vl ? &launch_sweep_f32<SCH, HLLCT, VANLEER, TY> : &launch_sweep_f32<SCH, HLLCT, MINMOD, TY>;
+    if (riemann == HLL)
+        return vl ? &launch_sweep_f32<SCH, HLL, VANLEER, TY> : &launch_sweep_f32<SCH, HLL, MINMOD, TY>;
+    return nullptr;
 }
 
 } // namespace ibtfo

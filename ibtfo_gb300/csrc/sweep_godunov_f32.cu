@@ -4,16 +4,10 @@
 
 namespace ibtfo {
 
-SweepLaunch sweep_launcher_godunov_f32(int riemann, int limiter)
+SweepLaunch sweep_launcher_godunov_f32(int riemann, int limiter, int ty)
 {
     const bool vl = (limiter == VANLEER);
-    if (riemann == SW)
-        return vl ? &launch_sweep_f32<GODUNOV, SW, VANLEER> : &launch_sweep_f32<GODUNOV, SW, MINMOD>;
-    if (riemann == HLLCT)
-        return vl ? &launch_sweep_f32<GODUNOV, HLLCT, VANLEER> : &launch_sweep_f32<GODUNOV, HLLCT, MINMOD>;
-    if (riemann == HLL)
-        return vl ? &launch_sweep_f32<GODUNOV, HLL, VANLEER> : &launch_sweep_f32<GODUNOV, HLL, MINMOD>;
-    return nullptr; // PVRS: FP64 precisions only
+    return ty == TILE_Y ? select_f32<GODUNOV, TILE_Y>(riemann, vl) : select_f32<GODUNOV, FAST_TILE_Y>(riemann, vl);
 }
 
 } // namespace ibtfo

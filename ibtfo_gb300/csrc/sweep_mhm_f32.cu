@@ -4,16 +4,10 @@
 
 namespace ibtfo {
 
-SweepLaunch sweep_launcher_mhm_f32(int riemann, int limiter)
+SweepLaunch sweep_launcher_mhm_f32(int riemann, int limiter, int ty)
 {
     const bool vl = (limiter == VANLEER);
-    if (riemann == SW)
-        return vl ? &launch_sweep_f32<MHM, SW, VANLEER> : &launch_sweep_f32<MHM, SW, MINMOD>;
-    if (riemann == HLLCT)
-        return vl ? &launch_sweep_f32<MHM, HLLCT, VANLEER> : &launch_sweep_f32<MHM, HLLCT, MINMOD>;
-    if (riemann == HLL)
-        return vl ? &launch_sweep_f32<MHM, HLL, VANLEER> : &launch_sweep_f32<MHM, HLL, MINMOD>;
-    return nullptr; // PVRS: FP64 precisions only
+    return ty == TILE_Y ? select_f32<MHM, TILE_Y>(riemann, vl) : select_f32<MHM, FAST_TILE_Y>(riemann, vl);
 }
 
 } // namespace ibtfo

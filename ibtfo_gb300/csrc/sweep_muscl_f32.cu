@@ -4,16 +4,10 @@
 
 namespace ibtfo {
 
-SweepLaunch sweep_launcher_muscl_f32(int riemann, int limiter)
+SweepLaunch sweep_launcher_muscl_f32(int riemann, int limiter, int ty)
 {
     const bool vl = (limiter == VANLEER);
-    if (riemann == SW)
-        return vl ? &launch_sweep_f32<MUSCL, SW, VANLEER> : &launch_sweep_f32<MUSCL, SW, MINMOD>;
-    if (riemann == HLLCT)
-        return vl ? &launch_sweep_f32<MUSCL, HLLCT, VANLEER> : &launch_sweep_f32<MUSCL, HLLCT, MINMOD>;
-    if (riemann == HLL)
-        return vl ? &launch_sweep_f32<MUSCL, HLL, VANLEER> : &launch_sweep_f32<MUSCL, HLL, MINMOD>;
-    return nullptr; // PVRS: FP64 precisions only
+    return ty == TILE_Y ? select_f32<MUSCL, TILE_Y>(riemann, vl) : select_f32<MUSCL, FAST_TILE_Y>(riemann, vl);
 }
 
 } // namespace ibtfo

@@ -85,9 +85,8 @@ def test_batch_equals_alone(precision, shape):
         b.synchronize()
         for k, c in enumerate(cs):
             # the mass sum is bit for bit where the batch's tiles are the case
-            # path's (32x16 for fp64_fast, 32x8 for the FP32 form)
-            same((c.get_state(), c.progress()), ref[k],
-                 exact_mass=(shape == ("32x16" if precision == "fp64_fast" else "32x8")))
+            # path's (32x16 for fp64_fast and the FP32 form)
+            same((c.get_state(), c.progress()), ref[k], exact_mass=(shape == "32x16"))
             assert prog[k][0]["iter"] == ref[k][1]["iter"]
             assert ref[k][1]["nan_cells"] == 0
     # the short case stopped at its own t_end; the others ran every step
@@ -101,7 +100,8 @@ def test_batch_join_and_leave():
     precision = "fp32c"
     sp = specs()
     a, bb, cc = make(sp[0], precision), make(sp[1], precision), make(sp[2], precision)
-    with ib.Batch("MUSCL", "HLLC", "minmod", precision) as b:
+    # the case path's tiles (32x16): the mass sums bit for bit as well
+    with ib.Batch("MUSCL", "HLLC", "minmod", precision, tile_shape="32x16") as b:
         sa = b.add(a)
         b.add(bb)
         b.advance(20)

@@ -23,7 +23,7 @@ def _p(a):
 
 
 def same_progress(a, b):
-    """Loop scalars equal; the mass to 1e-14 relative: fp64_fast sums it over
+    """Loop scalars equal; the mass to 1e-14 relative: fp64_fast and FP32 sum it over
     32x16 tiles in ibtfo_step and over the 32x8 tiles of the host step's row
     bands, an order that changes its last bits."""
     assert {k: v for k, v in a.items() if k != "mass"} == {k: v for k, v in b.items() if k != "mass"}

@@ -129,7 +129,8 @@ def stream(n, seed=7):
 def test_served_results_equal_alone_runs():
     reqs = stream(10)
     bufs = {k: ib.PinnedBuffer(nx * ny) for (k, nx, ny, *_rest) in reqs}
-    with ib.Server(precision="fp32c", chunk_steps=16, tile_shape="32x8") as srv:
+    # the case path's tiles (32x16): the mass sums bit for bit as well
+    with ib.Server(precision="fp32c", chunk_steps=16, tile_shape="32x16") as srv:
         built = {}
         for (k, nx, ny, m, rf, cx, cy, arr) in reqs:
             r = shock_cylinder_request(k, nx, ny, m, rf, cx, cy, arrival=arr, density_out=bufs[k])
