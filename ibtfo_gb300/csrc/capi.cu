@@ -566,10 +566,13 @@ ibtfo_status ibtfo_create(const ibtfo_config *cfg, ibtfo_case **out)
     g.f32 = (k.precision == IBTFO_PRECISION_FP32_COMPENSATED) ? 1 : 0;
     set_derived_constants(g);
     c->nblocks = ((k.n_x + TILE_X - 1) / TILE_X) * ((k.n_y + TILE_Y - 1) / TILE_Y);
-    // rows per tile: the fp64_fast and FP32 sweeps run 32 x FAST_TILE_Y tiles
-    // except with PVRS; Lax, the strict form and the cut-cell kernels 32x8
-    c->tile_y = ((k.precision == IBTFO_PRECISION_FP64_FAST || k.precision == IBTFO_PRECISION_FP32_COMPENSATED) &&
-                 k.scheme != IBTFO_SCHEME_LAX && k.boundary != IBTFO_BOUNDARY_CCM && k.riemann != IBTFO_RIEMANN_PVRS)
+    // rows per tile: the fp64_fast and FP32 sweeps and the FP32 cut-cell sweep
+    // run 32 x FAST_TILE_Y tiles, except with PVRS; Lax, the strict form and
+    // the FP64 cut-cell sweeps 32x8 (ccm_tile_rows in csrc/ccm_impl.cuh)
+    const bool ccm = k.boundary == IBTFO_BOUNDARY_CCM;
+    const bool f32 = k.precision == IBTFO_PRECISION_FP32_COMPENSATED;
+    c->tile_y = ((k.precision == IBTFO_PRECISION_FP64_FAST && !ccm) || f32) && k.scheme != IBTFO_SCHEME_LAX &&
+                        k.riemann != IBTFO_RIEMANN_PVRS
                     ? FAST_TILE_Y
                     : TILE_Y;
     c->sweep = sweep_launcher(k.scheme, k.riemann, k.limiter, k.precision, c->tile_y);

@@ -44,11 +44,19 @@ __device__ __forceinline__ bool low_order_cell(uint8_t t) { return t == CELL_SOL
 // cells have A = 0 and a meaningless F)
 __device__ __forceinline__ double face_term(double A, double F) { return (A > 0.0) ? A * F : 0.0; }
 
+// rows of a cut-cell tile: 32x16 in the FP32 form (256 threads, two cells
+// each: fewer faces and staged cells per cell), 32x8 in FP64
+template <int PREC>
+constexpr int ccm_tile_rows()
+{
+    return PREC == 2 ? FAST_TILE_Y : TILE_Y;
+}
+
 template <int SCH, int RIE, int LIM, int PREC>
-__global__ void __launch_bounds__(TILE_X *TILE_Y) ccm_sweep_kernel(const CcmArgs ca)
+__global__ void __launch_bounds__(TILE_X *TILE_Y, PREC == 2 ? 4 : 1) ccm_sweep_kernel(const CcmArgs ca)
 {
     using T = typename std::conditional<PREC == 2, float, double>::type;
-    constexpr int TX = TILE_X, TY = TILE_Y, NT = TX * TY, WX = TX + 4, WY = TY + 4;
+    constexpr int TX = TILE_X, TY = ccm_tile_rows<PREC>(), NT = TILE_X * TILE_Y, WX = TX + 4, WY = TY + 4;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     auto &s = *reinterpret_cast<CcmSmem<T, TX, TY> *>(smem_raw);
 
@@ -165,8 +173,10 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) ccm_sweep_kernel(const CcmArgs
 
     using Stats = typename std::conditional<PREC == 2, CellStats32, CellStats>::type;
     Stats cs;
+#pragma unroll 1
+    for (int q = tid; q < TX * TY; q += NT)
     {
-        const int c = tid % TX, r = tid / TX;
+        const int c = q % TX, r = q / TX;
         const int i = i0 + c, j = j0 + r;
         const uint8_t t = s.sT[r + 2][c + 2];
         const long long o = (long long)j * pitch + i;
@@ -308,7 +318,7 @@ template <int SCH, int RIE, int LIM, int PREC>
 void launch_ccm_sweep(const CcmArgs &a, dim3 grid, dim3 block, cudaStream_t s)
 {
     using T = typename std::conditional<PREC == 2, float, double>::type;
-    ccm_sweep_kernel<SCH, RIE, LIM, PREC><<<grid, block, sizeof(CcmSmem<T, TILE_X, TILE_Y>), s>>>(a);
+    ccm_sweep_kernel<SCH, RIE, LIM, PREC><<<grid, block, sizeof(CcmSmem<T, TILE_X, ccm_tile_rows<PREC>()>), s>>>(a);
 }
 
 // every Riemann solver and limiter of one scheme and precision (the HLLC key
