@@ -212,7 +212,8 @@ constexpr int TILE_Y = 8;
 // per cell, not 1.69.  Every sweep CTA has TILE_X x TILE_Y threads.
 constexpr int FAST_TILE_Y = 16;
 
-SweepLaunch sweep_launcher(int scheme, int riemann, int limiter, int precision);
+// the sweep of a configuration over TILE_X x ty tiles (capi.cu)
+SweepLaunch sweep_launcher(int scheme, int riemann, int limiter, int precision, int ty);
 void launch_fill(const FillArgs &a, cudaStream_t s);
 // ghost records [g0, g1) of a step in flight (FillArgs.pre_flip)
 void launch_fill_ghosts(const FillArgs &a, int g0, int g1, cudaStream_t s);
