@@ -32,8 +32,8 @@ SweepLaunch sweep_launcher_mhm_f32(int riemann, int limiter, int ty);
 SweepLaunch sweep_launcher_godunov_f32(int riemann, int limiter, int ty);
 SweepLaunch sweep_launcher_lax();
 
-// the sweep of a case's configuration over TILE_X x ty tiles (ty = TILE_Y
-// or, for the fp64_fast sweeps without PVRS, FAST_TILE_Y)
+// the sweep of a case's configuration over TILE_X x ty tiles (ty = TILE_Y,
+// or FAST_TILE_Y for the fp64_fast sweeps without PVRS and the FP32 sweeps)
 SweepLaunch sweep_launcher(int scheme, int riemann, int limiter, int precision, int ty)
 {
     const int r = (riemann == HLLC) ? HLL : riemann; // HLLC/Riemann_solver.cpp is HLL
@@ -210,8 +210,7 @@ static void drop_graphs(ibtfo_case *c)
 static void make_bands(ibtfo_case *c, const std::vector<unsigned> &tiles)
 {
     const GridDesc &g = c->g;
-    const int TY = TILE_Y;
-    const int nty = (g.n_y + TY - 1) / TY;
+    const int nty = (g.n_y + TILE_Y - 1) / TILE_Y;
     c->band_rows.assign(NBANDS + 1, 0);
     c->out_rows.assign(NBANDS + 1, 0);
     c->band_tiles.assign(NBANDS + 1, 0);
@@ -222,8 +221,8 @@ static void make_bands(ibtfo_case *c, const std::vector<unsigned> &tiles)
         // the first and the last band half as tall as the others: the
         // pipeline waits for the first chunk alone and drains the last one alone
         const int tb = (k == NBANDS) ? nty : (int)((long long)(2 * k - 1) * nty / (2 * NBANDS - 2));
-        c->band_rows[k] = (k == NBANDS) ? g.N : std::min(g.N, g.ng + tb * TY + 2);
-        c->out_rows[k] = (k == NBANDS) ? g.N : std::min(g.N, g.ng + tb * TY);
+        c->band_rows[k] = (k == NBANDS) ? g.N : std::min(g.N, g.ng + tb * TILE_Y + 2);
+        c->out_rows[k] = (k == NBANDS) ? g.N : std::min(g.N, g.ng + tb * TILE_Y);
         while (t < tiles.size() && (int)(tiles[t] >> 16) < tb)
             t++;
         c->band_tiles[k] = (k == NBANDS) ? (int)tiles.size() : (int)t;
