@@ -58,3 +58,30 @@ def test_fixture_set_covers_every_variant():
         assert any(k[3] == b for k in seen), b
     assert any(k[2] == "VanLeer" for k in seen)
     assert any(k[4] == "periodic" for k in seen)
+
+
+def test_reference_step_leaves_solid_cells_as_they_are():
+    """The reference copies U_NEW into U_OLD for fluid cells only
+    (IDWBaseGFM/GFM_Bound.cpp:24-35) and rewrites the ghost cells and the
+    domain ring: every other cell keeps what the caller put there, step after
+    step.  ibtfo_put_state and the in-place ibtfo_step_host keep this."""
+    from ibtfo_gb300 import cases
+    w = cases.inclined_channel(128, 64)
+    g = w.grid
+    o = oracle.OracleCase(g.n_x, g.n_y, g.ng, (g.lo_x, g.lo_y), (g.hi_x, g.hi_y), w.gamma, w.cfl, w.scheme,
+                          w.riemann, w.limiter, w.boundary, w.gbc)
+    o.setup_geometry(cases.channel_phi(g))
+    types = o.get("XYCOORD").reshape(g.N, g.M, 6)[..., 5]
+    u0 = cases.channel_init(g, types.reshape(-1), w.gamma).reshape(g.N, g.M, 4)
+    solid = types == 1
+    solid[:2 * g.ng, :] = solid[-2 * g.ng:, :] = False  # the ring and the cells its fill reads
+    solid[:, :2 * g.ng] = solid[:, -2 * g.ng:] = False
+    assert solid.sum() > 1000
+    mark = np.array([7.0, 0.5, -0.25, 30.0])
+    u0[solid] = mark
+    o.set_initial_state(u0.reshape(-1))
+    o.run(3)
+    u = o.get("U_OLD").reshape(g.N, g.M, 4)
+    assert (u[solid] == mark).all()
+    assert not np.array_equal(u[types == 0], u0[types == 0])  # the fluid did move
+    o.close()
