@@ -364,14 +364,17 @@ class Case:
     def step_host_ptr(self, in_ptr: int, out_ptr: int):
         """One step on host buffers (raw addresses, M*N*4 doubles each; may be
         the same): put the state, step, read the new state back; returns the
-        progress."""
+        progress.  In place, from the second call on the same buffer, only
+        the cells a step reads go in and only those it can change come back;
+        solid cells keep what the buffer holds."""
         p = Progress()
         _check(lib().ibtfo_step_host(self.h, C.cast(C.c_void_p(in_ptr), _DP), C.cast(C.c_void_p(out_ptr), _DP),
                                      C.byref(p)))
         return p.as_dict()
 
     def step_host_bytes(self, in_place=True):
-        """(host-to-device, device-to-host) bytes of one step_host_ptr call."""
+        """(host-to-device, device-to-host) bytes of one step_host_ptr call
+        (in place: a call after the first on the same buffer)."""
         a, b = C.c_longlong(), C.c_longlong()
         _check(lib().ibtfo_step_host_bytes(self.h, 1 if in_place else 0, C.byref(a), C.byref(b)))
         return a.value, b.value
