@@ -67,11 +67,17 @@ def profile_run(args):
     torch.cuda.synchronize()
 
 
-def config_json(w, l2="flushed between timed steps (256 MiB write)"):
+L2_NOTE = "flushed between timed steps (256 MiB write)"
+
+
+def config_json(w):
+    """The workload, the same dict in both arms.  The arithmetic each arm
+    runs is the line's own "precision" key (the GPU arm's precision key, or
+    "fp64", the reference's strict binary64, for the reference arm)."""
     g = w.grid
     return {"workload": w.name, "n_x": g.n_x, "n_y": g.n_y, "domain": [g.lo_x, g.lo_y, g.hi_x, g.hi_y],
             "scheme": w.scheme, "riemann": w.riemann, "limiter": w.limiter, "boundary": w.boundary,
-            "cfl": w.cfl, "gamma": w.gamma, "precision": PRECISION, "l2": l2}
+            "cfl": w.cfl, "gamma": w.gamma}
 
 
 def measured_peaks():
@@ -528,7 +534,7 @@ def main():
         line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": METRIC, "n_gpus": world,
                 "steps": n, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": config_json(w, l2="n/a (host cores)"),
+                "config": config_json(w), "precision": "fp64", "l2": "n/a (host cores)",
                 "cpu_baseline": {"value": rate, "unit": METRIC, "cores": cores, "kind": "port", "sample": sample},
                 "e2e": {"value": rate, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
@@ -589,7 +595,7 @@ def main():
     e2e_val = job_rate(world, cells, r["e2e_steps"], r["e2e_s"])
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K, "warmup": args.warmup,
             "ms_per_step": r["step_ms"] / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic", "config": config_json(w),
+            "dtype": "f64", "data": "synthetic", "config": config_json(w), "precision": PRECISION, "l2": L2_NOTE,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "peak_source": peak_kind, "kernel": "sweep_kernel",
                          "algorithmic_bytes_per_cell": BYTES_PER_CELL, "sweep_ms": r["sweep_ms"] / K},

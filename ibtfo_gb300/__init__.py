@@ -167,6 +167,8 @@ SIGNATURES = {
     "ibtfo_case_init": (C.c_int, [C.c_char_p, _P, C.POINTER(Config), _DP, _DP]),
     "ibtfo_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(_P)]),
     "ibtfo_host_free": (C.c_int, [_P]),
+    "ibtfo_fp64_pipe_rate": (C.c_int, [C.c_int, _DP, _DP]),
+    "ibtfo_fast_math_eval": (C.c_int, [C.c_int, _DP, _DP, C.c_int]),
     "ibtfo_query": (C.c_int, [_P]),
     "ibtfo_write_vtk": (C.c_int, [_P, C.c_char_p, C.c_int]),
     "ibtfo_write_vtk_async": (C.c_int, [_P, C.c_char_p, C.c_int]),
@@ -257,6 +259,27 @@ def _dp(a: np.ndarray):
 
 def launch_count() -> int:
     return lib().ibtfo_launch_count()
+
+
+def fp64_pipe_rate(iters: int = 4096) -> tuple[float, float]:
+    """(FP64 thread instructions per second, seconds of the timed launch) of
+    the current GPU: independent DFMA chains on every SM, CUDA-event timed."""
+    r, t = C.c_double(), C.c_double()
+    _check(lib().ibtfo_fp64_pipe_rate(int(iters), C.byref(r), C.byref(t)))
+    return r.value, t.value
+
+
+FAST_MATH = {"rcp_f64": 0, "sqrt_f64": 1, "rcp_f32": 2, "sqrt_f32": 3, "div_f64": 4, "libsqrt_f64": 5,
+             "div_f32": 6, "libsqrt_f32": 7}
+
+
+def fast_math_eval(fn: str, x) -> np.ndarray:
+    """The fast precisions' reciprocal / square root (or CUDA's IEEE ones)
+    evaluated on the GPU at the values x (float64 in and out)."""
+    x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1)
+    y = np.empty_like(x)
+    _check(lib().ibtfo_fast_math_eval(FAST_MATH[fn], _dp(x), _dp(y), int(x.size)))
+    return y
 
 
 class Case:

@@ -80,7 +80,7 @@ def build(force: bool = False, jobs: int | None = None, verbose: bool = False) -
         raise RuntimeError("CUDA build failed:\n" + "\n".join(errors))
     if todo or not os.path.exists(LIB):
         tmp = LIB + ".tmp"
-        cmd = [nv] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcuda"] * 0
+        cmd = [nv] + ARCH + ["-shared", "-o", tmp] + objs
         p = subprocess.run(cmd, capture_output=True, text=True)
         if p.returncode != 0:
             raise RuntimeError("link failed:\n" + p.stdout + p.stderr)

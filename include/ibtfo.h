@@ -467,6 +467,32 @@ ibtfo_status ibtfo_query(ibtfo_case *c);
 ibtfo_status ibtfo_host_alloc(size_t bytes, void **p);
 ibtfo_status ibtfo_host_free(void *p);
 
+/* ---------------------------------------------------------------- measurement
+ *
+ * No reference counterpart.  FP64 pipe rate of the current GPU: a kernel of
+ * independent DFMA chains (8 per thread, 8 CTAs of 256 threads per SM,
+ * `iters` FMAs per chain) timed with CUDA events after one warm-up launch.
+ * *inst_per_s = FP64 thread instructions per second (flops = twice that);
+ * *seconds (may be NULL) = the timed launch.  The plain FP64 sweep is bound
+ * by this rate, not by HBM bandwidth. */
+ibtfo_status ibtfo_fp64_pipe_rate(int iters, double *inst_per_s, double *seconds);
+/* y[i] = f(x[i]) on the GPU for n host values (copies in and out), for
+ * error-bound tests of the arithmetic the fast precisions use: their
+ * reciprocal and square root (Newton-Raphson refinements of the hardware
+ * estimates; the FP32 ones take x and return the result as float) and,
+ * for comparison, CUDA's IEEE division and square root. */
+enum {
+    IBTFO_MATH_RCP_F64 = 0,     /* fp64_fast 1/x */
+    IBTFO_MATH_SQRT_F64 = 1,    /* fp64_fast sqrt(x) */
+    IBTFO_MATH_RCP_F32 = 2,     /* FP32 form 1/x */
+    IBTFO_MATH_SQRT_F32 = 3,    /* FP32 form sqrt(x) */
+    IBTFO_MATH_DIV_F64 = 4,     /* 1.0 / x, IEEE double division */
+    IBTFO_MATH_LIBSQRT_F64 = 5, /* sqrt(x), CUDA's double square root */
+    IBTFO_MATH_DIV_F32 = 6,     /* 1.0f / x, IEEE float division */
+    IBTFO_MATH_LIBSQRT_F32 = 7  /* sqrtf(x), CUDA's float square root */
+};
+ibtfo_status ibtfo_fast_math_eval(int fn, const double *x, double *y, int n);
+
 #ifdef __cplusplus
 }
 #endif

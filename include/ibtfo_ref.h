@@ -2,8 +2,8 @@
  * lists, over host arrays, backed by the GB300 library.
  *
  * A reference driver (Test/<case>/<Case>.cpp) links these through one-line
- * C++ forwarding functions in place of the Src/ files of its
- * Makefile slots.  Each function takes the same arguments as the reference
+ * C++ forwarding functions (ibtfo_gb300/forward/ibtfo_forward.cpp) in place
+ * of the Src/ files of its Makefile slots.  Each function takes the same arguments as the reference
  * function it replaces (file:line below); the trailing (ndevices, device)
  * pair is accepted and must describe one device.
  *

@@ -17,6 +17,16 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 
+
+def reference_dir() -> str | None:
+    """Root of the reference's source checkout (the directory holding Src/ and
+    Test/): $IBTFO_REFERENCE_DIR, else a directory named `reference` beside
+    this repository.  None when neither holds the sources (e.g. on a machine
+    that only runs the built library)."""
+    cand = os.environ.get("IBTFO_REFERENCE_DIR") or \
+        os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+    return cand if os.path.isdir(os.path.join(cand, "Src")) else None
+
 SCHEMES = {"MUSCL": 0, "MHM": 1, "Godunov": 2, "Lax": 3}
 TIME_ADVANCES = {"SingleStep": 0, "RK2": 1}
 RIEMANNS = {"HLL": 0, "HLLC": 1, "PVRS": 2, "StegerWarming": 3}

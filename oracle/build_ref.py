@@ -98,11 +98,16 @@ def build_one(ref, spec, force=False):
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=None,
+                    help="reference source root (default: $IBTFO_REFERENCE_DIR, else ../reference beside the repo)")
     ap.add_argument("--jobs", type=int, default=os.cpu_count() or 4)
     ap.add_argument("--force", action="store_true")
     ap.add_argument("variants", nargs="*", help="names like ref_MUSCL_HLL_minmod_Regular_file")
     a = ap.parse_args(argv)
+    if a.ref is None:
+        sys.path.insert(0, os.path.dirname(HERE))
+        from oracle import reference_dir
+        a.ref = reference_dir() or ""
     if not os.path.isdir(os.path.join(a.ref, "Src")):
         print(f"reference sources not found under {a.ref}; nothing built")
         return 0
