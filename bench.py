@@ -56,6 +56,8 @@ def profile_run(args):
     from ibtfo_gb300 import cases
     if args.workload == "vortex":
         w, inputs = cases.vortex_periodic(args.size), vortex_inputs
+        if args.riemann:
+            w.riemann = args.riemann
     elif args.workload == "obstacles":
         w, inputs = cases.shock_obstacles(args.size, args.size // 2), obstacle_inputs
     else:
@@ -89,19 +91,45 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profiled_traffic():
-    """DRAM bytes per sweep launch from the committed ncu summary, scaled to
-    the benchmark grid, or None."""
+def profiled_value(key):
+    """A per-launch figure of the headline sweep from the committed ncu
+    summary (a line `key: value ...`), or None."""
     p = os.path.join(ROOT, "profiles", "sweep_inclined_channel.md")
     if not os.path.exists(p):
         return None
     for line in open(p):
-        if line.startswith("traffic_bytes_per_launch_full_grid:"):
+        if line.startswith(key + ":"):
             try:
                 return float(line.split(":", 1)[1].split()[0])
             except ValueError:
                 return None
     return None
+
+
+def profiled_traffic():
+    """DRAM bytes per sweep launch from the committed ncu summary, or None."""
+    return profiled_value("traffic_bytes_per_launch_full_grid")
+
+
+def link_rate(nbytes, reps=10):
+    """Host link of this box: GB/s of page-locked host -> device and device ->
+    host copies of `nbytes` (CUDA events on one stream, after a warm-up)."""
+    import torch
+    h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    s = torch.cuda.Stream()
+    out = {}
+    for name, (dst, src) in (("h2d", (d, h)), ("d2h", (h, d))):
+        with torch.cuda.stream(s):
+            dst.copy_(src, non_blocking=True)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            for _ in range(reps):
+                dst.copy_(src, non_blocking=True)
+            e1.record(s)
+        s.synchronize()
+        out[name + "_gbs"] = reps * nbytes / (e0.elapsed_time(e1) * 1e-3) / 1e9
+    return out
 
 
 # ------------------------------------------------------------------ clocks
@@ -317,9 +345,14 @@ def gpu_arm(args, rank, world, local_rank, precision=None, e2e=True, w=None, inp
     e2e_s = time.perf_counter() - t0
     e2e_bytes = c.step_host_bytes(in_place=True)
     pin.close()
+    link = link_rate(g.M * g.N * 4 * 8) if e2e else None
+    if link is not None:
+        link["numa_nodes"] = len([d for d in os.listdir("/sys/devices/system/node") if d.startswith("node")]) \
+            if os.path.isdir("/sys/devices/system/node") else None
 
     step_ms, sweep_ms, e2e_s = max_over_ranks([step_ms, sweep_ms, e2e_s], world, "cuda")
     res = {"step_ms": step_ms, "sweep_ms": sweep_ms, "e2e_s": e2e_s, "e2e_steps": e2e_steps, "e2e_bytes": e2e_bytes,
+           "link": link,
            "cells": cells,
            "launches": launches, "clocks": clk.summary(), "progress": prog, "M": g.M, "N": g.N}
     if snapshot:
@@ -333,7 +366,7 @@ def served_request(ib, r, arrival, density_out=None):
     post = cases.post_shock(r.mach)
     return ib.request(r.id, r.n_x, r.n_y, (0.0, 0.0), (r.width, r.height), r.t_end,
                       bodies=[ib.circle(r.xc, r.yc, r.radius)], x_split=r.x_shock, left=post,
-                      right=(1.0, 0.0, 0.0, 1.0), arrival=arrival, density_out=density_out)
+                      right=(1.0, 0.0, 0.0, 1.0), arrival=arrival, cfl=r.cfl, density_out=density_out)
 
 
 def obstacle_bodies(ib, obstacles):
@@ -410,46 +443,50 @@ def ccm_leg(steps=40, warmup=3, n_x=8192, n_y=4096, full=False):
     return out
 
 
-SERVE_RIEMANN = "HLLC_Toro"
-
-
-def serve_leg(n_requests=24, rates=(None, 2.0), precision="fp32c", plain_precision="fp64_fast",
+def serve_leg(n_requests=64, rates=(None, 2.0, 4.0), precision="fp32c", plain_precision="fp64_fast",
               max_cells=2048 * 2048):
-    """The served batch stream (first `n_requests` of the seeded stream):
-    cases/s and p50/p99 latency of the server at each arrival rate (None: all
-    requests at t = 0, the server's capacity), the same requests run plainly
-    one after another in `plain_precision`, and each served density against
-    the plain one (relative L1 and L-inf).
+    """The served batch stream (the first `n_requests` of the seed-42 stream,
+    grids log-uniform over 128^2..max_cells): cases/s and p50/p99 latency of
+    the server at each arrival rate (None: all requests at t = 0, the
+    server's capacity); the same requests run plainly one after another in
+    `plain_precision` (timed: cases/s of the plain path); each served density
+    against the plain one, both at t_end and at the served run's step count
+    (the loop stops at the first now_t >= t_end with no clipping,
+    Test/Sod/Sod.cpp:123,176, so runs whose dt sequences differ in rounding
+    can stop one step apart; the matched-step figure is the arithmetic
+    error).
 
-    The solver is the contact-restoring HLLC with its positivity safeguards:
-    the reference's HLLC (its HLL solver) and Steger-Warming turn these cases
-    to NaN from about Mach 2 on (a face pressure below zero in the expansion
-    behind the cylinder, which the oracle reproduces)."""
+    Solver and CFL: cases.SERVE_RIEMANN (HLL with Toro's wave speeds and the
+    positivity safeguards) at cases.SERVE_CFL (0.3), under which the stream's
+    Mach 3-4 cases are well conditioned (a 1e-7 perturbation stays 1e-7)."""
     import ibtfo_gb300 as ib
     from ibtfo_gb300 import cases
     base = cases.served_stream(n_requests, 1.0, seed=42, max_cells=max_cells)
     cells = sum(r.n_x * r.n_y for r in base)
+    riemann = cases.SERVE_RIEMANN
     bufs = {r.id: ib.PinnedBuffer(r.n_x * r.n_y) for r in base}
-    out = {"workload": f"shock over a cylinder, first {n_requests} requests of the seed-42 stream "
-                       f"(cells per request log-uniform up to {max_cells}) "
+    out = {"workload": f"shock over a cylinder, the first {n_requests} requests of the seed-42 stream, "
+                       f"cells per request log-uniform over 128^2..{max_cells} "
                        f"(grids {min(r.n_x * r.n_y for r in base)}..{max(r.n_x * r.n_y for r in base)} cells, "
-                       f"{cells} cells in all), MUSCL + {SERVE_RIEMANN} + minmod, IDWBaseGFM, CFL 0.45, "
-                       f"1.5 crossings",
+                       f"{cells} cells in all; Mach {min(r.mach for r in base):.2f}..{max(r.mach for r in base):.2f}), "
+                       f"MUSCL + {riemann} + minmod, IDWBaseGFM, CFL {base[0].cfl}, 1.5 crossings; "
+                       f"all {n_requests} served and run plainly, nothing extrapolated",
            "served_precision": precision, "plain_precision": plain_precision, "rates": []}
-    cell_updates = 0
+    served = None
     for rate in rates:
         arrivals = [0.0] * n_requests if rate is None else \
             [r.arrival for r in cases.served_stream(n_requests, rate, seed=42, max_cells=max_cells)]
-        with ib.Server(riemann=SERVE_RIEMANN, precision=precision, chunk_steps=32, tile_shape="auto") as srv:
+        with ib.Server(riemann=riemann, precision=precision, chunk_steps=32, tile_shape="auto") as srv:
             for r, a in zip(base, arrivals):
                 srv.submit(served_request(ib, r, a, density_out=bufs[r.id]))
             srv.start()
             srv.run(max_seconds=1200)
             res = srv.poll(max_results=n_requests + 8)
             st = srv.stats()
+        res = sorted(res, key=lambda q: q["id"])
         lat = sorted(x["finished"] - x["arrival"] for x in res)
         span = max(x["finished"] for x in res)
-        cell_updates = sum(r.n_x * r.n_y * x["iter"] for r, x in zip(base, sorted(res, key=lambda q: q["id"])))
+        cell_updates = sum(r.n_x * r.n_y * x["iter"] for r, x in zip(base, res))
         out["rates"].append({
             "rate_per_s": rate if rate is not None else "all at t=0", "cases": len(res),
             "failed": sum(1 for x in res if x["status"] != 0), "seconds": span, "cases_per_s": len(res) / span,
@@ -457,30 +494,66 @@ def serve_leg(n_requests=24, rates=(None, 2.0), precision="fp32c", plain_precisi
             "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
             "peak_active": st["peak_active"], "peak_bytes": st["peak_bytes"],
             "tiling": {"shape": ib.TILE_SHAPES_BY_ID.get(st["tile_shape"]), "ctas_per_sm": st["ctas_per_sm"]}})
+        if served is None:
+            served = res
     served_rho = {k: b.array.copy() for k, b in bufs.items()}
     for b in bufs.values():
         b.close()
     # the same requests run plainly, one after another
-    errs, linf = [], []
-    t0 = time.perf_counter()
-    for r in base:
-        with ib.Case(r.n_x, r.n_y, lo=(0.0, 0.0), hi=(r.width, r.height), cfl=0.45, t_end=r.t_end,
-                     max_iter=2 ** 31 - 1, scheme="MUSCL", riemann=SERVE_RIEMANN, boundary="IDWBaseGFM",
+    l1_end, l1_match, linf_match, iters_equal = [], [], [], 0
+    plain_s = 0.0
+    for r, sres in zip(base, served):
+        it_s = sres["iter"]
+        with ib.Case(r.n_x, r.n_y, lo=(0.0, 0.0), hi=(r.width, r.height), cfl=r.cfl, t_end=r.t_end,
+                     max_iter=2 ** 31 - 1, scheme="MUSCL", riemann=riemann, boundary="IDWBaseGFM",
                      precision=plain_precision) as c:
+            t0 = time.perf_counter()
             c.setup_bodies([ib.circle(r.xc, r.yc, r.radius)])
             c.init_x_split(r.x_shock, cases.post_shock(r.mach), (1.0, 0.0, 0.0, 1.0))
-            c.run()
-            rho = c.density().reshape(-1)
-        errs.append(float(np.abs(served_rho[r.id] - rho).sum() / np.abs(rho).sum()))
-        linf.append(float(np.abs(served_rho[r.id] - rho).max() / np.abs(rho).max()))
-    plain_s = time.perf_counter() - t0
+            c.advance(it_s)  # the loop stops early if it reaches t_end first
+            rho_match = c.density().reshape(-1) if c.progress()["iter"] == it_s else None
+            p = c.run()
+            plain_s += time.perf_counter() - t0
+            rho_end = c.density().reshape(-1)
+            iters_equal += int(p["iter"] == it_s)
+            while p["iter"] < it_s:  # the served run took more steps: continue past t_end (untimed)
+                p = c.step()
+            if rho_match is None:
+                rho_match = c.density().reshape(-1)
+        a = served_rho[r.id]
+        l1_end.append(float(np.abs(a - rho_end).sum() / np.abs(rho_end).sum()))
+        l1_match.append(float(np.abs(a - rho_match).sum() / np.abs(rho_match).sum()))
+        linf_match.append(float(np.abs(a - rho_match).max() / np.abs(rho_match).max()))
+    cell_updates = sum(r.n_x * r.n_y * x["iter"] for r, x in zip(base, served))
     out["plain"] = {"seconds": plain_s, "cases_per_s": n_requests / plain_s,
                     "Gcell_updates_per_s": cell_updates / plain_s / 1e9}
     out["served_vs_plain_cases_per_s"] = out["rates"][0]["cases_per_s"] / out["plain"]["cases_per_s"]
-    out["density_l1_vs_plain"] = {"max": max(errs), "median": float(np.median(errs)),
-                                  "within_1e-5": sum(1 for e in errs if e <= 1e-5), "of": len(errs)}
-    out["density_linf_vs_plain"] = {"max": max(linf), "median": float(np.median(linf))}
-    out["nan_results"] = sum(1 for x in res if x["nan_cells"])
+    out["density_l1_vs_plain"] = {"at": "the served run's step count", "max": max(l1_match),
+                                  "median": float(np.median(l1_match)),
+                                  "within_1e-5": sum(1 for e in l1_match if e <= 1e-5), "of": len(l1_match)}
+    out["density_linf_vs_plain"] = {"max": max(linf_match), "median": float(np.median(linf_match))}
+    out["density_l1_vs_plain_at_t_end"] = {"max": max(l1_end), "median": float(np.median(l1_end)),
+                                           "within_1e-5": sum(1 for e in l1_end if e <= 1e-5),
+                                           "same_step_count": iters_equal, "of": len(l1_end)}
+    out["nan_results"] = sum(1 for x in served if x["nan_cells"])
+    return out
+
+
+def fp64_roofline(sweep_s):
+    """The bound of the FP64 sweep: FP64 thread instructions per launch (DADD
+    + DMUL + DFMA, from the committed ncu capture of the same launch) per
+    second of the CUDA-event-timed sweep, against this GPU's FP64 pipe rate
+    measured now (ibtfo_fp64_pipe_rate: independent DFMA chains on every SM)."""
+    import ibtfo_gb300 as ib
+    ops = profiled_value("fp64_thread_inst_per_launch_full_grid")
+    peak, _ = ib.fp64_pipe_rate(16384)
+    out = {"bound": "fp64 pipe", "unit": "G FP64 thread-inst/s", "peak": peak / 1e9,
+           "peak_source": "measured in this run (DFMA chains, CUDA events)", "ops_per_launch": ops,
+           "ops_source": "ncu sm__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on.sum of one launch "
+                         "(profiles/sweep_inclined_channel.md)"}
+    if ops:
+        out["achieved"] = ops / sweep_s / 1e9
+        out["frac"] = out["achieved"] / out["peak"]
     return out
 
 
@@ -494,10 +567,10 @@ def main():
     ap.add_argument("--profile-workload", dest="workload", choices=("channel", "vortex", "obstacles"), default=None,
                     help="only step this workload (profiler captures)")
     ap.add_argument("--size", type=int, default=4096, help="grid size for --profile-workload")
+    ap.add_argument("--riemann", default=None, help="Riemann key for --profile-workload vortex")
     ap.add_argument("--precision", default=PRECISION, choices=("fp64", "fp64_fast", "fp32c"))
-    ap.add_argument("--serve-requests", type=int, default=24, help="requests of the served-stream leg (0: skip)")
-    ap.add_argument("--serve-max-cells", type=int, default=None,
-                    help="largest request grid (default: 2048^2 with --serve-only, 1024^2 in the full run)")
+    ap.add_argument("--serve-requests", type=int, default=64, help="requests of the served-stream leg (0: skip)")
+    ap.add_argument("--serve-max-cells", type=int, default=2048 * 2048, help="largest request grid (cells)")
     ap.add_argument("--serve-only", action="store_true", help="run only the served-stream leg")
     ap.add_argument("--ccm-only", action="store_true", help="run only the cut-cell (shock over obstacles) leg")
     ap.add_argument("--ccm-full", action="store_true", help="cut-cell leg: also run to t_end = 1.0")
@@ -515,8 +588,7 @@ def main():
     if args.serve_only:
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        print(json.dumps({"serve": serve_leg(args.serve_requests, max_cells=args.serve_max_cells or 2048 * 2048)}),
-              flush=True)
+        print(json.dumps({"serve": serve_leg(args.serve_requests, max_cells=args.serve_max_cells)}), flush=True)
         return 0
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -583,8 +655,7 @@ def main():
     # the served stream (rank 0; replicas would serve their own streams)
     serve = None
     if args.serve_requests > 0:
-        serve = serve_leg(args.serve_requests, rates=(None, 8.0),
-                          max_cells=args.serve_max_cells or 1024 * 1024)
+        serve = serve_leg(args.serve_requests, max_cells=args.serve_max_cells)
     K = args.steps
     step_s = r["step_ms"] * 1e-3
     value = job_rate(world, cells, K, step_s)
@@ -598,11 +669,13 @@ def main():
             "dtype": "f64", "data": "synthetic", "config": config_json(w), "precision": PRECISION, "l2": L2_NOTE,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "peak_source": peak_kind, "kernel": "sweep_kernel",
-                         "algorithmic_bytes_per_cell": BYTES_PER_CELL, "sweep_ms": r["sweep_ms"] / K},
+                         "algorithmic_bytes_per_cell": BYTES_PER_CELL, "sweep_ms": r["sweep_ms"] / K,
+                         "fp64": fp64_roofline(sweep_s)},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_val, "unit": METRIC, "h2d_bytes_per_step": r["e2e_bytes"][0],
                     "d2h_bytes_per_step": r["e2e_bytes"][1], "steps": r["e2e_steps"],
-                    "call": "ibtfo_step_host, in place on a page-locked host array"},
+                    "call": "ibtfo_step_host, in place on a page-locked host array",
+                    "vs_device_resident": e2e_val / value, "link": r["link"]},
             "gpu_launches": r["launches"], "clocks": r["clocks"],
             "other_precision": {"precision": other, "value": job_rate(world, cells, K, r2["step_ms"] * 1e-3),
                                 "unit": METRIC, "sweep_ms": r2["sweep_ms"] / K},

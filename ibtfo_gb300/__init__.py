@@ -23,7 +23,7 @@ LIB_PATH = os.path.join(HERE, "libibtfo_gb300.so")
 
 SCHEMES = {"MUSCL": 0, "MHM": 1, "Godunov": 2, "Lax": 3}
 TIME_ADVANCES = {"SingleStep": 0, "RK2": 1}
-RIEMANNS = {"HLL": 0, "HLLC": 1, "PVRS": 2, "StegerWarming": 3, "HLLC_Toro": 4}
+RIEMANNS = {"HLL": 0, "HLLC": 1, "PVRS": 2, "StegerWarming": 3, "HLLC_Toro": 4, "HLL_Toro": 5}
 LIMITERS = {"minmod": 0, "VanLeer": 1}
 BOUNDARIES = {"Regular": 0, "IDWBaseGFM": 1, "LinearBaseGFM": 2, "RiemannBaseGFM": 3, "BCGFM": 4, "HBCGFM": 5,
               "CCM": 6}

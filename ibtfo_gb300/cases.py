@@ -241,6 +241,20 @@ def vortex_periodic(n=4096, riemann="HLLC_Toro"):
 
 # served batch stream --------------------------------------------------------
 
+# The served stream's solver and CFL number.  The reference's HLLC key is its
+# HLL solver; HLL_Toro is that flux with wave-speed estimates that stay
+# defined behind a Mach-4 body, and CFL 0.3 keeps the unsplit update inside
+# its stability range on these flows.  Measured on the stream's Mach 3-4
+# requests (FP64, a 1e-7 relative perturbation of the initial state): with
+# HLL_Toro at CFL 0.3 the perturbation stays near 1e-7 at t_end; at CFL 0.45
+# it grows to 1e-3 (the reference's dt bounds one direction's Courant number,
+# ComputeDt.cpp:49, while both directions update from the same state), and
+# the contact-restoring HLLC_Toro grows it to 1e-2 at either CFL (the
+# odd-even decoupling of contact-restoring solvers at strong grid-aligned
+# shocks).
+SERVE_RIEMANN = "HLL_Toro"
+SERVE_CFL = 0.3
+
 
 @dataclass
 class ServedRequest:
@@ -256,6 +270,7 @@ class ServedRequest:
     radius: float
     x_shock: float
     t_end: float
+    cfl: float = SERVE_CFL
 
 
 def served_stream(n_requests, rate, seed=42, min_cells=128 * 128, max_cells=2048 * 2048, crossings=1.5,
@@ -287,11 +302,11 @@ def served_stream(n_requests, rate, seed=42, min_cells=128 * 128, max_cells=2048
     return out
 
 
-def served_steps_estimate(r: ServedRequest, cfl=0.45, gamma=1.4):
+def served_steps_estimate(r: ServedRequest, cfl=None, gamma=1.4):
     """Steps to t_end with the post-shock maximum wave speed (u2 + a2)."""
     rho2, u2, _, p2 = post_shock(r.mach, gamma)
     lam = u2 + math.sqrt(gamma * p2 / rho2)
-    return int(math.ceil(r.t_end / (cfl * (r.width / r.n_x) / lam)))
+    return int(math.ceil(r.t_end / ((cfl or r.cfl) * (r.width / r.n_x) / lam)))
 
 
 # shock over random obstacles (cut cells) -----------------------------------

@@ -351,7 +351,7 @@ ibtfo_status ibtfo_batch_create(const ibtfo_batch_config *cfg, ibtfo_batch **out
     const ibtfo_batch_config &k = *cfg;
     if (k.precision != IBTFO_PRECISION_FP64_FAST && k.precision != IBTFO_PRECISION_FP32_COMPENSATED)
         return bfail(IBTFO_EINVAL, "batches run the fp64_fast or FP32 compensated precision");
-    if (k.scheme < 0 || k.scheme > 2 || k.riemann < 0 || k.riemann > 4 || k.limiter < 0 || k.limiter > 1)
+    if (k.scheme < 0 || k.scheme > 2 || k.riemann < 0 || k.riemann > 5 || k.limiter < 0 || k.limiter > 1)
         return bfail(IBTFO_EINVAL, "unknown scheme/riemann/limiter key (batches run MUSCL, MHM or Godunov)");
     if (k.tile_shape < 0 || k.tile_shape >= SHAPE_COUNT || k.ctas_per_sm < 0 || k.graph_steps < 0)
         return bfail(IBTFO_EINVAL, "bad tile_shape / ctas_per_sm / graph_steps");

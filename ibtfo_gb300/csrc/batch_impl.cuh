@@ -38,11 +38,15 @@ __global__ void __launch_bounds__(BATCH_THREADS) batch_sweep_kernel(const BatchH
         const int j0 = g.ng + (int)(e.x >> 16) * TY;
         if constexpr (PREC == 2)
         {
-            auto &s = *reinterpret_cast<SweepSmem32<TX, TY> *>(smem_raw);
             const float *U = reinterpret_cast<const float *>(cur ? a.buf1 : a.buf0);
             float *V = reinterpret_cast<float *>(cur ? a.buf0 : a.buf1);
             CellStats32 cs;
-            sweep_tile32<SCH, RIE, LIM, TX, TY, NT>(s, g, U, V, a.type, i0, j0, dt, cs);
+            if constexpr (RIE == HLLT)
+                sweep_tile32_delta<SCH, RIE, LIM, TX, TY, NT>(*reinterpret_cast<SweepSmem32D<TX, TY> *>(smem_raw), g,
+                                                              U, V, a.type, i0, j0, dt, cs);
+            else
+                sweep_tile32<SCH, RIE, LIM, TX, TY, NT>(*reinterpret_cast<SweepSmem32<TX, TY> *>(smem_raw), g, U, V,
+                                                        a.type, i0, j0, dt, cs);
             block_reduce_finalize32<NT>(cs, st, a.partial, g, (unsigned)bc.ntiles, e.y);
         }
         else
@@ -62,7 +66,7 @@ struct BatchVariant
 {
     static constexpr size_t smem()
     {
-        return PREC == 2 ? sizeof(SweepSmem32<TX, TY>) : sizeof(SweepSmem64<TX, TY>);
+        return PREC == 2 ? sizeof(Smem32<RIE, TX, TY>) : sizeof(SweepSmem64<TX, TY>);
     }
     static void launch(const BatchHeader *h, int grid, cudaStream_t s)
     {
@@ -113,6 +117,9 @@ BatchKernel batch_kernel_scheme(int riemann, int limiter, int shape)
     case HLLCT:
         return vl ? batch_kernel_shape<SCH, HLLCT, VANLEER, PREC>(shape)
                   : batch_kernel_shape<SCH, HLLCT, MINMOD, PREC>(shape);
+    case HLLT:
+        return vl ? batch_kernel_shape<SCH, HLLT, VANLEER, PREC>(shape)
+                  : batch_kernel_shape<SCH, HLLT, MINMOD, PREC>(shape);
     default:
         return vl ? batch_kernel_shape<SCH, HLL, VANLEER, PREC>(shape) : batch_kernel_shape<SCH, HLL, MINMOD, PREC>(shape);
     }

@@ -404,7 +404,8 @@ static int make_state_tmaps(ibtfo_case *c)
         return 0;
     const bool f32 = g.f32 != 0;
     const cuuint64_t elem = f32 ? sizeof(float) : sizeof(double);
-    const cuuint64_t dims[3] = {(cuuint64_t)g.M, (cuuint64_t)g.N, 4};
+    // FP32 form: all eight planes (hi 0-3, lo 4-7); a box covers four of them
+    const cuuint64_t dims[3] = {(cuuint64_t)g.M, (cuuint64_t)g.N, (cuuint64_t)(f32 ? 8 : 4)};
     const cuuint64_t strides[2] = {(cuuint64_t)g.pitch * elem, (cuuint64_t)g.plane * elem};
     const cuuint32_t estr[3] = {1, 1, 1};
     for (int h = 0; h < 2; h++)
@@ -528,7 +529,7 @@ ibtfo_status ibtfo_create(const ibtfo_config *cfg, ibtfo_case **out)
         return fail(IBTFO_EINVAL, "grid too large (n_x, n_y <= 262144 and at most 2^31 cells)");
     if (!(k.hi_x > k.lo_x) || !(k.hi_y > k.lo_y) || !(k.gamma > 1.0) || !(k.cfl_number > 0.0))
         return fail(IBTFO_EINVAL, "need hi > lo, gamma > 1, cfl_number > 0");
-    if (k.scheme < 0 || k.scheme > 3 || k.riemann < 0 || k.riemann > 4 || k.limiter < 0 || k.limiter > 1 ||
+    if (k.scheme < 0 || k.scheme > 3 || k.riemann < 0 || k.riemann > 5 || k.limiter < 0 || k.limiter > 1 ||
         k.boundary < 0 || k.boundary > 6 || k.global_boundary < 0 || k.global_boundary > 1 || k.precision < 0 ||
         k.precision > 2 || k.time_advance < 0 || k.time_advance > 1)
         return fail(IBTFO_EINVAL, "unknown scheme/riemann/limiter/boundary/global_boundary/precision/time key");
@@ -1012,6 +1013,9 @@ ibtfo_status ibtfo_get_progress(ibtfo_case *c, ibtfo_progress *p)
     p->dt = s.dt;
     p->mass = s.mass;
     p->mass_start = s.mass_start;
+    if (s.status & STATUS_STALL)
+        return fail(IBTFO_ETIMEOUT, "a tile's staging copy missed its bounded wait: the state of the steps since is "
+                                    "not trusted");
     return IBTFO_OK;
 }
 

@@ -11,6 +11,7 @@
 // of the whole row/column, last match wins, unchanged when nothing matches)
 // becomes index arithmetic plus a check of the neighbouring brackets with
 // the exact coordinate values, which selects the same bracket.
+#include <algorithm>
 #include <vector>
 
 #include "internal.h"
@@ -246,24 +247,20 @@ __global__ void scheme_index_kernel(GridDesc g, int bc, const double *__restrict
 
 static inline unsigned nblk(long long n, int b) { return (unsigned)((n + b - 1) / b); }
 
-// one flag per tx x ty sweep tile: does it hold an interior fluid (or cut) cell?
-__global__ void tile_flags_kernel(GridDesc g, const uint8_t *__restrict__ type, int tx, int ty, int ntx, int nty,
-                                  uint8_t *flags)
+// per tx x ty sweep tile: the number of interior fluid (or cut) cells it holds
+__global__ void tile_counts_kernel(GridDesc g, const uint8_t *__restrict__ type, int tx, int ty, int ntx, int nty,
+                                   int *counts)
 {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ntx * nty)
         return;
     int bx = t % ntx, by = t / ntx;
     int i0 = g.ng + bx * tx, j0 = g.ng + by * ty;
-    uint8_t f = 0;
-    for (int j = j0; j < j0 + ty && j < g.ng + g.n_y && !f; j++)
+    int n = 0;
+    for (int j = j0; j < j0 + ty && j < g.ng + g.n_y; j++)
         for (int i = i0; i < i0 + tx && i < g.ng + g.n_x; i++)
-            if (updated_cell(type[(long long)j * g.pitch + i]))
-            {
-                f = 1;
-                break;
-            }
-    flags[t] = f;
+            n += updated_cell(type[(long long)j * g.pitch + i]) ? 1 : 0;
+    counts[t] = n;
 }
 
 int active_tile_list(const GridDesc &g, const uint8_t *d_type, int tx, int ty, std::vector<unsigned> &list,
@@ -271,24 +268,43 @@ int active_tile_list(const GridDesc &g, const uint8_t *d_type, int tx, int ty, s
 {
     const int ntx = (g.n_x + tx - 1) / tx, nty = (g.n_y + ty - 1) / ty;
     const int n = ntx * nty;
-    uint8_t *d_flags = nullptr;
-    if (cudaMallocAsync(&d_flags, n, s) != cudaSuccess)
+    int *d_counts = nullptr;
+    if (cudaMallocAsync(&d_counts, sizeof(int) * n, s) != cudaSuccess)
         return 2;
-    tile_flags_kernel<<<nblk(n, 256), 256, 0, s>>>(g, d_type, tx, ty, ntx, nty, d_flags);
+    tile_counts_kernel<<<nblk(n, 256), 256, 0, s>>>(g, d_type, tx, ty, ntx, nty, d_counts);
     count_launch();
-    std::vector<uint8_t> flags(n);
-    cudaError_t e = cudaMemcpyAsync(flags.data(), d_flags, n, cudaMemcpyDeviceToHost, s);
-    cudaFreeAsync(d_flags, s);
+    std::vector<int> counts(n);
+    cudaError_t e = cudaMemcpyAsync(counts.data(), d_counts, sizeof(int) * n, cudaMemcpyDeviceToHost, s);
+    cudaFreeAsync(d_counts, s);
     if (e == cudaSuccess)
         e = cudaStreamSynchronize(s);
     if (e != cudaSuccess)
         return 5;
     list.clear();
+    std::vector<int> work;
     for (int t = 0; t < n; t++)
-        if (flags[t])
+        if (counts[t])
+        {
             list.push_back((unsigned)(t % ntx) | ((unsigned)(t / ntx) << 16));
+            work.push_back(counts[t]);
+        }
     if (list.empty())
         list.push_back(0u); // a tile without fluid still runs the loop accounting
+    else if (tx == TILE_X && ty == FAST_TILE_Y)
+    {
+        // the 32x16 sweeps solve only the faces their fluid cells read, so a
+        // tile's time follows its fluid count: longest first, so that the last
+        // CTAs of a launch are the short ones (the row-band lists of the
+        // host-array step keep row order)
+        std::vector<int> idx(list.size());
+        for (size_t k = 0; k < idx.size(); k++)
+            idx[k] = (int)k;
+        std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return work[a] > work[b]; });
+        std::vector<unsigned> sorted(list.size());
+        for (size_t k = 0; k < idx.size(); k++)
+            sorted[k] = list[idx[k]];
+        list.swap(sorted);
+    }
     return 0;
 }
 

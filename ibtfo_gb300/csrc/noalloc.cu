@@ -14,8 +14,6 @@
 // file-scope array below instead of allocated memory.  The array is part of
 // the loaded library: every GPU that loads the library holds it until the
 // process exits.
-#include <mutex>
-
 #include "../../include/ibtfo.h"
 #include "internal.h"
 
@@ -26,31 +24,24 @@ void set_last_error(const char *msg);
 namespace {
 constexpr int kStateSlots = 16;        // doubles reserved for the DevState (128 bytes)
 constexpr int kMaxTiles = 65536;       // 32x8-cell tiles: at most 16,777,216 interior cells
-constexpr int kMaxDevices = 64;
 static_assert(sizeof(ibtfo::DevState) <= kStateSlots * sizeof(double), "DevState slot too small");
 } // namespace
 
 // 512 KiB + 128 B per device
 static __device__ __align__(256) double g_noalloc_scratch[kStateSlots + kMaxTiles];
 
-static std::mutex g_noalloc_mu;
-static double *g_noalloc_addr[kMaxDevices] = {};
-
-// Device address of the scratch array on the current device, looked up once
-// per device (with that device current) and cached.
-static cudaError_t noalloc_scratch(int dev, double **out)
+// Device address of the scratch array on the current device.  Looked up on
+// every call (a cheap runtime query, so a call after cudaDeviceReset or in a
+// new primary context gets the current address); the first lookup on a device
+// may load the library's module there, which is why the first call on a
+// device should come before any stream capture.
+static cudaError_t noalloc_scratch(double **out)
 {
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_addr[dev])
-    {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess)
-            return e;
-        g_noalloc_addr[dev] = static_cast<double *>(p);
-    }
-    *out = g_noalloc_addr[dev];
-    return cudaSuccess;
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e == cudaSuccess)
+        *out = static_cast<double *>(p);
+    return e;
 }
 
 __global__ void noalloc_out_kernel(const ibtfo::DevState *st, double *out)
@@ -85,16 +76,8 @@ extern "C" ibtfo_status ibtfo_dt_mass_noalloc(const double *d_u, long long plane
                      "32 x 8 interior cells, e.g. 4096 x 4096)");
         return IBTFO_EINVAL;
     }
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e == cudaSuccess && (dev < 0 || dev >= kMaxDevices))
-    {
-        set_last_error("ibtfo_dt_mass_noalloc: device ordinal out of range");
-        return IBTFO_EINVAL;
-    }
     double *scratch = nullptr;
-    if (e == cudaSuccess)
-        e = noalloc_scratch(dev, &scratch);
+    cudaError_t e = noalloc_scratch(&scratch);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     DevState *st = reinterpret_cast<DevState *>(scratch);
     // the maxima and the finishing-block ticket must start at zero; the

@@ -183,7 +183,7 @@ ibtfo_status ibtfo_config_from_inp(const ibtfo_inp *p, ibtfo_config *cfg)
 
     static const char *const schemes[] = {"MUSCL", "MHM", "Godunov", "Lax"};
     static const char *const times[] = {"SingleStep", "RK2"};
-    static const char *const riemanns[] = {"HLL", "HLLC", "PVRS", "StegerWarming", "HLLC_Toro"};
+    static const char *const riemanns[] = {"HLL", "HLLC", "PVRS", "StegerWarming", "HLLC_Toro", "HLL_Toro"};
     static const char *const limiters[] = {"minmod", "VanLeer"};
     static const char *const bounds[] = {"Regular", "IDWBaseGFM", "LinearBaseGFM", "RiemannBaseGFM", "BCGFM", "HBCGFM",
                                          "CCM"};
@@ -196,7 +196,7 @@ ibtfo_status ibtfo_config_from_inp(const ibtfo_inp *p, ibtfo_config *cfg)
         int n;
         int *dst;
         int def;
-    } slots[] = {{"Scheme", schemes, 4, &c.scheme, 0},        {"Riemann", riemanns, 5, &c.riemann, 0},
+    } slots[] = {{"Scheme", schemes, 4, &c.scheme, 0},        {"Riemann", riemanns, 6, &c.riemann, 0},
                  {"Limiter", limiters, 2, &c.limiter, 0},     {"Boundary", bounds, 7, &c.boundary, 0},
                  {"Global_Boundary", globals, 2, &c.global_boundary, 0}, {"Precision", precs, 3, &c.precision, 0},
                  {"Time", times, 2, &c.time_advance, 0}};

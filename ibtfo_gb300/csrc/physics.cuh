@@ -14,7 +14,10 @@
 namespace ibtfo {
 
 enum Scheme { MUSCL = 0, MHM = 1, GODUNOV = 2, LAX = 3 };
-enum Riemann { HLL = 0, HLLC = 1, PVRS = 2, SW = 3, HLLCT = 4 };
+enum Riemann { HLL = 0, HLLC = 1, PVRS = 2, SW = 3, HLLCT = 4, HLLT = 5 };
+// the solver keys with no reference counterpart that carry the positivity
+// safeguards (first-order fallback of unphysical face pairs, pressure floor)
+constexpr bool safeguarded(int rie) { return rie == HLLCT || rie == HLLT; }
 enum Limiter { MINMOD = 0, VANLEER = 1 };
 
 // pow(x, 0.5): +0 for a zero of either sign (as pow gives), sqrt otherwise

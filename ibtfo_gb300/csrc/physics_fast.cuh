@@ -285,6 +285,44 @@ __device__ __forceinline__ void hllc_toro(const T UL[4], const T UR[4], const Ga
         F[k] = Fk[k] + S * (Us[k] - U[k]);
 }
 
+// HLL flux in either direction with Toro's PVRS wave-speed estimates
+// (the HLL_Toro key, and the cut-cell method's HLL/HLLC keys)
+// (p* >= 0, q_K = 1 for p* <= p_K; Toro 2009, eqs. 10.59-10.60), which stay
+// defined in strong expansions where the reference's HLL estimate takes the
+// square root of a negative number
+template <typename T, int NRM>
+__device__ __forceinline__ void hll_plain(const T UL[4], const T UR[4], const GasConst<T> &K, T F[4])
+{
+    const Prim<T> L = prim_fast<T, NRM>(UL, K), R = prim_fast<T, NRM>(UR, K);
+    T p_star = (T)0.5 * (L.p + R.p) + (T)0.125 * (L.un - R.un) * ((L.r + R.r) * (L.a + R.a));
+    p_star = p_star > (T)0 ? p_star : (T)0;
+    const T t = K.c1 * p_star;
+    const T S_L = L.un - ((p_star > L.p) ? sqrt_t(L.gi * fma_t(K.c2, L.p, t)) : L.a);
+    const T S_R = R.un + ((p_star > R.p) ? sqrt_t(R.gi * fma_t(K.c2, R.p, t)) : R.a);
+    T FL[4], FR[4];
+    flux_fast<T, NRM>(UL, L, FL);
+    flux_fast<T, NRM>(UR, R, FR);
+    if (S_L >= 0)
+    {
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            F[k] = FL[k];
+    }
+    else if (S_R <= 0)
+    {
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            F[k] = FR[k];
+    }
+    else
+    {
+        const T inv = rcp_t(S_R - S_L), srsl = S_R * S_L;
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            F[k] = (S_R * FL[k] - S_L * FR[k] + srsl * (UR[k] - UL[k])) * inv;
+    }
+}
+
 // MHM predictor with h2 = 0.5 * dt / h precomputed
 template <typename T, int NRM>
 __device__ __forceinline__ void mhm_predict_fast(T UL[4], T UR[4], const GasConst<T> &K, T h2)
@@ -381,7 +419,7 @@ __device__ __forceinline__ void x_face_fast(const T c0[4], const T c1[4], const 
     face_states_fast<T, SCH, LIM>(c0, c1, c2, c3, UL, UR);
     if (SCH == MHM)
         mhm_predict_fast<T, 1>(UL, UR, K, h2);
-    if constexpr (RIE == HLLCT)
+    if constexpr (safeguarded(RIE))
         if (SCH != GODUNOV)
             positivity_fallback(c1, c2, UL, UR);
     if constexpr (RIE == PVRS)
@@ -390,6 +428,8 @@ __device__ __forceinline__ void x_face_fast(const T c0[4], const T c1[4], const 
         sw_fast<T, 1>(UL, UR, K, F);
     else if constexpr (RIE == HLLCT)
         hllc_toro<T, 1>(UL, UR, K, F);
+    else if constexpr (RIE == HLLT)
+        hll_plain<T, 1>(UL, UR, K, F);
     else
         hll_fast<T, 1>(UL, UR, K, F);
 }
@@ -402,7 +442,7 @@ __device__ __forceinline__ int y_face_fast(const T c0[4], const T c1[4], const T
     face_states_fast<T, SCH, LIM>(c0, c1, c2, c3, UD, UU);
     if (SCH == MHM)
         mhm_predict_fast<T, 2>(UD, UU, K, h2);
-    if constexpr (RIE == HLLCT)
+    if constexpr (safeguarded(RIE))
         if (SCH != GODUNOV)
             positivity_fallback(c1, c2, UD, UU);
     if constexpr (RIE == PVRS)
@@ -417,6 +457,11 @@ __device__ __forceinline__ int y_face_fast(const T c0[4], const T c1[4], const T
         hllc_toro<T, 2>(UD, UU, K, G);
         return 0;
     }
+    else if constexpr (RIE == HLLT)
+    {
+        hll_plain<T, 2>(UD, UU, K, G);
+        return 0;
+    }
     else
         return hll_fast<T, 2>(UD, UU, K, G) ? 0 : 0xF;
 }
@@ -426,43 +471,6 @@ __device__ __forceinline__ int y_face_fast(const T c0[4], const T c1[4], const T
 // The cut-cell method has no reference counterpart, so its faces use the
 // plain HLL flux in both directions (no Y-face slot reuse), Steger-Warming, or
 // the contact-restoring HLLC.
-
-// HLL flux in either direction with Toro's PVRS wave-speed estimates
-// (p* >= 0, q_K = 1 for p* <= p_K; Toro 2009, eqs. 10.59-10.60), which stay
-// defined in strong expansions where the reference's HLL estimate takes the
-// square root of a negative number
-template <typename T, int NRM>
-__device__ __forceinline__ void hll_plain(const T UL[4], const T UR[4], const GasConst<T> &K, T F[4])
-{
-    const Prim<T> L = prim_fast<T, NRM>(UL, K), R = prim_fast<T, NRM>(UR, K);
-    T p_star = (T)0.5 * (L.p + R.p) + (T)0.125 * (L.un - R.un) * ((L.r + R.r) * (L.a + R.a));
-    p_star = p_star > (T)0 ? p_star : (T)0;
-    const T t = K.c1 * p_star;
-    const T S_L = L.un - ((p_star > L.p) ? sqrt_t(L.gi * fma_t(K.c2, L.p, t)) : L.a);
-    const T S_R = R.un + ((p_star > R.p) ? sqrt_t(R.gi * fma_t(K.c2, R.p, t)) : R.a);
-    T FL[4], FR[4];
-    flux_fast<T, NRM>(UL, L, FL);
-    flux_fast<T, NRM>(UR, R, FR);
-    if (S_L >= 0)
-    {
-#pragma unroll
-        for (int k = 0; k < 4; k++)
-            F[k] = FL[k];
-    }
-    else if (S_R <= 0)
-    {
-#pragma unroll
-        for (int k = 0; k < 4; k++)
-            F[k] = FR[k];
-    }
-    else
-    {
-        const T inv = rcp_t(S_R - S_L), srsl = S_R * S_L;
-#pragma unroll
-        for (int k = 0; k < 4; k++)
-            F[k] = (S_R * FL[k] - S_L * FR[k] + srsl * (UR[k] - UL[k])) * inv;
-    }
-}
 
 template <typename T, int NRM, int RIE>
 __device__ __forceinline__ void ccm_solve(const T UL[4], const T UR[4], const GasConst<T> &K, T F[4])

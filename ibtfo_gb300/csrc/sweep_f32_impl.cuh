@@ -15,7 +15,10 @@
 // the same bytes as the FP64 path, with the arithmetic on the FP32 pipes.
 #pragma once
 
+#include <type_traits>
+
 #include "internal.h"
+#include "physics_delta.cuh"
 #include "physics_fast.cuh"
 #include "sweep_impl.cuh"
 
@@ -69,6 +72,7 @@ struct SweepSmem32
     float sG[4][TY + 1][TX];
     float sC[4]; // dt/dx, dt/dy, dt/(2dx), dt/(2dy) of this step (one thread computes them)
     unsigned char sKeep[TY + 1][TX];
+    TileFaces<TX, TY> tf; // the faces some fluid cell of the tile reads
 };
 
 // Advance the tile whose first interior cell is (i0, j0) from U into V (float
@@ -100,9 +104,9 @@ __device__ __forceinline__ void sweep_tile32(SweepSmem32<TX, TY> &s, const GridD
     }
 
     bool staged = false;
+    __shared__ uint64_t bar;
     if (tmap)
     {
-        __shared__ uint64_t bar;
         if (tid == 0)
             mbar_init(&bar, 1);
         __syncthreads();
@@ -111,9 +115,19 @@ __device__ __forceinline__ void sweep_tile32(SweepSmem32<TX, TY> &s, const GridD
             mbar_expect_tx(&bar, (unsigned)sizeof(s.sU));
             tma_load_3d(&s.sU[0][0][0], tmap, i0 - 2, j0 - 2, 0, &bar);
         }
+    }
+    // cell flags and the face list while the copy is in flight
+    tile_faces_build<TX, TY, NT>(s.tf, s.sKeep, g, type, i0, j0);
+    if (tmap)
+    {
         staged = __syncthreads_and(mbar_wait(&bar, 0));
+        // a copy that missed the bounded wait: the step is reported as failed
+        // (STATUS_STALL makes the host return IBTFO_ETIMEOUT); the tile is
+        // staged element-wise and, before the CTA leaves the tile, the copy is
+        // waited for once more, so that a late copy lands while this CTA
+        // still owns the shared memory (it brings the values staged here)
         if (!staged && tid == 0 && status)
-            atomicOr(status, STATUS_STALL); // stage element-wise instead (a late copy brings the same values)
+            atomicOr(status, STATUS_STALL);
     }
     // stage the tile and its halo: one index computation per cell, four planes
     if (!staged)
@@ -140,18 +154,16 @@ __device__ __forceinline__ void sweep_tile32(SweepSmem32<TX, TY> &s, const GridD
     // X faces of the tile's rows (sF rows 1..TY; a warp reads one row of sU:
     // columns 0..TX-1 first, the last column after) and all Y faces; the X
     // faces of the row below the tile follow below, where needed
-    constexpr int NXF = (TX + 1) * TY;
-    constexpr int NYF = TX * (TY + 1);
-    for (int q = tid; q < NXF + NYF; q += NT)
+    constexpr int NXF = TileFaces<TX, TY>::NXF;
+    const int nfaces = s.tf.n;
+    for (int t = tid; t < nfaces; t += NT)
     {
+        const int q = tile_face(s.tf, t);
         float c0[4], c1[4], c2[4], c3[4], f[4];
         if (q < NXF)
         {
             int r, fc;
-            if (q < TX * TY)
-                r = q / TX + 1, fc = q - (r - 1) * TX;
-            else
-                r = q - TX * TY + 1, fc = TX;
+            x_face_of<TX, TY>(q, r, fc);
 #pragma unroll
             for (int k = 0; k < 4; k++)
             {
@@ -167,8 +179,8 @@ __device__ __forceinline__ void sweep_tile32(SweepSmem32<TX, TY> &s, const GridD
         }
         else
         {
-            int qq = q - NXF;
-            int r = qq / TX, c = qq - r * TX;
+            int r, c;
+            y_face_of<TX, TY>(q, r, c);
 #pragma unroll
             for (int k = 0; k < 4; k++)
             {
@@ -186,24 +198,27 @@ __device__ __forceinline__ void sweep_tile32(SweepSmem32<TX, TY> &s, const GridD
         }
     }
     __syncthreads();
-    // X faces (i + 1/2, j0 - 1), read only where a bottom Y face kept the X
-    // flux of its slot (the reference's Y-solver aliasing)
-    if (tid < TX && s.sKeep[0][tid])
+    // a Y face (i, j - 1/2) that kept the X-face flux of its slot (the
+    // reference's Y-solver aliasing) reads the X face (i + 1/2, j - 1): solved
+    // here where the list did not (always for the row below the tile)
+    for (int q = tid; q < TX * TY; q += NT)
     {
-        const int fc = tid + 1;
+        const int r = q / TX, c = q - r * TX, fc = c + 1;
+        if (!s.sKeep[r][c] || x_face_listed(s.tf, r, fc))
+            continue;
         float c0[4], c1[4], c2[4], c3[4], f[4];
 #pragma unroll
         for (int k = 0; k < 4; k++)
         {
-            c0[k] = s.sU[k][1][fc];
-            c1[k] = s.sU[k][1][fc + 1];
-            c2[k] = s.sU[k][1][fc + 2];
-            c3[k] = s.sU[k][1][fc + 3];
+            c0[k] = s.sU[k][r + 1][fc];
+            c1[k] = s.sU[k][r + 1][fc + 1];
+            c2[k] = s.sU[k][r + 1][fc + 2];
+            c3[k] = s.sU[k][r + 1][fc + 3];
         }
         x_face_fast<float, SCH, RIE, LIM>(c0, c1, c2, c3, K, hx2, f);
 #pragma unroll
         for (int k = 0; k < 4; k++)
-            s.sF[k][0][fc] = f[k];
+            s.sF[k][r][fc] = f[k];
     }
     __syncthreads();
 
@@ -211,7 +226,7 @@ __device__ __forceinline__ void sweep_tile32(SweepSmem32<TX, TY> &s, const GridD
     {
         const int c = cell % TX, r = cell / TX;
         const int i = i0 + c, j = j0 + r;
-        if (i < g.ng + g.n_x && j < g.ng + g.n_y && type[(long long)j * pitch + i] == 0)
+        if (s.tf.fluid[r + 1][c + 1])
         {
             const long long o = (long long)j * pitch + i;
             const int kp = s.sKeep[r + 1][c], km = s.sKeep[r][c];
@@ -227,7 +242,7 @@ __device__ __forceinline__ void sweep_tile32(SweepSmem32<TX, TY> &s, const GridD
                 lo[k] = U[(4 + k) * P + o];
                 two_float_sub(hi[k], lo[k], d);
             }
-            if constexpr (RIE == HLLCT)
+            if constexpr (safeguarded(RIE))
             {
                 float e;
                 if (pressure_floor_energy(hi, e))
@@ -261,6 +276,197 @@ __device__ __forceinline__ void sweep_tile32(SweepSmem32<TX, TY> &s, const GridD
             cs.nans += (isnan(hi[0]) || isnan(hi[1]) || isnan(hi[2]) || isnan(hi[3])) ? 1 : 0;
         }
     }
+    if (tmap && !staged && tid == 0)
+        mbar_wait(&bar, 0); // bounded: the copy that missed the first wait
+}
+
+// Shared memory of one FP32 tile in difference form (HLL_Toro): the hi and lo
+// planes of the tile and its two-cell halo, and per face P = F - F(lower /
+// left cell) and Q = F - F(upper / right cell) (physics_delta.cuh).
+template <int TX, int TY>
+struct SweepSmem32D
+{
+    float sU[8][TY + 4][TX + 4]; // planes 0-3 hi, 4-7 lo (the buffer's plane order)
+    float sFP[4][TY + 1][TX + 1];
+    float sFQ[4][TY + 1][TX + 1];
+    float sGP[4][TY + 1][TX];
+    float sGQ[4][TY + 1][TX];
+    float sC[4];
+    unsigned char sKeep[TY + 1][TX]; // no slot reuse under HLL_Toro: cleared, kept for the face list
+    TileFaces<TX, TY> tf;
+};
+
+// the FP32 tile's shared memory for a Riemann key
+template <int RIE, int TX, int TY>
+using Smem32 = typename std::conditional<RIE == HLLT, SweepSmem32D<TX, TY>, SweepSmem32<TX, TY>>::type;
+
+// sweep_tile32 for HLL_Toro in difference form: the same tile, face list,
+// update, floor, RK2 stages and statistics; the faces store (P, Q) and the
+// update takes P_east - Q_west and P_north - Q_south.  With `tmap` the hi
+// and lo planes of the box come by two bulk tensor copies (planes 0-3 and
+// 4-7 of the case's 8-plane tensor map).
+template <int SCH, int RIE, int LIM, int TX, int TY, int NT>
+__device__ __forceinline__ void sweep_tile32_delta(SweepSmem32D<TX, TY> &s, const GridDesc &g,
+                                                   const float *__restrict__ U, float *__restrict__ V,
+                                                   const uint8_t *__restrict__ type, int i0, int j0, double dt,
+                                                   CellStats32 &cs, int stage = 0, const CUtensorMap *tmap = nullptr,
+                                                   int *status = nullptr)
+{
+    constexpr int WX = TX + 4, WY = TY + 4;
+    const long long P = g.plane;
+    const int pitch = g.pitch;
+    const int tid = threadIdx.x;
+    if (tid == 0)
+    {
+        const float dtf = (float)dt;
+        s.sC[0] = dtf * g.idxf;
+        s.sC[1] = dtf * g.idyf;
+        s.sC[2] = 0.5f * s.sC[0];
+        s.sC[3] = 0.5f * s.sC[1];
+    }
+    bool staged = false;
+    __shared__ uint64_t bar;
+    if (tmap)
+    {
+        if (tid == 0)
+            mbar_init(&bar, 1);
+        __syncthreads();
+        if (tid == 0)
+        {
+            mbar_expect_tx(&bar, (unsigned)sizeof(s.sU));
+            tma_load_3d(&s.sU[0][0][0], tmap, i0 - 2, j0 - 2, 0, &bar);
+            tma_load_3d(&s.sU[4][0][0], tmap, i0 - 2, j0 - 2, 4, &bar);
+        }
+    }
+    tile_faces_build<TX, TY, NT>(s.tf, s.sKeep, g, type, i0, j0);
+    if (tmap)
+    {
+        staged = __syncthreads_and(mbar_wait(&bar, 0));
+        // as in sweep_tile32: a missed wait fails the step, the tile is staged
+        // element-wise, and the copy is waited for again before the CTA leaves
+        if (!staged && tid == 0 && status)
+            atomicOr(status, STATUS_STALL);
+    }
+    if (!staged)
+        for (int q = tid; q < WX * WY; q += NT)
+        {
+            const int ly = q / WX, lx = q - ly * WX;
+            const int gi = i0 - 2 + lx, gj = j0 - 2 + ly;
+            float v[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+            if (gi < g.M && gj < g.N)
+            {
+                const float *src = U + (long long)gj * pitch + gi;
+#pragma unroll
+                for (int k = 0; k < 8; k++)
+                    v[k] = src[k * P];
+            }
+#pragma unroll
+            for (int k = 0; k < 8; k++)
+                s.sU[k][ly][lx] = v[k];
+        }
+    __syncthreads();
+
+    const GasConst<float> K(g.gf, g.gm1f, g.c1f, g.c2f, g.igm1f, g.ig2f);
+    const float hx2 = s.sC[2], hy2 = s.sC[3];
+    constexpr int NXF = TileFaces<TX, TY>::NXF;
+    const int nfaces = s.tf.n;
+    for (int t = tid; t < nfaces; t += NT)
+    {
+        const int q = tile_face(s.tf, t);
+        float h[4][4], l[4][4], fp[4], fq[4];
+        if (q < NXF)
+        {
+            int r, fc;
+            x_face_of<TX, TY>(q, r, fc);
+#pragma unroll
+            for (int n = 0; n < 4; n++)
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                {
+                    h[n][k] = s.sU[k][r + 1][fc + n];
+                    l[n][k] = s.sU[4 + k][r + 1][fc + n];
+                }
+            face_delta<SCH, LIM, 1>(h[0], l[0], h[1], l[1], h[2], l[2], h[3], l[3], K, hx2, fp, fq);
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+            {
+                s.sFP[k][r][fc] = fp[k];
+                s.sFQ[k][r][fc] = fq[k];
+            }
+        }
+        else
+        {
+            int r, c;
+            y_face_of<TX, TY>(q, r, c);
+#pragma unroll
+            for (int n = 0; n < 4; n++)
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                {
+                    h[n][k] = s.sU[k][r + n][c + 2];
+                    l[n][k] = s.sU[4 + k][r + n][c + 2];
+                }
+            face_delta<SCH, LIM, 2>(h[0], l[0], h[1], l[1], h[2], l[2], h[3], l[3], K, hy2, fp, fq);
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+            {
+                s.sGP[k][r][c] = fp[k];
+                s.sGQ[k][r][c] = fq[k];
+            }
+        }
+    }
+    __syncthreads();
+
+    for (int cell = tid; cell < TX * TY; cell += NT)
+    {
+        const int c = cell % TX, r = cell / TX;
+        if (s.tf.fluid[r + 1][c + 1])
+        {
+            const long long o = (long long)(j0 + r) * pitch + (i0 + c);
+            const float lx = s.sC[0], ly = s.sC[1];
+            float hi[4], lo[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+            {
+                // F_e - F_w = P_e - Q_w, G_n - G_s = P_n - Q_s
+                const float d = fmaf(lx, s.sFP[k][r + 1][c + 1] - s.sFQ[k][r + 1][c],
+                                     ly * (s.sGP[k][r + 1][c] - s.sGQ[k][r][c]));
+                hi[k] = s.sU[k][r + 2][c + 2];
+                lo[k] = s.sU[4 + k][r + 2][c + 2];
+                two_float_sub(hi[k], lo[k], d);
+            }
+            float e;
+            if (pressure_floor_energy(hi, e))
+            {
+                hi[3] = e;
+                lo[3] = 0.0f;
+            }
+            if (stage == 2)
+            {
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    two_float_average(hi[k], lo[k], V[k * P + o], V[(4 + k) * P + o]);
+            }
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+            {
+                V[k * P + o] = hi[k];
+                V[(4 + k) * P + o] = lo[k];
+            }
+            if (stage == 1)
+                continue;
+            const float ir = rcp_t(hi[0]);
+            const float u = hi[1] * ir, w = hi[2] * ir;
+            const float p = K.gm1 * (hi[3] - 0.5f * hi[0] * (u * u + w * w));
+            cs.amax = fmaxf(cs.amax, sqrt_t(K.g * p * ir));
+            cs.umax = fmaxf(cs.umax, fabsf(u));
+            cs.vmax = fmaxf(cs.vmax, fabsf(w));
+            two_float_acc(cs.mhi, cs.mlo, hi[0], lo[0]);
+            cs.nans += (isnan(hi[0]) || isnan(hi[1]) || isnan(hi[2]) || isnan(hi[3])) ? 1 : 0;
+        }
+    }
+    if (tmap && !staged && tid == 0)
+        mbar_wait(&bar, 0); // bounded: the copy that missed the first wait
 }
 
 // Block reduction in FP32 (compensated for the mass); thread 0 converts the
@@ -323,14 +529,14 @@ __device__ __forceinline__ void block_reduce_finalize32(CellStats32 cs, DevState
 }
 
 // one case: one 256-thread CTA per active tile of TILE_X x TY cells (32x8:
-// 40 registers, 6 CTAs per SM; 32x16: 5 CTAs per SM)
+// 40 registers, 6 CTAs per SM; 32x16: 5 CTAs per SM; the difference form of
+// HLL_Toro: 3 CTAs per SM, its 32x16 tile holding 62 KB of shared memory)
 template <int SCH, int RIE, int LIM, int TY>
-__global__ void __launch_bounds__(TILE_X *TILE_Y, TY == TILE_Y ? 6 : 5)
+__global__ void __launch_bounds__(TILE_X *TILE_Y, RIE == HLLT ? 3 : (TY == TILE_Y ? 6 : 5))
     sweep_f32_kernel(const __grid_constant__ SweepArgs a)
 {
     constexpr int NT = TILE_X * TILE_Y;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    auto &s = *reinterpret_cast<SweepSmem32<TILE_X, TY> *>(smem_raw);
 
     const GridDesc &g = a.g;
     DevState *st = a.st;
@@ -347,15 +553,45 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y, TY == TILE_Y ? 6 : 5)
     const int i0 = g.ng + (int)(tile & 0xFFFFu) * TILE_X;
     const int j0 = g.ng + (int)(tile >> 16) * TY;
     CellStats32 cs;
-    sweep_tile32<SCH, RIE, LIM, TILE_X, TY, NT>(s, g, U, V, a.type, i0, j0, dt, cs, a.stage,
-                                                a.tma ? &a.tmap[cur] : nullptr, &st->status);
+    if constexpr (RIE == HLLT)
+        sweep_tile32_delta<SCH, RIE, LIM, TILE_X, TY, NT>(*reinterpret_cast<SweepSmem32D<TILE_X, TY> *>(smem_raw), g,
+                                                          U, V, a.type, i0, j0, dt, cs, a.stage,
+                                                          a.tma ? &a.tmap[cur] : nullptr, &st->status);
+    else
+        sweep_tile32<SCH, RIE, LIM, TILE_X, TY, NT>(*reinterpret_cast<SweepSmem32<TILE_X, TY> *>(smem_raw), g, U, V,
+                                                    a.type, i0, j0, dt, cs, a.stage, a.tma ? &a.tmap[cur] : nullptr,
+                                                    &st->status);
     block_reduce_finalize32<NT>(cs, st, a.partial, g, a.nblocks ? a.nblocks : gridDim.x, bid, a.stage == 1);
 }
 
 template <int SCH, int RIE, int LIM, int TY>
 void launch_sweep_f32(const SweepArgs &a, dim3 grid, dim3 block, cudaStream_t s)
 {
-    sweep_f32_kernel<SCH, RIE, LIM, TY><<<grid, block, sizeof(SweepSmem32<TILE_X, TY>), s>>>(a);
+    sweep_f32_kernel<SCH, RIE, LIM, TY><<<grid, block, sizeof(Smem32<RIE, TILE_X, TY>), s>>>(a);
+}
+
+// The launcher of one instantiation; a tile whose shared memory exceeds the
+// default 48 KB (the difference form's 32x16 tile) has the limit raised on the
+// current device, once per device, when a case picks the launcher (outside
+// any stream capture).
+template <int SCH, int RIE, int LIM, int TY>
+SweepLaunch prepared_f32_launcher()
+{
+    constexpr int smem = (int)sizeof(Smem32<RIE, TILE_X, TY>);
+    if (smem > 48 * 1024)
+    {
+        static std::atomic<unsigned long long> ready{0};
+        int dev = 0;
+        cudaGetDevice(&dev);
+        const unsigned long long bit = 1ull << (dev & 63);
+        if (!(ready.load() & bit))
+        {
+            cudaFuncSetAttribute(sweep_f32_kernel<SCH, RIE, LIM, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 smem);
+            ready.fetch_or(bit);
+        }
+    }
+    return &launch_sweep_f32<SCH, RIE, LIM, TY>;
 }
 
 // the launchers of one scheme over TILE_X x TY tiles (nullptr: PVRS, FP64 precisions only)
@@ -366,6 +602,8 @@ SweepLaunch select_f32(int riemann, bool vl)
         return vl ? &launch_sweep_f32<SCH, SW, VANLEER, TY> : &launch_sweep_f32<SCH, SW, MINMOD, TY>;
     if (riemann == HLLCT)
         return vl ? &launch_sweep_f32<SCH, HLLCT, VANLEER, TY> : &launch_sweep_f32<SCH, HLLCT, MINMOD, TY>;
+    if (riemann == HLLT)
+        return vl ? prepared_f32_launcher<SCH, HLLT, VANLEER, TY>() : prepared_f32_launcher<SCH, HLLT, MINMOD, TY>();
     if (riemann == HLL)
         return vl ? &launch_sweep_f32<SCH, HLL, VANLEER, TY> : &launch_sweep_f32<SCH, HLL, MINMOD, TY>;
     return nullptr;

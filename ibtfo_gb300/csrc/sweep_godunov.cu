@@ -12,6 +12,7 @@ SweepLaunch sweep_launcher_godunov(int riemann, int limiter)
     case PVRS: return vl ? &launch_sweep<GODUNOV, PVRS, VANLEER, 0> : &launch_sweep<GODUNOV, PVRS, MINMOD, 0>;
     case SW: return vl ? &launch_sweep<GODUNOV, SW, VANLEER, 0> : &launch_sweep<GODUNOV, SW, MINMOD, 0>;
     case HLLCT: return vl ? &launch_sweep<GODUNOV, HLLCT, VANLEER, 0> : &launch_sweep<GODUNOV, HLLCT, MINMOD, 0>;
+    case HLLT: return vl ? &launch_sweep<GODUNOV, HLLT, VANLEER, 0> : &launch_sweep<GODUNOV, HLLT, MINMOD, 0>;
     default: return vl ? &launch_sweep<GODUNOV, HLL, VANLEER, 0> : &launch_sweep<GODUNOV, HLL, MINMOD, 0>;
     }
 }

@@ -13,6 +13,7 @@ static SweepLaunch select(int riemann, bool vl)
     case PVRS: return vl ? &launch_sweep<GODUNOV, PVRS, VANLEER, 1> : &launch_sweep<GODUNOV, PVRS, MINMOD, 1>;
     case SW: return vl ? prepared_sweep_launcher<GODUNOV, SW, VANLEER, 1, TY>() : prepared_sweep_launcher<GODUNOV, SW, MINMOD, 1, TY>();
     case HLLCT: return vl ? prepared_sweep_launcher<GODUNOV, HLLCT, VANLEER, 1, TY>() : prepared_sweep_launcher<GODUNOV, HLLCT, MINMOD, 1, TY>();
+    case HLLT: return vl ? prepared_sweep_launcher<GODUNOV, HLLT, VANLEER, 1, TY>() : prepared_sweep_launcher<GODUNOV, HLLT, MINMOD, 1, TY>();
     default: return vl ? prepared_sweep_launcher<GODUNOV, HLL, VANLEER, 1, TY>() : prepared_sweep_launcher<GODUNOV, HLL, MINMOD, 1, TY>();
     }
 }

@@ -23,6 +23,7 @@
 #include "internal.h"
 #include "physics.cuh"
 #include "physics_fast.cuh"
+#include "tile_faces.cuh"
 #include "tma.cuh"
 
 namespace ibtfo {
@@ -263,6 +264,7 @@ struct SweepSmem64
     double sG[4][TY + 1][TX];
     double sC[4]; // fp64_fast: dt/dx, dt/dy, dt/(2dx), dt/(2dy), computed once per tile
     unsigned char sKeep[TY + 1][TX];
+    TileFaces<TX, TY> tf; // the faces some fluid cell of the tile reads
 };
 
 // Advance the tile whose first interior cell is (i0, j0) from U into V and
@@ -283,7 +285,7 @@ __device__ __forceinline__ void sweep_tile64(SweepSmem64<TX, TY> &s, const GridD
     const long long P = g.plane;
     const int pitch = g.pitch;
     const int tid = threadIdx.x;
-    constexpr bool FASTPHYS = FAST || RIE == HLLCT; // faces evaluated by physics_fast.cuh
+    constexpr bool FASTPHYS = FAST || safeguarded(RIE); // faces evaluated by physics_fast.cuh
     if (FASTPHYS && tid == 0)
     {
         s.sC[0] = dt * g.idx;
@@ -293,9 +295,9 @@ __device__ __forceinline__ void sweep_tile64(SweepSmem64<TX, TY> &s, const GridD
     }
 
     bool staged = false;
+    __shared__ uint64_t bar;
     if (tmap)
     {
-        __shared__ uint64_t bar;
         if (tid == 0)
             mbar_init(&bar, 1);
         __syncthreads();
@@ -304,9 +306,19 @@ __device__ __forceinline__ void sweep_tile64(SweepSmem64<TX, TY> &s, const GridD
             mbar_expect_tx(&bar, (unsigned)sizeof(s.sU));
             tma_load_3d(&s.sU[0][0][0], tmap, i0 - 2, j0 - 2, 0, &bar);
         }
+    }
+    // cell flags and the face list while the copy is in flight
+    tile_faces_build<TX, TY, NT>(s.tf, s.sKeep, g, type, i0, j0);
+    if (tmap)
+    {
         staged = __syncthreads_and(mbar_wait(&bar, 0));
+        // a copy that missed the bounded wait: the step is reported as failed
+        // (STATUS_STALL makes the host return IBTFO_ETIMEOUT); the tile is
+        // staged element-wise and, before the CTA leaves the tile, the copy is
+        // waited for once more, so that a late copy lands while this CTA
+        // still owns the shared memory (it brings the values staged here)
         if (!staged && tid == 0 && status)
-            atomicOr(status, STATUS_STALL); // stage element-wise instead (a late copy brings the same values)
+            atomicOr(status, STATUS_STALL);
     }
     // stage the tile and its halo (always inside the padded array: ng >= 2),
     // one index computation per cell for the four planes
@@ -334,18 +346,16 @@ __device__ __forceinline__ void sweep_tile64(SweepSmem64<TX, TY> &s, const GridD
     const double hx2 = FASTPHYS ? s.sC[2] : 0.0, hy2 = FASTPHYS ? s.sC[3] : 0.0; // MHM predictor of physics_fast
     // X faces of the tile's rows (sF rows 1..TY) and all Y faces; the X faces
     // of the row below the tile (sF row 0) follow below, where needed
-    constexpr int NXF = (TX + 1) * TY;
-    constexpr int NYF = TX * (TY + 1);
-    for (int q = tid; q < NXF + NYF; q += NT)
+    constexpr int NXF = TileFaces<TX, TY>::NXF;
+    const int nfaces = s.tf.n;
+    for (int t = tid; t < nfaces; t += NT)
     {
+        const int q = tile_face(s.tf, t);
         double c0[4], c1[4], c2[4], c3[4], f[4];
         if (q < NXF)
         {
-            int r, fc; // a warp reads one row of sU: columns 0..TX-1 first, the last column after
-            if (q < TX * TY)
-                r = q / TX + 1, fc = q - (r - 1) * TX;
-            else
-                r = q - TX * TY + 1, fc = TX;
+            int r, fc;
+            x_face_of<TX, TY>(q, r, fc);
 #pragma unroll
             for (int k = 0; k < 4; k++)
             {
@@ -364,8 +374,8 @@ __device__ __forceinline__ void sweep_tile64(SweepSmem64<TX, TY> &s, const GridD
         }
         else
         {
-            int qq = q - NXF;
-            int r = qq / TX, c = qq - r * TX;
+            int r, c;
+            y_face_of<TX, TY>(q, r, c);
 #pragma unroll
             for (int k = 0; k < 4; k++)
             {
@@ -399,20 +409,23 @@ __device__ __forceinline__ void sweep_tile64(SweepSmem64<TX, TY> &s, const GridD
         }
     }
     __syncthreads();
-    // a bottom Y face (j0 - 1/2) that kept the X-face flux of its slot, as
-    // the reference's Y solver does in some branches, reads the X face
-    // (i + 1/2, j0 - 1): solved only for those columns
-    if (tid < TX && s.sKeep[0][tid])
+    // a Y face (i, j - 1/2) that kept the X-face flux of its slot, as the
+    // reference's Y solver does in some branches, reads the X face
+    // (i + 1/2, j - 1): solved here where the list did not (always for the
+    // row below the tile)
+    for (int q = tid; q < TX * TY; q += NT)
     {
-        const int fc = tid + 1;
+        const int r = q / TX, c = q - r * TX, fc = c + 1;
+        if (!s.sKeep[r][c] || x_face_listed(s.tf, r, fc))
+            continue;
         double c0[4], c1[4], c2[4], c3[4], f[4];
 #pragma unroll
         for (int k = 0; k < 4; k++)
         {
-            c0[k] = s.sU[k][1][fc];
-            c1[k] = s.sU[k][1][fc + 1];
-            c2[k] = s.sU[k][1][fc + 2];
-            c3[k] = s.sU[k][1][fc + 3];
+            c0[k] = s.sU[k][r + 1][fc];
+            c1[k] = s.sU[k][r + 1][fc + 1];
+            c2[k] = s.sU[k][r + 1][fc + 2];
+            c3[k] = s.sU[k][r + 1][fc + 3];
         }
         if (FASTPHYS)
             x_face_fast<double, SCH, RIE, LIM>(c0, c1, c2, c3, K, hx2, f);
@@ -420,7 +433,7 @@ __device__ __forceinline__ void sweep_tile64(SweepSmem64<TX, TY> &s, const GridD
             x_face<SCH, RIE, LIM>(c0, c1, c2, c3, gam, dt, g.dx, f);
 #pragma unroll
         for (int k = 0; k < 4; k++)
-            s.sF[k][0][fc] = f[k];
+            s.sF[k][r][fc] = f[k];
     }
     __syncthreads();
 
@@ -429,7 +442,7 @@ __device__ __forceinline__ void sweep_tile64(SweepSmem64<TX, TY> &s, const GridD
     {
         const int c = cell % TX, r = cell / TX;
         const int i = i0 + c, j = j0 + r;
-        if (i < g.ng + g.n_x && j < g.ng + g.n_y && type[(long long)j * pitch + i] == 0)
+        if (s.tf.fluid[r + 1][c + 1])
         {
             const int kp = s.sKeep[r + 1][c], km = s.sKeep[r][c];
             const double lx = FAST ? s.sC[0] : 0.0, ly = FAST ? s.sC[1] : 0.0;
@@ -450,7 +463,7 @@ __device__ __forceinline__ void sweep_tile64(SweepSmem64<TX, TY> &s, const GridD
                     v[k] = x - dt * (gp - gm) / g.dy;
                 }
             }
-            if constexpr (RIE == HLLCT)
+            if constexpr (safeguarded(RIE))
                 pressure_floor(v);
             if (stage == 2)
                 rk2_average(V, (long long)j * pitch + i, P, v);
@@ -465,6 +478,8 @@ __device__ __forceinline__ void sweep_tile64(SweepSmem64<TX, TY> &s, const GridD
                 cell_stats(v, gam, g.dx, g.dy, cs);
         }
     }
+    if (tmap && !staged && tid == 0)
+        mbar_wait(&bar, 0); // bounded: the copy that missed the first wait
 }
 
 // one case: one CTA of TILE_X x TILE_Y threads per active tile of TILE_X x TY

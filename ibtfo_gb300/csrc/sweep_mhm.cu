@@ -12,6 +12,7 @@ SweepLaunch sweep_launcher_mhm(int riemann, int limiter)
     case PVRS: return vl ? &launch_sweep<MHM, PVRS, VANLEER, 0> : &launch_sweep<MHM, PVRS, MINMOD, 0>;
     case SW: return vl ? &launch_sweep<MHM, SW, VANLEER, 0> : &launch_sweep<MHM, SW, MINMOD, 0>;
     case HLLCT: return vl ? &launch_sweep<MHM, HLLCT, VANLEER, 0> : &launch_sweep<MHM, HLLCT, MINMOD, 0>;
+    case HLLT: return vl ? &launch_sweep<MHM, HLLT, VANLEER, 0> : &launch_sweep<MHM, HLLT, MINMOD, 0>;
     default: return vl ? &launch_sweep<MHM, HLL, VANLEER, 0> : &launch_sweep<MHM, HLL, MINMOD, 0>;
     }
 }

@@ -13,6 +13,7 @@ static SweepLaunch select(int riemann, bool vl)
     case PVRS: return vl ? &launch_sweep<MHM, PVRS, VANLEER, 1> : &launch_sweep<MHM, PVRS, MINMOD, 1>;
     case SW: return vl ? prepared_sweep_launcher<MHM, SW, VANLEER, 1, TY>() : prepared_sweep_launcher<MHM, SW, MINMOD, 1, TY>();
     case HLLCT: return vl ? prepared_sweep_launcher<MHM, HLLCT, VANLEER, 1, TY>() : prepared_sweep_launcher<MHM, HLLCT, MINMOD, 1, TY>();
+    case HLLT: return vl ? prepared_sweep_launcher<MHM, HLLT, VANLEER, 1, TY>() : prepared_sweep_launcher<MHM, HLLT, MINMOD, 1, TY>();
     default: return vl ? prepared_sweep_launcher<MHM, HLL, VANLEER, 1, TY>() : prepared_sweep_launcher<MHM, HLL, MINMOD, 1, TY>();
     }
 }

@@ -13,6 +13,7 @@ static SweepLaunch select(int riemann, bool vl)
     case PVRS: return vl ? &launch_sweep<MUSCL, PVRS, VANLEER, 1> : &launch_sweep<MUSCL, PVRS, MINMOD, 1>;
     case SW: return vl ? prepared_sweep_launcher<MUSCL, SW, VANLEER, 1, TY>() : prepared_sweep_launcher<MUSCL, SW, MINMOD, 1, TY>();
     case HLLCT: return vl ? prepared_sweep_launcher<MUSCL, HLLCT, VANLEER, 1, TY>() : prepared_sweep_launcher<MUSCL, HLLCT, MINMOD, 1, TY>();
+    case HLLT: return vl ? prepared_sweep_launcher<MUSCL, HLLT, VANLEER, 1, TY>() : prepared_sweep_launcher<MUSCL, HLLT, MINMOD, 1, TY>();
     default: return vl ? prepared_sweep_launcher<MUSCL, HLL, VANLEER, 1, TY>() : prepared_sweep_launcher<MUSCL, HLL, MINMOD, 1, TY>();
     }
 }

@@ -53,13 +53,20 @@ enum { IBTFO_TIME_SINGLESTEP = 0, IBTFO_TIME_RK2 = 1 };
  * reconstructed state has rho <= 0 or an internal energy below 1e-6 of E
  * takes the first-order pair (the two cell averages), and an updated fluid
  * cell whose internal energy falls below 1e-5 of E has E raised to
- * E_kin + 1e-5 E */
+ * E_kin + 1e-5 E.  HLL_TORO (no reference counterpart) is the reference's
+ * HLL flux with Toro's wave-speed estimates (p* clamped at 0, q_K = 1 where
+ * p* <= p_K, so no square root of a negative number behind a strong
+ * shock), no Y-face slot reuse, and the same two safeguards; like every HLL
+ * flux it does not suffer the carbuncle / odd-even decoupling of
+ * contact-restoring solvers at strong grid-aligned shocks.  Under the
+ * cut-cell method it is the same solver as the HLL/HLLC keys. */
 enum {
     IBTFO_RIEMANN_HLL = 0,
     IBTFO_RIEMANN_HLLC = 1,
     IBTFO_RIEMANN_PVRS = 2,
     IBTFO_RIEMANN_STEGER_WARMING = 3,
-    IBTFO_RIEMANN_HLLC_TORO = 4
+    IBTFO_RIEMANN_HLLC_TORO = 4,
+    IBTFO_RIEMANN_HLL_TORO = 5
 };
 enum { IBTFO_LIMITER_MINMOD = 0, IBTFO_LIMITER_VANLEER = 1 };
 enum {
@@ -105,7 +112,9 @@ typedef struct ibtfo_config {
 /* The reference time-loop scalars after the last completed step. */
 typedef struct ibtfo_progress {
     int iter;       /* completed steps */
-    int status;     /* bit 0: a fluid cell held NaN after some step (sticky) */
+    int status;     /* bit 0: a fluid cell held NaN after some step (sticky); bit 1: a
+                       sweep tile's staging copy missed its bounded wait (sticky; the
+                       calls that report progress then return IBTFO_ETIMEOUT) */
     int nan_cells;  /* fluid cells with a NaN component after the latest step */
     int reserved;
     double now_t;   /* loop time, advanced by the dt computed after each step (Sod.cpp:176) */
@@ -285,10 +294,14 @@ ibtfo_status ibtfo_case_init(const char *name, const ibtfo_inp *p, const ibtfo_c
  * inside the library (512 KiB per GPU, held by every GPU that loads the
  * library until the process exits), so grids above 65536 tiles of 32 x 8
  * interior cells (e.g. 4096 x 4096) are rejected with IBTFO_EINVAL.  The
- * first call on a device looks up that array's device address: make that
- * first call before any stream capture.  Every call shares the one array and
- * it keeps the last call's contents: calls that overlap on the GPU (other
- * streams, other threads) race and give wrong results. */
+ * first call on a device looks up that array's device address (every call
+ * looks it up; the first may load the library's code onto that device): make
+ * that first call before any stream capture.  Every call shares the one array
+ * and it keeps the last call's contents: calls that overlap on the GPU (other
+ * streams, other threads) race and give wrong results.  NaN is not reported:
+ * a NaN density in a fluid cell makes the mass NaN, and NaN in the other
+ * components drops out of the maxima (ibtfo_get_progress of a case counts
+ * NaN cells). */
 ibtfo_status ibtfo_dt_mass_noalloc(const double *d_u, long long plane, int pitch, const unsigned char *d_type,
                                    int n_x, int n_y, int num_ghost_cell, double lo_x, double lo_y, double hi_x,
                                    double hi_y, double gamma, double cfl_number, double *d_out, void *stream);

@@ -7,7 +7,8 @@ and through size-independent properties where it does not:
 
 * inclined channel, 2048x1024, MUSCL + HLLC + minmod, IDWBaseGFM: geometry
   bit for bit, dt / mass sequences and state within 1e-12 relative of the
-  oracle after 10 steps (both FP64 keys); the host-array step (row bands
+  oracle after 10 steps, and the run to t_end = 0.2 with the oracle's step
+  count and L1 density within 1e-10 (both FP64 keys); the host-array step (row bands
   copied while the sweep runs) bit for bit with put + step + get;
 * periodic isentropic vortex, 4096x4096, MHM + minmod: with the reference's
   HLLC, within 1e-12 of the oracle after 3 steps; with the contact-restoring
@@ -96,6 +97,43 @@ def test_channel_full_size_matches_oracle(channel_oracle, precision):
         uo, un = c.get_state(u_new=True)
     assert_state_close(uo, ref["u_old"], "U_OLD")
     assert_state_close(un, ref["u_new"], "U_NEW")
+
+
+@pytest.fixture(scope="module")
+def channel_oracle_t_end():
+    """The oracle's run of the full channel to its t_end = 0.2 (the loop of
+    Test/InclineSod/InclineSod.cpp:131-189: stop at the first now_t >= t_end)."""
+    w = cases.inclined_channel()
+    oracle.set_threads(16)
+    phi = cases.channel_phi(w.grid)
+    o = oracle_case(w)
+    o.setup_geometry(phi)
+    u0 = cases.channel_init(w.grid, o.get("XYCOORD").reshape(-1, 6)[:, 5], w.gamma)
+    o.set_initial_state(u0)
+    o.run(10 ** 6, w.t_end)
+    out = dict(w=w, phi=phi, u0=u0, u_old=o.get("U_OLD"), **o.scalars())
+    o.close()
+    return out
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp64_fast"])
+def test_channel_full_size_to_t_end(channel_oracle_t_end, precision):
+    """2048x1024 inclined channel run to t_end = 0.2 (about 500 steps): the
+    same step count and now_t as the oracle, and L1 density within 1e-10
+    (relative) of the oracle's."""
+    ref = channel_oracle_t_end
+    w = ref["w"]
+    with ib.Case.from_workload(w, precision=precision) as c:
+        c.setup_geometry(ref["phi"])
+        c.set_state(ref["u0"])
+        p = c.run()
+        u = c.get_state()
+    assert p["iter"] == ref["iter"], (p["iter"], ref["iter"])
+    assert seq_close([p["now_t"]], [ref["now_t"]])
+    a = u.reshape(-1, 4)[:, 0]
+    b = ref["u_old"].reshape(-1, 4)[:, 0]
+    l1 = float(np.abs(a - b).sum() / np.abs(b).sum())
+    assert l1 <= 1e-10, l1
 
 
 def test_channel_full_size_host_step_equals_put_step_get():
