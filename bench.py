@@ -260,6 +260,52 @@ def vortex_errors(w, rhos):
     return out
 
 
+def vortex_period_leg(n_big=4096, n_pair=1024, perturb=1e-7):
+    """The vortex workload advected one full period (t = 10, the loop's
+    t_end): the FP32 form at n_big^2 (steps, seconds, density against the
+    analytic vortex at its loop time); at n_pair^2 the FP32 form, fp64_fast
+    to the same step count, and fp64_fast from an initial state perturbed by
+    `perturb` (relative, seeded) -- the FP64 run's own sensitivity, the scale
+    against which the FP32 form's distance from FP64 is read."""
+    import ibtfo_gb300 as ib
+    from ibtfo_gb300 import cases
+
+    def rel(a, b):
+        d = np.abs(a - b)
+        return {"l1": float(d.sum() / np.abs(b).sum()), "linf": float(d.max() / np.abs(b).max())}
+
+    def run(n, prec, max_iter=2 ** 31 - 1, pert=0.0):
+        w = cases.vortex_periodic(n)
+        g = w.grid
+        phi, u0 = cases.isentropic_vortex(g)
+        if pert:
+            u0 = u0.reshape(-1, 4) * (1.0 + pert * np.random.default_rng(3).standard_normal((g.M * g.N, 4)))
+        with ib.Case.from_workload(w, precision=prec, max_iter=max_iter) as c:
+            c.setup_geometry(phi)
+            c.set_state(np.ascontiguousarray(u0).reshape(-1))
+            t0 = time.perf_counter()
+            p = c.run()
+            secs = time.perf_counter() - t0
+            rho = c.density()
+        _, ex = cases.isentropic_vortex(g, t=p["now_t"])
+        return p, rho, secs, ex.reshape(g.N, g.M, 4)[g.ng:-g.ng, g.ng:-g.ng, 0]
+
+    w = cases.vortex_periodic(n_big)
+    out = {"t_end": w.t_end, "scheme": w.scheme, "riemann": w.riemann, "time": w.time, "cfl": w.cfl}
+    p, rho, secs, ex = run(n_big, "fp32c")
+    out[f"fp32c_{n_big}"] = {"steps": p["iter"], "now_t": p["now_t"], "seconds": secs,
+                             "Gcell_updates_per_s": n_big * n_big * p["iter"] / secs / 1e9,
+                             "vs_analytic": rel(rho, ex), "nan_cells": p["nan_cells"]}
+    p32, r32, s32, e32 = run(n_pair, "fp32c")
+    p64, r64, s64, e64 = run(n_pair, "fp64_fast", max_iter=p32["iter"])
+    pp, rp, _, _ = run(n_pair, "fp64_fast", max_iter=p32["iter"], pert=perturb)
+    out[f"pair_{n_pair}"] = {"steps": [p32["iter"], p64["iter"]], "seconds": [s32, s64],
+                             "fp32c_vs_fp64": rel(r32, r64), "fp64_perturbed_vs_fp64": rel(rp, r64),
+                             "perturbation": perturb, "fp64_vs_analytic": rel(r64, e64),
+                             "fp32c_vs_analytic": rel(r32, e32)}
+    return out
+
+
 def max_over_ranks(values, world, device):
     """Element-wise maximum of per-rank timings over all ranks (the slowest
     replica sets the whole job's time); identity for one rank."""
@@ -456,27 +502,27 @@ def serve_leg(n_requests=64, rates=(None, 2.0, 4.0), precision="fp32c", plain_pr
     can stop one step apart; the matched-step figure is the arithmetic
     error).
 
-    Solver and CFL: cases.SERVE_RIEMANN (HLL with Toro's wave speeds and the
-    positivity safeguards) at cases.SERVE_CFL (0.3), under which the stream's
-    Mach 3-4 cases are well conditioned (a 1e-7 perturbation stays 1e-7)."""
+    Solver, time integration and CFL: cases.SERVE_RIEMANN (HLL with Toro's
+    wave speeds and the positivity safeguards), cases.SERVE_TIME (RK2) at
+    cases.SERVE_CFL (0.45); cases.py gives the measurements behind them."""
     import ibtfo_gb300 as ib
     from ibtfo_gb300 import cases
     base = cases.served_stream(n_requests, 1.0, seed=42, max_cells=max_cells)
     cells = sum(r.n_x * r.n_y for r in base)
-    riemann = cases.SERVE_RIEMANN
+    riemann, tadv = cases.SERVE_RIEMANN, cases.SERVE_TIME
     bufs = {r.id: ib.PinnedBuffer(r.n_x * r.n_y) for r in base}
     out = {"workload": f"shock over a cylinder, the first {n_requests} requests of the seed-42 stream, "
                        f"cells per request log-uniform over 128^2..{max_cells} "
                        f"(grids {min(r.n_x * r.n_y for r in base)}..{max(r.n_x * r.n_y for r in base)} cells, "
                        f"{cells} cells in all; Mach {min(r.mach for r in base):.2f}..{max(r.mach for r in base):.2f}), "
-                       f"MUSCL + {riemann} + minmod, IDWBaseGFM, CFL {base[0].cfl}, 1.5 crossings; "
+                       f"MUSCL + {riemann} + minmod, Time = {tadv}, IDWBaseGFM, CFL {base[0].cfl}, 1.5 crossings; "
                        f"all {n_requests} served and run plainly, nothing extrapolated",
            "served_precision": precision, "plain_precision": plain_precision, "rates": []}
     served = None
     for rate in rates:
         arrivals = [0.0] * n_requests if rate is None else \
             [r.arrival for r in cases.served_stream(n_requests, rate, seed=42, max_cells=max_cells)]
-        with ib.Server(riemann=riemann, precision=precision, chunk_steps=32, tile_shape="auto") as srv:
+        with ib.Server(riemann=riemann, precision=precision, chunk_steps=32, tile_shape="auto", time=tadv) as srv:
             for r, a in zip(base, arrivals):
                 srv.submit(served_request(ib, r, a, density_out=bufs[r.id]))
             srv.start()
@@ -506,7 +552,7 @@ def serve_leg(n_requests=64, rates=(None, 2.0, 4.0), precision="fp32c", plain_pr
         it_s = sres["iter"]
         with ib.Case(r.n_x, r.n_y, lo=(0.0, 0.0), hi=(r.width, r.height), cfl=r.cfl, t_end=r.t_end,
                      max_iter=2 ** 31 - 1, scheme="MUSCL", riemann=riemann, boundary="IDWBaseGFM",
-                     precision=plain_precision) as c:
+                     precision=plain_precision, time=tadv) as c:
             t0 = time.perf_counter()
             c.setup_bodies([ib.circle(r.xc, r.yc, r.radius)])
             c.init_x_split(r.x_shock, cases.post_shock(r.mach), (1.0, 0.0, 0.0, 1.0))
@@ -535,6 +581,9 @@ def serve_leg(n_requests=64, rates=(None, 2.0, 4.0), precision="fp32c", plain_pr
     out["density_l1_vs_plain_at_t_end"] = {"max": max(l1_end), "median": float(np.median(l1_end)),
                                            "within_1e-5": sum(1 for e in l1_end if e <= 1e-5),
                                            "same_step_count": iters_equal, "of": len(l1_end)}
+    worst = sorted(range(len(base)), key=lambda k: -l1_match[k])[:5]
+    out["worst_requests"] = [{"id": base[k].id, "grid": [base[k].n_x, base[k].n_y], "mach": base[k].mach,
+                              "steps": served[k]["iter"], "l1": l1_match[k], "linf": linf_match[k]} for k in worst]
     out["nan_results"] = sum(1 for x in served if x["nan_cells"])
     return out
 
@@ -575,6 +624,7 @@ def main():
     ap.add_argument("--ccm-only", action="store_true", help="run only the cut-cell (shock over obstacles) leg")
     ap.add_argument("--ccm-full", action="store_true", help="cut-cell leg: also run to t_end = 1.0")
     ap.add_argument("--no-ccm", action="store_true", help="skip the cut-cell leg")
+    ap.add_argument("--no-period", action="store_true", help="skip the vortex's one-period leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.workload:
@@ -645,6 +695,8 @@ def main():
         rhos[prec] = (rv.get("rho"), rv.get("rho_t"))
     if rank == 0:
         forms["errors"] = vortex_errors(wv, rhos)
+        if not args.no_period:
+            forms["one_period"] = vortex_period_leg()
     if world > 1:
         import torch
         torch.distributed.destroy_process_group()
@@ -681,8 +733,8 @@ def main():
                                 "unit": METRIC, "sweep_ms": r2["sweep_ms"] / K},
             "serve": serve,
             "cut_cells": ccm,
-            "forms": {"workload": wv.name, "scheme": wv.scheme, "riemann": wv.riemann, "boundary": "periodic",
-                      **forms},
+            "forms": {"workload": wv.name, "scheme": wv.scheme, "riemann": wv.riemann, "time": wv.time,
+                      "cfl": wv.cfl, "boundary": "periodic", **forms},
             "final": {"iter": r["progress"]["iter"], "nan_cells": r["progress"]["nan_cells"]}}
     print(json.dumps(line), flush=True)
     return 0

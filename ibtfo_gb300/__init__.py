@@ -62,7 +62,7 @@ _DP = C.POINTER(C.c_double)
 class BatchConfig(C.Structure):
     _fields_ = [("scheme", C.c_int), ("riemann", C.c_int), ("limiter", C.c_int), ("precision", C.c_int),
                 ("tile_shape", C.c_int), ("ctas_per_sm", C.c_int), ("graph_steps", C.c_int),
-                ("reserved", C.c_int * 5)]
+                ("time_advance", C.c_int), ("reserved", C.c_int * 4)]
 
 
 class BatchTiling(C.Structure):
@@ -94,7 +94,8 @@ MAX_BODIES = 8
 class ServerConfig(C.Structure):
     _fields_ = [("scheme", C.c_int), ("riemann", C.c_int), ("limiter", C.c_int), ("precision", C.c_int),
                 ("memory_budget", C.c_longlong), ("max_active", C.c_int), ("chunk_steps", C.c_int),
-                ("tile_shape", C.c_int), ("ctas_per_sm", C.c_int), ("reserved", C.c_int * 6)]
+                ("tile_shape", C.c_int), ("ctas_per_sm", C.c_int), ("time_advance", C.c_int),
+                ("reserved", C.c_int * 5)]
 
 
 class Request(C.Structure):
@@ -305,7 +306,7 @@ class Case:
         g = w.grid
         kw = dict(n_x=g.n_x, n_y=g.n_y, ng=g.ng, lo=(g.lo_x, g.lo_y), hi=(g.hi_x, g.hi_y), gamma=w.gamma, cfl=w.cfl,
                   t_end=w.t_end, scheme=w.scheme, riemann=w.riemann, limiter=w.limiter, boundary=w.boundary,
-                  gbc=w.gbc)
+                  gbc=w.gbc, time=getattr(w, "time", "SingleStep"))
         kw.update(over)
         return cls(**kw)
 
@@ -487,9 +488,9 @@ class Batch:
     `synchronize`."""
 
     def __init__(self, scheme="MUSCL", riemann="HLL", limiter="minmod", precision="fp32c", tile_shape="32x8",
-                 ctas_per_sm=0, graph_steps=16):
+                 ctas_per_sm=0, graph_steps=16, time="SingleStep"):
         cfg = BatchConfig(SCHEMES[scheme], RIEMANNS[riemann], LIMITERS[limiter], PRECISIONS[precision],
-                          TILE_SHAPES[tile_shape], ctas_per_sm, graph_steps)
+                          TILE_SHAPES[tile_shape], ctas_per_sm, graph_steps, TIME_ADVANCES[time])
         h = _P()
         _check(lib().ibtfo_batch_create(C.byref(cfg), C.byref(h)))
         self.h = h
@@ -615,10 +616,11 @@ class Server:
     """Continuous-batching request loop (native; see ibtfo_server_* in ibtfo.h)."""
 
     def __init__(self, scheme="MUSCL", riemann="HLLC", limiter="minmod", precision="fp32c", memory_budget=0,
-                 max_active=0, chunk_steps=32, tile_shape="32x8", ctas_per_sm=0):
+                 max_active=0, chunk_steps=32, tile_shape="32x8", ctas_per_sm=0, time="SingleStep"):
         cfg = ServerConfig(SCHEMES[scheme], RIEMANNS[riemann], LIMITERS[limiter], PRECISIONS[precision],
                            int(memory_budget), int(max_active), int(chunk_steps),
-                           -1 if tile_shape == "auto" else TILE_SHAPES[tile_shape], int(ctas_per_sm))
+                           -1 if tile_shape == "auto" else TILE_SHAPES[tile_shape], int(ctas_per_sm),
+                           TIME_ADVANCES[time])
         h = _P()
         _check(lib().ibtfo_server_create(C.byref(cfg), C.byref(h)))
         self.h = h

@@ -205,6 +205,7 @@ class Workload:
     boundary: str
     gbc: str = "walls"
     extra: dict = field(default_factory=dict)
+    time: str = "SingleStep"
 
 
 def sod_tube(n_x=400, n_y=100):
@@ -220,40 +221,45 @@ def inclined_channel(n_x=2048, n_y=1024, boundary="IDWBaseGFM"):
                     "MUSCL", "HLLC", "minmod", boundary, extra={"angle": 30.0, "width": 0.25})
 
 
-def vortex_periodic(n=4096, riemann="HLLC_Toro"):
-    """Isentropic vortex, periodic n x n on [0,10]^2, beta 5, MHM + HLLC, t 10.
+def vortex_periodic(n=4096, riemann="HLL_Toro", time="RK2"):
+    """Isentropic vortex, periodic n x n on [0,10]^2, beta 5, MHM + HLLC
+    (the reference's HLLC key is its HLL solver: here HLL_Toro), Time = RK2,
+    CFL 0.25, advected one period (t 10).
 
-    The vortex's vertical velocity exceeds the sound speed in part of the
-    core; the reference's HLLC (its HLL solver, which reuses the X-face flux
-    where S_D >= 0) turns the state to NaN there within a few dozen steps, so
-    the workload runs the contact-restoring HLLC ("HLLC_Toro").
+    Solver: the vortex's vertical velocity exceeds the sound speed in part of
+    the core; the reference's HLL, which reuses the X-face flux where
+    S_D >= 0, turns the state to NaN there within a few dozen steps.
+    HLL_Toro is the same HLL flux without that slot reuse and with wave-speed
+    estimates defined everywhere.
 
-    CFL 0.25: the reference's update is unsplit (both directions from the
-    same state) while its time step is sized on one direction only
-    (ComputeDt.cpp:49, dt = CFL dx / max wave speed), so on this diagonal
-    stream the summed Courant number is about twice CFL.  At CFL 0.5 the
-    scheme is linearly unstable here: a 1e-12 perturbation of the initial
-    state grows to 1e-3 in 200 steps (FP64, MUSCL and MHM alike); at 0.25 it
-    stays near 1e-8 after 400 steps."""
+    Time integration: with Time = SingleStep (forward Euler) the reference's
+    MUSCL and MHM updates are unstable in smooth flow at any CFL; the limiter
+    only bounds the growth.  Measured on this flow to t = 10 (FP64, 1024^2,
+    CFL 0.25): a 1e-7 relative perturbation of the initial state ends at 1.8e-3
+    (L1 density) after single steps, at 2.1e-5 after RK2 steps, against a
+    distance of 1.6e-4 from the exact solution.  CFL 0.25: the reference's
+    time step bounds one direction's Courant number (ComputeDt.cpp:49) while
+    both directions update from the same state, and this stream is diagonal."""
     return Workload(f"isentropic_vortex_{n}", Grid(n, n, 2, 0.0, 0.0, 10.0, 10.0), 1.4, 0.25, 10.0,
-                    "MHM", riemann, "minmod", "Regular", gbc="periodic", extra={"beta": 5.0})
+                    "MHM", riemann, "minmod", "Regular", gbc="periodic", extra={"beta": 5.0}, time=time)
 
 
 # served batch stream --------------------------------------------------------
 
-# The served stream's solver and CFL number.  The reference's HLLC key is its
-# HLL solver; HLL_Toro is that flux with wave-speed estimates that stay
-# defined behind a Mach-4 body, and CFL 0.3 keeps the unsplit update inside
-# its stability range on these flows.  Measured on the stream's Mach 3-4
-# requests (FP64, a 1e-7 relative perturbation of the initial state): with
-# HLL_Toro at CFL 0.3 the perturbation stays near 1e-7 at t_end; at CFL 0.45
-# it grows to 1e-3 (the reference's dt bounds one direction's Courant number,
-# ComputeDt.cpp:49, while both directions update from the same state), and
-# the contact-restoring HLLC_Toro grows it to 1e-2 at either CFL (the
-# odd-even decoupling of contact-restoring solvers at strong grid-aligned
-# shocks).
+# The served stream's solver, time integration and CFL number.  The
+# reference's HLLC key is its HLL solver; HLL_Toro is that flux with
+# wave-speed estimates that stay defined behind a Mach-4 body.  Measured on
+# the stream's Mach 2-4 requests (FP64, a 1e-7 relative perturbation of the
+# initial state, L1 density at t_end):
+#   HLLC_Toro, single steps, CFL 0.3 or 0.45:  1e-2 (odd-even decoupling of
+#     contact-restoring solvers at strong grid-aligned shocks)
+#   HLL_Toro, single steps, CFL 0.45: up to 1e-3; CFL 0.3: 1e-7 on grids up
+#     to 900 cells wide, but the forward-Euler update is unstable in smooth
+#     flow, and on the larger grids the wake amplifies FP32 rounding to 1e-4
+#   HLL_Toro, Time = RK2, CFL 0.45: 6e-7 to 1e-5 (the wake's own growth)
 SERVE_RIEMANN = "HLL_Toro"
-SERVE_CFL = 0.3
+SERVE_TIME = "RK2"
+SERVE_CFL = 0.45
 
 
 @dataclass

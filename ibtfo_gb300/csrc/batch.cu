@@ -309,16 +309,27 @@ ibtfo_status upload(ibtfo_batch *b)
     return IBTFO_OK;
 }
 
+// kernel launches of one step
+int launches_per_step(const ibtfo_batch *b)
+{
+    return (b->cfg.time_advance == IBTFO_TIME_RK2 ? 2 : 1) * (b->need_phase1 ? 3 : 2);
+}
+
 void enqueue_steps(ibtfo_batch *b, int n)
 {
+    // Time = RK2: the first stage and its boundary pass, then the second
+    // stage (which does the loop accounting) and its boundary pass, as the
+    // one-case step does
+    const bool rk2 = b->cfg.time_advance == IBTFO_TIME_RK2;
     for (int s = 0; s < n; s++)
-    {
-        b->kern.launch(b->d_hdr, b->grid_sweep, b->stream);
-        count_launch();
-        launch_batch_fill(b->d_hdr, 0, b->grid_fill, b->stream);
-        if (b->need_phase1)
-            launch_batch_fill(b->d_hdr, 1, b->grid_fill, b->stream);
-    }
+        for (int stage = rk2 ? 1 : 0; stage <= (rk2 ? 2 : 0); stage++)
+        {
+            b->kern.launch(b->d_hdr, b->grid_sweep, b->stream, stage);
+            count_launch();
+            launch_batch_fill(b->d_hdr, 0, b->grid_fill, b->stream);
+            if (b->need_phase1)
+                launch_batch_fill(b->d_hdr, 1, b->grid_fill, b->stream);
+        }
 }
 
 ibtfo_status build_graph(ibtfo_batch *b)
@@ -355,6 +366,8 @@ ibtfo_status ibtfo_batch_create(const ibtfo_batch_config *cfg, ibtfo_batch **out
         return bfail(IBTFO_EINVAL, "unknown scheme/riemann/limiter key (batches run MUSCL, MHM or Godunov)");
     if (k.tile_shape < 0 || k.tile_shape >= SHAPE_COUNT || k.ctas_per_sm < 0 || k.graph_steps < 0)
         return bfail(IBTFO_EINVAL, "bad tile_shape / ctas_per_sm / graph_steps");
+    if (k.time_advance < 0 || k.time_advance > 1)
+        return bfail(IBTFO_EINVAL, "unknown time_advance key");
     ibtfo_batch *b = new ibtfo_batch();
     b->cfg = k;
     if (b->cfg.graph_steps == 0)
@@ -449,8 +462,8 @@ ibtfo_status ibtfo_batch_add(ibtfo_batch *b, ibtfo_case *c, int *slot)
         return bfail(IBTFO_ESTATE, "no state: call ibtfo_set_state before adding the case");
     if (fa.bc == BC_CCM)
         return bfail(IBTFO_EINVAL, "cut-cell cases run one per launch (their mixing step is not batched)");
-    if (case_time_advance(c) != IBTFO_TIME_SINGLESTEP)
-        return bfail(IBTFO_EINVAL, "Time = RK2 cases run one per launch");
+    if (case_time_advance(c) != b->cfg.time_advance)
+        return bfail(IBTFO_EINVAL, "the case's Time key differs from the batch's");
     const int r0 = (rie == IBTFO_RIEMANN_HLLC) ? IBTFO_RIEMANN_HLL : rie;
     const int r1 = (b->cfg.riemann == IBTFO_RIEMANN_HLLC) ? IBTFO_RIEMANN_HLL : b->cfg.riemann;
     if (sch != b->cfg.scheme || r0 != r1 || lim != b->cfg.limiter || prec != b->cfg.precision)
@@ -534,7 +547,7 @@ ibtfo_status ibtfo_batch_advance(ibtfo_batch *b, int nsteps)
             return s;
     }
     int left = nsteps;
-    const int per_step = b->need_phase1 ? 3 : 2;
+    const int per_step = launches_per_step(b);
     if (left >= b->cfg.graph_steps)
     {
         if (!b->graph)

@@ -14,7 +14,7 @@
 namespace ibtfo {
 
 template <int SCH, int RIE, int LIM, int PREC, int TX, int TY>
-__global__ void __launch_bounds__(BATCH_THREADS) batch_sweep_kernel(const BatchHeader *__restrict__ h)
+__global__ void __launch_bounds__(BATCH_THREADS) batch_sweep_kernel(const BatchHeader *__restrict__ h, int stage)
 {
     constexpr int NT = BATCH_THREADS;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -34,8 +34,9 @@ __global__ void __launch_bounds__(BATCH_THREADS) batch_sweep_kernel(const BatchH
         const double dt = st->dt;
         const int cur = st->cur;
         const GridDesc &g = a.g;
-        const int i0 = g.ng + (int)(e.x & 0xFFFFu) * TX;
-        const int j0 = g.ng + (int)(e.x >> 16) * TY;
+        const int i0 = g.ng + tile_ix(e.x) * TX;
+        const int j0 = g.ng + tile_jy(e.x) * TY;
+        const bool interior = (e.x & TILE_INTERIOR) != 0;
         if constexpr (PREC == 2)
         {
             const float *U = reinterpret_cast<const float *>(cur ? a.buf1 : a.buf0);
@@ -43,11 +44,12 @@ __global__ void __launch_bounds__(BATCH_THREADS) batch_sweep_kernel(const BatchH
             CellStats32 cs;
             if constexpr (RIE == HLLT)
                 sweep_tile32_delta<SCH, RIE, LIM, TX, TY, NT>(*reinterpret_cast<SweepSmem32D<TX, TY> *>(smem_raw), g,
-                                                              U, V, a.type, i0, j0, dt, cs);
+                                                              U, V, a.type, i0, j0, dt, cs, stage, nullptr, nullptr,
+                                                              interior);
             else
                 sweep_tile32<SCH, RIE, LIM, TX, TY, NT>(*reinterpret_cast<SweepSmem32<TX, TY> *>(smem_raw), g, U, V,
-                                                        a.type, i0, j0, dt, cs);
-            block_reduce_finalize32<NT>(cs, st, a.partial, g, (unsigned)bc.ntiles, e.y);
+                                                        a.type, i0, j0, dt, cs, stage, nullptr, nullptr, interior);
+            block_reduce_finalize32<NT>(cs, st, a.partial, g, (unsigned)bc.ntiles, e.y, stage == 1);
         }
         else
         {
@@ -55,8 +57,9 @@ __global__ void __launch_bounds__(BATCH_THREADS) batch_sweep_kernel(const BatchH
             const double *U = cur ? a.buf1 : a.buf0;
             double *V = cur ? a.buf0 : a.buf1;
             CellStats cs;
-            sweep_tile64<SCH, RIE, LIM, 1, TX, TY, NT>(s, g, U, V, a.type, i0, j0, dt, cs);
-            block_reduce_finalize<NT>(cs, st, a.partial, g, true, false, (unsigned)bc.ntiles, e.y);
+            sweep_tile64<SCH, RIE, LIM, 1, TX, TY, NT>(s, g, U, V, a.type, i0, j0, dt, cs, stage, nullptr, nullptr,
+                                                       interior);
+            block_reduce_finalize<NT>(cs, st, a.partial, g, true, false, (unsigned)bc.ntiles, e.y, stage == 1);
         }
     }
 }
@@ -68,9 +71,9 @@ struct BatchVariant
     {
         return PREC == 2 ? sizeof(Smem32<RIE, TX, TY>) : sizeof(SweepSmem64<TX, TY>);
     }
-    static void launch(const BatchHeader *h, int grid, cudaStream_t s)
+    static void launch(const BatchHeader *h, int grid, cudaStream_t s, int stage)
     {
-        batch_sweep_kernel<SCH, RIE, LIM, PREC, TX, TY><<<grid, BATCH_THREADS, smem(), s>>>(h);
+        batch_sweep_kernel<SCH, RIE, LIM, PREC, TX, TY><<<grid, BATCH_THREADS, smem(), s>>>(h, stage);
     }
     static int prepare()
     {

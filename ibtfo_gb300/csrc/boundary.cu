@@ -177,13 +177,24 @@ __device__ void fill_ring(const FillArgs &a, const View &v, double *dst, long lo
         else if (j >= n_y + ng)
             sj = j - n_y;
         const bool src_interior_row = (sj >= ng && sj < ng + n_y);
-        for (int k = 0; k < 4; k++)
+        const long long so = (long long)sj * pitch + si;
+        const double *src;
+        if (row || !src_interior_row || (sj != j))
+            src = (v.interior(si, sj) && updated_cell(v.type[so])) ? v.next : v.prev; // S(.) of an interior cell
+        else
+            src = v.next; // interior row, after the fill
+        if (a.g.f32)
         {
-            if (row || !src_interior_row || (sj != j))
-                out[k] = v.S(si, sj, k); // value S(.) of an interior cell
-            else
-                out[k] = v.N_(si, sj, k); // interior row, after the fill
+            // the FP32 form's (hi, lo) pair copied as it is: a round trip
+            // through FP64 re-splits a pair whose lo is exactly half an ulp
+            const float *sf = reinterpret_cast<const float *>(src);
+            float *df = reinterpret_cast<float *>(dst);
+            for (int k = 0; k < 8; k++)
+                df[k * a.g.plane + o] = sf[k * a.g.plane + so];
+            return;
         }
+        for (int k = 0; k < 4; k++)
+            out[k] = state_ld(src, k, so, a.g);
     }
     else if (row)
     {

@@ -223,7 +223,7 @@ static void make_bands(ibtfo_case *c, const std::vector<unsigned> &tiles)
         const int tb = (k == NBANDS) ? nty : (int)((long long)(2 * k - 1) * nty / (2 * NBANDS - 2));
         c->band_rows[k] = (k == NBANDS) ? g.N : std::min(g.N, g.ng + tb * TILE_Y + 2);
         c->out_rows[k] = (k == NBANDS) ? g.N : std::min(g.N, g.ng + tb * TILE_Y);
-        while (t < tiles.size() && (int)(tiles[t] >> 16) < tb)
+        while (t < tiles.size() && tile_jy(tiles[t]) < tb)
             t++;
         c->band_tiles[k] = (k == NBANDS) ? (int)tiles.size() : (int)t;
     }
@@ -233,7 +233,7 @@ static void make_bands(ibtfo_case *c, const std::vector<unsigned> &tiles)
         int lo = g.M, hi = 0;
         for (int q = c->band_tiles[k]; q < c->band_tiles[k + 1]; q++)
         {
-            const int tx = (int)(tiles[q] & 0xFFFFu);
+            const int tx = tile_ix(tiles[q]);
             lo = std::min(lo, g.ng + tx * TILE_X);
             hi = std::max(hi, std::min(g.ng + g.n_x, g.ng + (tx + 1) * TILE_X));
         }
@@ -309,7 +309,7 @@ static void make_in_boxes(ibtfo_case *c, const std::vector<unsigned> &tiles)
     const int halo = std::max(2, g.ng);
     for (unsigned t : tiles)
     {
-        const int i0 = g.ng + (int)(t & 0xFFFFu) * TILE_X, j0 = g.ng + (int)(t >> 16) * TILE_Y;
+        const int i0 = g.ng + tile_ix(t) * TILE_X, j0 = g.ng + tile_jy(t) * TILE_Y;
         add(j0 - halo, j0 + TILE_Y + halo, i0 - halo, i0 + TILE_X + halo);
     }
     for (int k = 0; k < NBANDS; k++)
@@ -889,12 +889,13 @@ static void enqueue_advance(ibtfo_case *c, int guard)
     count_launch();
 }
 
-static void enqueue_step(ibtfo_case *c, int guard)
+// the sweep part of one iteration: Time = RK2, the first stage and its
+// Boundary + Global_Boundary, then the second stage with the average (the
+// loop accounting happens there); else the single sweep
+static void enqueue_sweeps(ibtfo_case *c, int guard)
 {
     if (c->cfg.time_advance == IBTFO_TIME_RK2)
     {
-        // first stage and its Boundary + Global_Boundary, then the second
-        // stage with the average (the loop accounting happens there)
         SweepArgs a = sweep_args(c, guard);
         a.stage = 1;
         c->sweep(a, dim3(c->ntiles), dim3(TILE_X * TILE_Y), c->stream);
@@ -903,10 +904,14 @@ static void enqueue_step(ibtfo_case *c, int guard)
         a.stage = 2;
         c->sweep(a, dim3(c->ntiles), dim3(TILE_X * TILE_Y), c->stream);
         count_launch();
-        enqueue_boundary(c);
         return;
     }
     enqueue_advance(c, guard);
+}
+
+static void enqueue_step(ibtfo_case *c, int guard)
+{
+    enqueue_sweeps(c, guard);
     enqueue_boundary(c);
 }
 
@@ -1472,7 +1477,7 @@ ibtfo_status ibtfo_enqueue_sweep(ibtfo_case *c)
     if (!c->state)
         return fail(IBTFO_ESTATE, "no state: call ibtfo_set_state first");
     cudaSetDevice(c->device);
-    enqueue_advance(c, 1);
+    enqueue_sweeps(c, 1);
     CK(cudaGetLastError());
     return IBTFO_OK;
 }

@@ -76,8 +76,8 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y, PREC == 2 ? 4 : 1) ccm_sweep_k
     const long long P = g.plane;
     const int pitch = g.pitch;
     const unsigned tile = a.tiles[blockIdx.x];
-    const int i0 = g.ng + (int)(tile & 0xFFFFu) * TX;
-    const int j0 = g.ng + (int)(tile >> 16) * TY;
+    const int i0 = g.ng + tile_ix(tile) * TX;
+    const int j0 = g.ng + tile_jy(tile) * TY;
     const int tid = threadIdx.x;
     if (tid == 0)
     {

@@ -247,7 +247,10 @@ __global__ void scheme_index_kernel(GridDesc g, int bc, const double *__restrict
 
 static inline unsigned nblk(long long n, int b) { return (unsigned)((n + b - 1) / b); }
 
-// per tx x ty sweep tile: the number of interior fluid (or cut) cells it holds
+// per tx x ty sweep tile: the number of interior fluid (or cut) cells it
+// holds, plus TILE_COUNT_INTERIOR when every cell of the tile and of its
+// one-cell ring is an interior fluid cell
+constexpr int TILE_COUNT_INTERIOR = 1 << 30;
 __global__ void tile_counts_kernel(GridDesc g, const uint8_t *__restrict__ type, int tx, int ty, int ntx, int nty,
                                    int *counts)
 {
@@ -260,7 +263,15 @@ __global__ void tile_counts_kernel(GridDesc g, const uint8_t *__restrict__ type,
     for (int j = j0; j < j0 + ty && j < g.ng + g.n_y; j++)
         for (int i = i0; i < i0 + tx && i < g.ng + g.n_x; i++)
             n += updated_cell(type[(long long)j * g.pitch + i]) ? 1 : 0;
-    counts[t] = n;
+    bool interior = i0 - 1 >= g.ng && j0 - 1 >= g.ng && i0 + tx < g.ng + g.n_x && j0 + ty < g.ng + g.n_y;
+    for (int j = j0 - 1; j <= j0 + ty && interior; j++)
+        for (int i = i0 - 1; i <= i0 + tx; i++)
+            if (type[(long long)j * g.pitch + i] != CELL_FLUID)
+            {
+                interior = false;
+                break;
+            }
+    counts[t] = n | (interior ? TILE_COUNT_INTERIOR : 0);
 }
 
 int active_tile_list(const GridDesc &g, const uint8_t *d_type, int tx, int ty, std::vector<unsigned> &list,
@@ -285,8 +296,9 @@ int active_tile_list(const GridDesc &g, const uint8_t *d_type, int tx, int ty, s
     for (int t = 0; t < n; t++)
         if (counts[t])
         {
-            list.push_back((unsigned)(t % ntx) | ((unsigned)(t / ntx) << 16));
-            work.push_back(counts[t]);
+            const bool interior = (counts[t] & TILE_COUNT_INTERIOR) != 0;
+            list.push_back((unsigned)(t % ntx) | ((unsigned)(t / ntx) << 16) | (interior ? TILE_INTERIOR : 0u));
+            work.push_back(counts[t] & (TILE_COUNT_INTERIOR - 1));
         }
     if (list.empty())
         list.push_back(0u); // a tile without fluid still runs the loop accounting

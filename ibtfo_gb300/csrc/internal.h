@@ -212,6 +212,14 @@ constexpr int TILE_Y = 8;
 // per cell, not 1.69.  Every sweep CTA has TILE_X x TILE_Y threads.
 constexpr int FAST_TILE_Y = 16;
 
+// A tile-list entry: the tile's column index in bits 0-15, its row index in
+// bits 16-30, and TILE_INTERIOR when every cell of the tile and of the
+// one-cell ring around it is an interior fluid cell (the sweep then solves
+// every face without looking at cell types).
+constexpr unsigned TILE_INTERIOR = 0x80000000u;
+__host__ __device__ __forceinline__ int tile_ix(unsigned t) { return (int)(t & 0xFFFFu); }
+__host__ __device__ __forceinline__ int tile_jy(unsigned t) { return (int)((t >> 16) & 0x7FFFu); }
+
 // the sweep of a configuration over TILE_X x ty tiles (capi.cu)
 SweepLaunch sweep_launcher(int scheme, int riemann, int limiter, int precision, int ty);
 void launch_fill(const FillArgs &a, cudaStream_t s);
@@ -294,7 +302,8 @@ constexpr int FILL_THREADS = 64;
 
 struct BatchKernel
 {
-    void (*launch)(const BatchHeader *h, int grid, cudaStream_t s);
+    // stage: 0 a whole step; Time = RK2: 1 the first stage, 2 the second
+    void (*launch)(const BatchHeader *h, int grid, cudaStream_t s, int stage);
     int (*prepare)(); // sets the shared-memory limit, returns resident CTAs per SM (0 on failure)
 };
 // precision: 1 = fp64_fast, 2 = FP32 compensated (strict FP64 runs one case per launch)
@@ -328,7 +337,8 @@ void vtk_writer_destroy(VtkWriter *w, cudaStream_t s);
 // the tiles of TILE_X x ty cells holding fluid cells, on the device and (host_list) on the host
 int active_tiles(const GridDesc &g, const uint8_t *d_type, int ty, unsigned **d_tiles, int *ntiles, cudaStream_t s,
                  std::vector<unsigned> *host_list = nullptr);
-// host list of the tx x ty tiles holding at least one fluid cell (bx | by << 16);
+// host list of the tx x ty tiles holding at least one fluid cell (bx | by << 16,
+// with TILE_INTERIOR where it applies);
 // 0, or 2 (allocation) / 5 (CUDA error)
 int active_tile_list(const GridDesc &g, const uint8_t *d_type, int tx, int ty, std::vector<unsigned> &list,
                      cudaStream_t s);

@@ -28,25 +28,47 @@
 
 namespace ibtfo {
 
-// velocities and pressure of a base state (FP32)
+// reciprocal density, velocities and pressure of a base state (FP32)
 struct DeltaBase
 {
-    float un, ut, p;
+    float ir, un, ut, p;
 };
 
 template <int NRM>
 __device__ __forceinline__ DeltaBase delta_base(const float U[4], const GasConst<float> &K)
 {
     DeltaBase b;
-    const float ir = rcp_t(U[0]);
-    b.un = U[NRM] * ir;
-    b.ut = U[3 - NRM] * ir;
+    b.ir = rcp_t(U[0]);
+    b.un = U[NRM] * b.ir;
+    b.ut = U[3 - NRM] * b.ir;
     b.p = K.gm1 * fmaf(-0.5f, fmaf(U[NRM], b.un, U[3 - NRM] * b.ut), U[3]);
     return b;
 }
 
+// the primitive variables of a state from its base (no second reciprocal)
+__device__ __forceinline__ Prim<float> prim_of_base(const float U[4], const DeltaBase &b, const GasConst<float> &K)
+{
+    Prim<float> s;
+    s.r = U[0];
+    s.ir = b.ir;
+    s.un = b.un;
+    s.ut = b.ut;
+    s.p = b.p;
+    s.gi = K.g * b.ir;
+    s.a = sqrt_t(s.gi * s.p);
+    return s;
+}
+
+// physical() from the primitive variables: positive density and an internal
+// energy p / (gamma - 1) above 1e-6 of E (NaN fails)
+__device__ __forceinline__ bool physical_prim(float r, float p, float E, const GasConst<float> &K)
+{
+    return r > 0.0f && p * K.igm1 > 1e-6f * fabsf(E);
+}
+
 // dF = F(U_a + d) - F(U_a), normal direction NRM, from the base state U_a
-// (FP32 values, velocities and pressure in `a`) and the difference d:
+// (FP32 values, velocities and pressure in `a`), the difference d and
+// irb = 1 / (rho_a + d rho):
 //   du_n = (d m_n - u_n d rho) / rho_b          (u = m / rho)
 //   d(m_n u_n) = m_nb du_n + u_na d m_n,  d(m_t u_t) = m_tb du_t + u_ta d m_t
 //   dp = (gamma - 1) (dE - (d(m_n u_n) + d(m_t u_t)) / 2)
@@ -54,10 +76,9 @@ __device__ __forceinline__ DeltaBase delta_base(const float U[4], const GasConst
 // (components in state order; exact identities, so the rounding is relative
 // to the differences).
 template <int NRM>
-__device__ __forceinline__ void delta_flux(const float Ua[4], const DeltaBase &a, const float d[4],
+__device__ __forceinline__ void delta_flux(const float Ua[4], const DeltaBase &a, const float d[4], float irb,
                                            const GasConst<float> &K, float dF[4])
 {
-    const float irb = rcp_t(Ua[0] + d[0]);
     const float dun = (d[NRM] - a.un * d[0]) * irb;
     const float dut = (d[3 - NRM] - a.ut * d[0]) * irb;
     const float mnb = Ua[NRM] + d[NRM], mtb = Ua[3 - NRM] + d[3 - NRM];
@@ -71,8 +92,10 @@ __device__ __forceinline__ void delta_flux(const float Ua[4], const DeltaBase &a
 }
 
 // one face in difference form: cells c0 c1 | c2 c3 across it (hi and lo
-// parts), normal NRM; P = F_face - F(c1), Q = F_face - F(c2).  h2 = dt/(2h)
-// for the MHM predictor.
+// parts), normal NRM; P = F_face - F(c1), Q = F_face - F(c2).  hp = dt/(2h)
+// for the MHM predictor.  The reciprocal densities of the cell and face
+// states serve both the primitive variables and the flux differences, and
+// the positivity tests read the primitive variables.
 template <int SCH, int LIM, int NRM>
 __device__ __forceinline__ void face_delta(const float h0[4], const float l0[4], const float h1[4],
                                            const float l1[4], const float h2[4], const float l2[4],
@@ -105,25 +128,7 @@ __device__ __forceinline__ void face_delta(const float h0[4], const float l0[4],
     }
     const DeltaBase bL = delta_base<NRM>(UcL, K), bR = delta_base<NRM>(UcR, K);
     float dF[4], fL[4], fR[4];
-    delta_flux<NRM>(UcL, bL, D1, K, dF);
-    if (SCH != GODUNOV)
-    {
-        delta_flux<NRM>(UcL, bL, dL, K, fL);
-        delta_flux<NRM>(UcR, bR, dR, K, fR);
-        if (SCH == MHM)
-        {
-            // U_L, U_R += (dt / 2h) (F(U_L) - F(U_R)), F(U_L) - F(U_R) = dF_L - dF - dF_R
-#pragma unroll
-            for (int k = 0; k < 4; k++)
-            {
-                const float m = hp * ((fL[k] - dF[k]) - fR[k]);
-                dL[k] += m;
-                dR[k] += m;
-            }
-            delta_flux<NRM>(UcL, bL, dL, K, fL);
-            delta_flux<NRM>(UcR, bR, dR, K, fR);
-        }
-    }
+    delta_flux<NRM>(UcL, bL, D1, bR.ir, K, dF);
     float UL[4], UR[4];
 #pragma unroll
     for (int k = 0; k < 4; k++)
@@ -131,25 +136,55 @@ __device__ __forceinline__ void face_delta(const float h0[4], const float l0[4],
         UL[k] = h1[k] + (l1[k] + dL[k]);
         UR[k] = h2[k] + (l2[k] + dR[k]);
     }
-    if (SCH != GODUNOV && physical(UcL) && physical(UcR) && !(physical(UL) && physical(UR)))
+    Prim<float> L, R;
+    if (SCH == GODUNOV)
     {
-        // positivity fallback: the first-order pair (the two cell averages)
-#pragma unroll
-        for (int k = 0; k < 4; k++)
-        {
-            dL[k] = dR[k] = fL[k] = fR[k] = 0.0f;
-            UL[k] = UcL[k];
-            UR[k] = UcR[k];
-        }
-    }
-    else if (SCH == GODUNOV)
-    {
+        L = prim_of_base(UcL, bL, K);
+        R = prim_of_base(UcR, bR, K);
 #pragma unroll
         for (int k = 0; k < 4; k++)
             fL[k] = fR[k] = 0.0f;
     }
+    else
+    {
+        if (SCH == MHM)
+        {
+            // U_L, U_R += (dt / 2h) (F(U_L) - F(U_R)), F(U_L) - F(U_R) = dF_L - dF - dF_R
+            delta_flux<NRM>(UcL, bL, dL, rcp_t(UL[0]), K, fL);
+            delta_flux<NRM>(UcR, bR, dR, rcp_t(UR[0]), K, fR);
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+            {
+                const float m = hp * ((fL[k] - dF[k]) - fR[k]);
+                dL[k] += m;
+                dR[k] += m;
+                UL[k] = h1[k] + (l1[k] + dL[k]);
+                UR[k] = h2[k] + (l2[k] + dR[k]);
+            }
+        }
+        L = prim_fast<float, NRM>(UL, K);
+        R = prim_fast<float, NRM>(UR, K);
+        if (physical_prim(UcL[0], bL.p, UcL[3], K) && physical_prim(UcR[0], bR.p, UcR[3], K) &&
+            !(physical_prim(L.r, L.p, UL[3], K) && physical_prim(R.r, R.p, UR[3], K)))
+        {
+            // positivity fallback: the first-order pair (the two cell averages)
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+            {
+                dL[k] = dR[k] = fL[k] = fR[k] = 0.0f;
+                UL[k] = UcL[k];
+                UR[k] = UcR[k];
+            }
+            L = prim_of_base(UcL, bL, K);
+            R = prim_of_base(UcR, bR, K);
+        }
+        else
+        {
+            delta_flux<NRM>(UcL, bL, dL, L.ir, K, fL);
+            delta_flux<NRM>(UcR, bR, dR, R.ir, K, fR);
+        }
+    }
     // Toro's PVRS wave-speed estimates from the face states (hll_plain)
-    const Prim<float> L = prim_fast<float, NRM>(UL, K), R = prim_fast<float, NRM>(UR, K);
     float p_star = 0.5f * (L.p + R.p) + 0.125f * (L.un - R.un) * ((L.r + R.r) * (L.a + R.a));
     p_star = p_star > 0.0f ? p_star : 0.0f;
     const float t = K.c1 * p_star;

@@ -106,6 +106,7 @@ ibtfo_config config_of(const ibtfo_server *s, const ibtfo_request &r)
     k.boundary = r.boundary;
     k.global_boundary = r.global_boundary;
     k.precision = s->cfg.precision;
+    k.time_advance = s->cfg.time_advance;
     return k;
 }
 
@@ -296,6 +297,7 @@ ibtfo_status ibtfo_server_create(const ibtfo_server_config *cfg, ibtfo_server **
     bc.tile_shape = cfg->tile_shape >= 0 ? cfg->tile_shape : IBTFO_TILE_32x8;
     bc.ctas_per_sm = cfg->ctas_per_sm;
     bc.graph_steps = std::min(16, s->cfg.chunk_steps);
+    bc.time_advance = cfg->time_advance;
     ibtfo_status e = ibtfo_batch_create(&bc, &s->batch);
     if (e != IBTFO_OK)
     {

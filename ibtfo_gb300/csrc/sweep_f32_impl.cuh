@@ -88,7 +88,8 @@ template <int SCH, int RIE, int LIM, int TX, int TY, int NT>
 __device__ __forceinline__ void sweep_tile32(SweepSmem32<TX, TY> &s, const GridDesc &g, const float *__restrict__ U,
                                              float *__restrict__ V, const uint8_t *__restrict__ type, int i0, int j0,
                                              double dt, CellStats32 &cs, int stage = 0,
-                                             const CUtensorMap *tmap = nullptr, int *status = nullptr)
+                                             const CUtensorMap *tmap = nullptr, int *status = nullptr,
+                                             bool interior = false)
 {
     constexpr int WX = TX + 4, WY = TY + 4;
     const long long P = g.plane;
@@ -117,7 +118,7 @@ __device__ __forceinline__ void sweep_tile32(SweepSmem32<TX, TY> &s, const GridD
         }
     }
     // cell flags and the face list while the copy is in flight
-    tile_faces_build<TX, TY, NT>(s.tf, s.sKeep, g, type, i0, j0);
+    tile_faces_build<TX, TY, NT>(s.tf, s.sKeep, g, type, i0, j0, interior);
     if (tmap)
     {
         staged = __syncthreads_and(mbar_wait(&bar, 0));
@@ -226,7 +227,7 @@ __device__ __forceinline__ void sweep_tile32(SweepSmem32<TX, TY> &s, const GridD
     {
         const int c = cell % TX, r = cell / TX;
         const int i = i0 + c, j = j0 + r;
-        if (s.tf.fluid[r + 1][c + 1])
+        if (tile_cell_fluid(s.tf, r, c))
         {
             const long long o = (long long)j * pitch + i;
             const int kp = s.sKeep[r + 1][c], km = s.sKeep[r][c];
@@ -310,7 +311,7 @@ __device__ __forceinline__ void sweep_tile32_delta(SweepSmem32D<TX, TY> &s, cons
                                                    const float *__restrict__ U, float *__restrict__ V,
                                                    const uint8_t *__restrict__ type, int i0, int j0, double dt,
                                                    CellStats32 &cs, int stage = 0, const CUtensorMap *tmap = nullptr,
-                                                   int *status = nullptr)
+                                                   int *status = nullptr, bool interior = false)
 {
     constexpr int WX = TX + 4, WY = TY + 4;
     const long long P = g.plane;
@@ -338,7 +339,7 @@ __device__ __forceinline__ void sweep_tile32_delta(SweepSmem32D<TX, TY> &s, cons
             tma_load_3d(&s.sU[4][0][0], tmap, i0 - 2, j0 - 2, 4, &bar);
         }
     }
-    tile_faces_build<TX, TY, NT>(s.tf, s.sKeep, g, type, i0, j0);
+    tile_faces_build<TX, TY, NT>(s.tf, s.sKeep, g, type, i0, j0, interior);
     if (tmap)
     {
         staged = __syncthreads_and(mbar_wait(&bar, 0));
@@ -420,7 +421,7 @@ __device__ __forceinline__ void sweep_tile32_delta(SweepSmem32D<TX, TY> &s, cons
     for (int cell = tid; cell < TX * TY; cell += NT)
     {
         const int c = cell % TX, r = cell / TX;
-        if (s.tf.fluid[r + 1][c + 1])
+        if (tile_cell_fluid(s.tf, r, c))
         {
             const long long o = (long long)(j0 + r) * pitch + (i0 + c);
             const float lx = s.sC[0], ly = s.sC[1];
@@ -550,17 +551,18 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y, RIE == HLLT ? 3 : (TY == TILE_
     float *V = reinterpret_cast<float *>(cur ? a.buf0 : a.buf1);
     const unsigned bid = a.tile0 + blockIdx.x;
     const unsigned tile = a.tiles[bid];
-    const int i0 = g.ng + (int)(tile & 0xFFFFu) * TILE_X;
-    const int j0 = g.ng + (int)(tile >> 16) * TY;
+    const int i0 = g.ng + tile_ix(tile) * TILE_X;
+    const int j0 = g.ng + tile_jy(tile) * TY;
+    const bool interior = (tile & TILE_INTERIOR) != 0;
     CellStats32 cs;
     if constexpr (RIE == HLLT)
         sweep_tile32_delta<SCH, RIE, LIM, TILE_X, TY, NT>(*reinterpret_cast<SweepSmem32D<TILE_X, TY> *>(smem_raw), g,
                                                           U, V, a.type, i0, j0, dt, cs, a.stage,
-                                                          a.tma ? &a.tmap[cur] : nullptr, &st->status);
+                                                          a.tma ? &a.tmap[cur] : nullptr, &st->status, interior);
     else
         sweep_tile32<SCH, RIE, LIM, TILE_X, TY, NT>(*reinterpret_cast<SweepSmem32<TILE_X, TY> *>(smem_raw), g, U, V,
                                                     a.type, i0, j0, dt, cs, a.stage, a.tma ? &a.tmap[cur] : nullptr,
-                                                    &st->status);
+                                                    &st->status, interior);
     block_reduce_finalize32<NT>(cs, st, a.partial, g, a.nblocks ? a.nblocks : gridDim.x, bid, a.stage == 1);
 }
 

@@ -279,7 +279,8 @@ template <int SCH, int RIE, int LIM, int FAST, int TX, int TY, int NT>
 __device__ __forceinline__ void sweep_tile64(SweepSmem64<TX, TY> &s, const GridDesc &g, const double *__restrict__ U,
                                              double *__restrict__ V, const uint8_t *__restrict__ type, int i0, int j0,
                                              double dt, CellStats &cs, int stage = 0,
-                                             const CUtensorMap *tmap = nullptr, int *status = nullptr)
+                                             const CUtensorMap *tmap = nullptr, int *status = nullptr,
+                                             bool interior = false)
 {
     constexpr int WX = TX + 4, WY = TY + 4;
     const long long P = g.plane;
@@ -308,7 +309,7 @@ __device__ __forceinline__ void sweep_tile64(SweepSmem64<TX, TY> &s, const GridD
         }
     }
     // cell flags and the face list while the copy is in flight
-    tile_faces_build<TX, TY, NT>(s.tf, s.sKeep, g, type, i0, j0);
+    tile_faces_build<TX, TY, NT>(s.tf, s.sKeep, g, type, i0, j0, interior);
     if (tmap)
     {
         staged = __syncthreads_and(mbar_wait(&bar, 0));
@@ -442,7 +443,7 @@ __device__ __forceinline__ void sweep_tile64(SweepSmem64<TX, TY> &s, const GridD
     {
         const int c = cell % TX, r = cell / TX;
         const int i = i0 + c, j = j0 + r;
-        if (s.tf.fluid[r + 1][c + 1])
+        if (tile_cell_fluid(s.tf, r, c))
         {
             const int kp = s.sKeep[r + 1][c], km = s.sKeep[r][c];
             const double lx = FAST ? s.sC[0] : 0.0, ly = FAST ? s.sC[1] : 0.0;
@@ -510,11 +511,12 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y, (FAST && (RIE == HLL || RIE ==
     // the cell type), so the launch covers the active tiles only
     const unsigned bid = a.tile0 + blockIdx.x;
     const unsigned tile = a.tiles[bid];
-    const int i0 = g.ng + (int)(tile & 0xFFFFu) * TILE_X;
-    const int j0 = g.ng + (int)(tile >> 16) * TY;
+    const int i0 = g.ng + tile_ix(tile) * TILE_X;
+    const int j0 = g.ng + tile_jy(tile) * TY;
+    const bool interior = (tile & TILE_INTERIOR) != 0;
     CellStats cs;
     sweep_tile64<SCH, RIE, LIM, FAST, TILE_X, TY, NT>(s, g, U, V, a.type, i0, j0, dt, cs, a.stage,
-                                                      a.tma ? &a.tmap[cur] : nullptr, &st->status);
+                                                      a.tma ? &a.tmap[cur] : nullptr, &st->status, interior);
     block_reduce_finalize<NT>(cs, st, a.partial, g, true, false, a.nblocks ? a.nblocks : gridDim.x, bid,
                               a.stage == 1);
 }

@@ -45,8 +45,8 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y) lax_kernel(const SweepArgs a)
     double *V = cur ? a.buf0 : a.buf1;
     const unsigned bid = a.tile0 + blockIdx.x;
     const unsigned tile = a.tiles[bid];
-    const int i0 = g.ng + (int)(tile & 0xFFFFu) * TILE_X;
-    const int j0 = g.ng + (int)(tile >> 16) * TILE_Y;
+    const int i0 = g.ng + tile_ix(tile) * TILE_X;
+    const int j0 = g.ng + tile_jy(tile) * TILE_Y;
     const long long P = g.plane;
     const int pitch = g.pitch;
     const double gam = g.gamma;

@@ -8,8 +8,8 @@
 // side, taken from a compacted list so that every warp works on faces that
 // are needed.  The one other reader is the reference's Y-face slot reuse: a Y
 // face (i, j-1/2) that keeps the X-face flux of its slot reads the X face
-// (i+1/2, j-1), which tile_faces_aliased solves after the Y faces, where the
-// list left it out.
+// (i+1/2, j-1), which the sweep solves after the Y faces where the list left
+// it out (x_face_listed).
 //
 // Indexing, tile-local: the flag plane covers cells (i0-1 .. i0+TX,
 // j0-1 .. j0+TY) as fluid[ly][lx] with lx = i - (i0-1), ly = j - (j0-1); the
@@ -32,6 +32,7 @@ struct TileFaces
     unsigned short list[NXF + NYF];           // the candidates some fluid cell reads
     int n;                                    // list length
     int all;                                  // every cell of the flag plane is fluid: the list is 0..NXF+NYF-1
+                                              // (the flags are then not read)
 };
 
 // X face (i + 1/2, j) of candidate q < NXF: sF row r (1..TY), column fc (0..TX),
@@ -56,17 +57,29 @@ __device__ __forceinline__ void y_face_of(int q, int &r, int &c)
 }
 
 // Flags of the tile's cells and their one-cell ring, and the list of the
-// faces to solve.  sKeep (the Y-face slot-reuse bits) is cleared for the Y
-// faces left out, so that nothing reads a stale bit.  All NT threads call it;
+// faces to solve (for a tile the list marks interior: `all`, no flags
+// staged).  sKeep (the Y-face slot-reuse bits) is cleared for the Y faces
+// left out, so that nothing reads a stale bit.  All NT threads call it;
 // ends with a barrier.
 template <int TX, int TY, int NT>
 __device__ __forceinline__ void tile_faces_build(TileFaces<TX, TY> &f, unsigned char (*keep)[TX],
                                                  const GridDesc &g, const uint8_t *__restrict__ type, int i0,
-                                                 int j0)
+                                                 int j0, bool interior = false)
 {
     constexpr int W = TX + 2, H = TY + 2;
     constexpr int NC = TileFaces<TX, TY>::NXF + TileFaces<TX, TY>::NYF;
     const int tid = threadIdx.x;
+    if (interior)
+    {
+        // the tile list marks the tile: every cell and its ring is fluid
+        if (tid == 0)
+        {
+            f.n = NC;
+            f.all = 1;
+        }
+        __syncthreads();
+        return;
+    }
     int mine = 1;
     for (int q = tid; q < W * H; q += NT)
     {
@@ -121,6 +134,13 @@ __device__ __forceinline__ void tile_faces_build(TileFaces<TX, TY> &f, unsigned 
     if (tid == 0)
         f.all = 0;
     __syncthreads();
+}
+
+// whether cell (tile-local column c, row r) is updated
+template <int TX, int TY>
+__device__ __forceinline__ bool tile_cell_fluid(const TileFaces<TX, TY> &f, int r, int c)
+{
+    return f.all || f.fluid[r + 1][c + 1];
 }
 
 // candidate of list position t

@@ -45,7 +45,8 @@ enum { IBTFO_SCHEME_MUSCL = 0, IBTFO_SCHEME_MHM = 1, IBTFO_SCHEME_GODUNOV = 2, I
  * then 0.5 (U0 + U1 + dt L(U1)) on fluid cells, both stages with the dt of
  * the step (the two-stage method Src/Base/TimeAdvance/RK2/RK2.cpp describes;
  * that file itself does not compile); in the FP32 form the average is taken
- * on the (hi, lo) pairs.  Not with cut cells or in batches. */
+ * on the (hi, lo) pairs.  Not with cut cells; a batch runs one Time key
+ * for all its cases. */
 enum { IBTFO_TIME_SINGLESTEP = 0, IBTFO_TIME_RK2 = 1 };
 /* HLLC is the reference's HLLC directory, whose solver is HLL (including the
  * Y-face slot reuse); HLLC_TORO is a contact-restoring HLLC with no
@@ -238,7 +239,9 @@ ibtfo_status ibtfo_advance(ibtfo_case *c, int nsteps);
 /* The two launches of one guarded iteration, for callers that time or
  * capture them separately: the fused sweep (Advance + ComputeDt +
  * CaculateMass + loop accounting) and the boundary pass (ghost-fluid
- * Boundary + Global_Boundary).  ibtfo_advance(c, 1) == sweep then boundary. */
+ * Boundary + Global_Boundary).  ibtfo_advance(c, 1) == sweep then boundary.
+ * Time = RK2: the "sweep" is the first stage, its boundary pass and the
+ * second stage. */
 ibtfo_status ibtfo_enqueue_sweep(ibtfo_case *c);
 ibtfo_status ibtfo_enqueue_boundary(ibtfo_case *c);
 /* One iteration regardless of the loop condition; waits and reports. */
@@ -334,7 +337,9 @@ typedef struct ibtfo_batch_config {
     int tile_shape;   /* IBTFO_TILE_*: interior cells per CTA (256 threads) */
     int ctas_per_sm;  /* resident CTAs per SM of the persistent sweep (0: the occupancy limit) */
     int graph_steps;  /* steps per captured graph (0: 16) */
-    int reserved[5];
+    int time_advance; /* IBTFO_TIME_* of every case: RK2 steps are two sweeps, each followed by
+                         the boundary pass */
+    int reserved[4];
 } ibtfo_batch_config;
 
 typedef struct ibtfo_batch_tiling {
@@ -396,7 +401,8 @@ typedef struct ibtfo_server_config {
     int chunk_steps;         /* steps per scheduling round (0: 32) */
     int tile_shape;          /* IBTFO_TILE_*, or -1: autotune once 4 cases are active */
     int ctas_per_sm;         /* 0: the occupancy limit */
-    int reserved[6];
+    int time_advance;        /* IBTFO_TIME_* of every case */
+    int reserved[5];
 } ibtfo_server_config;
 
 typedef struct ibtfo_request {

@@ -8,7 +8,7 @@ sum is bitwise equal as well (other shapes sum the per-tile mass partials in
 another order: relative 1e-12).  Covers uneven grid sizes, ghost-fluid and
 plain boundaries, walls and periodic domain edges (the two-phase boundary
 pass), per-case loop ends, cases joining and leaving between steps, tile
-shapes, and the autotuner's trial steps."""
+shapes, Time = RK2, and the autotuner's trial steps."""
 import numpy as np
 import pytest
 
@@ -44,16 +44,16 @@ def specs():
     return out
 
 
-def make(spec, precision):
+def make(spec, precision, **over):
     w, phi, init = spec
-    c = ib.Case.from_workload(w, precision=precision, max_iter=2 ** 31 - 1)
+    c = ib.Case.from_workload(w, precision=precision, max_iter=2 ** 31 - 1, **over)
     c.setup_geometry(phi)
     c.set_state(init(c.cell_types()))
     return c
 
 
-def alone(spec, precision, n):
-    with make(spec, precision) as c:
+def alone(spec, precision, n, **over):
+    with make(spec, precision, **over) as c:
         c.advance(n)
         return c.get_state(), c.progress()
 
@@ -92,6 +92,34 @@ def test_batch_equals_alone(precision, shape):
     # the short case stopped at its own t_end; the others ran every step
     assert ref[3][1]["iter"] < n and ref[3][1]["now_t"] >= 0.01
     assert all(r[1]["iter"] == n for r in ref[:3])
+    for c in cs:
+        c.close()
+
+
+@pytest.mark.parametrize("precision", ["fp32c", "fp64_fast"])
+@pytest.mark.parametrize("riemann", ["HLLC", "HLL_Toro"])
+def test_rk2_batch_equals_alone(precision, riemann):
+    """Time = RK2 in a batch (two sweeps per step, each followed by the
+    boundary pass) equals the same cases run alone with RK2, bit for bit on
+    the case path's tiles (32x16), for the reference's HLL (HLLC key) and for
+    HLL_Toro (whose FP32 form solves faces in difference form)."""
+    n = 20  # one graph launch of 16 steps + 4 single steps
+    sp = specs()
+    over = dict(time="RK2", riemann=riemann)
+    ref = [alone(s, precision, n, **over) for s in sp]
+    cs = [make(s, precision, **over) for s in sp]
+    with ib.Batch("MUSCL", riemann, "minmod", precision, tile_shape="32x16", time="RK2") as b:
+        for c in cs:
+            b.add(c)
+        b.advance(n)
+        b.synchronize()
+        for k, c in enumerate(cs):
+            same((c.get_state(), c.progress()), ref[k])
+            assert ref[k][1]["nan_cells"] == 0
+        # a single-step case does not join an RK2 batch
+        with make(sp[1], precision, riemann=riemann) as other:
+            with pytest.raises(ib.IbtfoError):
+                b.add(other)
     for c in cs:
         c.close()
 

@@ -74,7 +74,10 @@ def test_stationary_contact(riemann, exact):
 
 
 def test_fp32c_isentropic_vortex_hllc():
-    w = cases.vortex_periodic(256)
+    # the contact-restoring HLLC with single steps (the FP32 form's plain,
+    # non-difference face solve); the vortex workload's own solver is covered
+    # in test_gpu_forms.py and test_gpu_fullsize.py
+    w = cases.vortex_periodic(256, riemann="HLLC_Toro", time="SingleStep")
     g = w.grid
     phi, u0 = cases.isentropic_vortex(g)
     res = {}

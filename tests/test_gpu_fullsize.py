@@ -11,8 +11,8 @@ and through size-independent properties where it does not:
   count and L1 density within 1e-10 (both FP64 keys); the host-array step (row bands
   copied while the sweep runs) bit for bit with put + step + get;
 * periodic isentropic vortex, 4096x4096, MHM + minmod: with the reference's
-  HLLC, within 1e-12 of the oracle after 3 steps; with the contact-restoring
-  HLLC_Toro (the timed workload), a periodic shift of the initial state gives
+  HLLC and single steps, within 1e-12 of the oracle after 3 steps; with the
+  timed workload's HLL_Toro and Time = RK2, a periodic shift of the initial state gives
   the same shift of the result bit for bit (tile seams land on other cells),
   mass and energy are conserved (FP64 to 1e-11 relative after 20 steps: the
   rounding of 16.7 M cell updates a step accumulates; the FP32 compensated
@@ -190,7 +190,7 @@ def interior_of(g, u):
 def test_vortex_full_size_matches_oracle():
     """4096x4096 periodic vortex with the reference's HLLC, 3 steps (the
     reference's HLLC goes to NaN on this flow after a few dozen steps, not in 3)."""
-    w = cases.vortex_periodic(4096, riemann="HLLC")
+    w = cases.vortex_periodic(4096, riemann="HLLC", time="SingleStep")
     g = w.grid
     phi, _ = cases.isentropic_vortex(g)
     u0 = periodic_state(g, vortex_interior(g))

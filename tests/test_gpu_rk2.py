@@ -119,14 +119,17 @@ def test_rk2_queued_steps_equal_single_steps():
     assert res[0][1]["now_t"] >= 0.05 and res[0][1]["iter"] < 45
 
 
-def test_rk2_and_lax_cases_stay_out_of_batches():
+def test_rk2_cases_join_rk2_batches_only_and_lax_stays_out():
     g = cases.Grid(64, 64, 2, 0.0, 0.0, 1.0, 1.0)
     phi, u0 = cases.sod_x(g)
     with ib.Case(64, 64, time="RK2", precision="fp64_fast") as c:
         c.setup_geometry(phi)
         c.set_state(u0)
         with ib.Batch("MUSCL", "HLL", "minmod", "fp64_fast") as b:
-            with pytest.raises(ib.IbtfoError, match="RK2"):
+            with pytest.raises(ib.IbtfoError, match="Time"):
                 b.add(c)
+        with ib.Batch("MUSCL", "HLL", "minmod", "fp64_fast", time="RK2") as b:
+            b.add(c)
+            assert len(b) == 1
     with pytest.raises(ib.IbtfoError):
         ib.Batch("Lax", "HLL", "minmod", "fp64_fast")
