@@ -14,7 +14,8 @@
 namespace ibtfo {
 
 template <int SCH, int RIE, int LIM, int PREC, int TX, int TY>
-__global__ void __launch_bounds__(BATCH_THREADS) batch_sweep_kernel(const BatchHeader *__restrict__ h, int stage)
+__global__ void __launch_bounds__(BATCH_THREADS, (PREC == 2 && RIE == HLLT) ? 3 : 1)
+    batch_sweep_kernel(const BatchHeader *__restrict__ h, int stage)
 {
     constexpr int NT = BATCH_THREADS;
     extern __shared__ __align__(128) unsigned char smem_raw[];
