@@ -83,3 +83,17 @@ def test_reference_arm_prints_on_rank_0_only():
     assert line["impl"] == "reference" and line["value"] > 0 and line["unit"] == line["metric"]
     assert line["cpu_baseline"]["kind"] in ("port", "reference") and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+
+
+def test_both_arms_report_the_same_config():
+    """The reference arm and the GPU arm describe the workload with the same
+    `config` dict (the arithmetic each runs is the line's own `precision`
+    key), so the two lines compare like for like."""
+    sys.path.insert(0, ROOT)
+    import bench
+    w = bench.workload()
+    cfg = bench.config_json(w)
+    assert cfg == bench.config_json(bench.workload())
+    assert "precision" not in cfg and "l2" not in cfg
+    assert (cfg["n_x"], cfg["n_y"], cfg["scheme"], cfg["riemann"], cfg["boundary"]) == \
+        (2048, 1024, "MUSCL", "HLLC", "IDWBaseGFM")
