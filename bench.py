@@ -691,10 +691,19 @@ def main():
                      snapshot=(rank == 0))
         cv = wv.grid.n_x * wv.grid.n_y
         sw_s = rv["sweep_ms"] * 1e-3 / kv
+        sweeps = 2 if wv.time == "RK2" else 1  # an RK2 step reads and writes the state twice
         forms[prec] = {"value": job_rate(world, cv, kv, rv["step_ms"] * 1e-3), "unit": METRIC,
-                       "steps": args.warmup + kv, "sweep_ms": rv["sweep_ms"] / kv,
-                       "roofline_frac": BYTES_PER_CELL * cv / sw_s / 1e9 / measured_peaks()[0]}
+                       "steps": args.warmup + kv, "sweep_ms": rv["sweep_ms"] / kv, "sweeps_per_step": sweeps,
+                       "roofline_frac": sweeps * BYTES_PER_CELL * cv / sw_s / 1e9 / measured_peaks()[0]}
         rhos[prec] = (rv.get("rho"), rv.get("rho_t"))
+    # for comparison: the FP32 sweep with the plain (not difference-form) face
+    # solve, as the contact-restoring HLLC with single steps runs it
+    wp = _cases.vortex_periodic(4096, riemann="HLLC_Toro", time="SingleStep")
+    rp = gpu_arm(args, rank, world, local_rank, precision="fp32c", e2e=False, w=wp, inputs=vortex_inputs, steps=kv)
+    forms["fp32c_plain_face_solve"] = {
+        "riemann": wp.riemann, "time": wp.time, "value": job_rate(world, cv, kv, rp["step_ms"] * 1e-3), "unit": METRIC,
+        "sweep_ms": rp["sweep_ms"] / kv,
+        "roofline_frac": BYTES_PER_CELL * cv / (rp["sweep_ms"] * 1e-3 / kv) / 1e9 / measured_peaks()[0]}
     if rank == 0:
         forms["errors"] = vortex_errors(wv, rhos)
         if not args.no_period:
