@@ -38,6 +38,17 @@ __global__ void __launch_bounds__(BATCH_THREADS, (PREC == 2 && RIE == HLLT) ? 3 
         const int i0 = g.ng + tile_ix(e.x) * TX;
         const int j0 = g.ng + tile_jy(e.x) * TY;
         const bool interior = (e.x & TILE_INTERIOR) != 0;
+        // the case's own tensor maps describe boxes of its one-case tiles
+        // (32x16 except under PVRS): the 32x16 shape stages tiles with them
+        const CUtensorMap *tm = nullptr;
+        if constexpr (TX == TILE_X && TY == FAST_TILE_Y && RIE != PVRS)
+            if (a.tma)
+            {
+                tm = &a.tmap[cur];
+                if (threadIdx.x == 0)
+                    tensormap_acquire(tm);
+            }
+        int *status = tm ? &st->status : nullptr;
         if constexpr (PREC == 2)
         {
             const float *U = reinterpret_cast<const float *>(cur ? a.buf1 : a.buf0);
@@ -45,11 +56,11 @@ __global__ void __launch_bounds__(BATCH_THREADS, (PREC == 2 && RIE == HLLT) ? 3 
             CellStats32 cs;
             if constexpr (RIE == HLLT)
                 sweep_tile32_delta<SCH, RIE, LIM, TX, TY, NT>(*reinterpret_cast<SweepSmem32D<TX, TY> *>(smem_raw), g,
-                                                              U, V, a.type, i0, j0, dt, cs, stage, nullptr, nullptr,
+                                                              U, V, a.type, i0, j0, dt, cs, stage, tm, status,
                                                               interior);
             else
                 sweep_tile32<SCH, RIE, LIM, TX, TY, NT>(*reinterpret_cast<SweepSmem32<TX, TY> *>(smem_raw), g, U, V,
-                                                        a.type, i0, j0, dt, cs, stage, nullptr, nullptr, interior);
+                                                        a.type, i0, j0, dt, cs, stage, tm, status, interior);
             block_reduce_finalize32<NT>(cs, st, a.partial, g, (unsigned)bc.ntiles, e.y, stage == 1);
         }
         else
@@ -58,7 +69,7 @@ __global__ void __launch_bounds__(BATCH_THREADS, (PREC == 2 && RIE == HLLT) ? 3 
             const double *U = cur ? a.buf1 : a.buf0;
             double *V = cur ? a.buf0 : a.buf1;
             CellStats cs;
-            sweep_tile64<SCH, RIE, LIM, 1, TX, TY, NT>(s, g, U, V, a.type, i0, j0, dt, cs, stage, nullptr, nullptr,
+            sweep_tile64<SCH, RIE, LIM, 1, TX, TY, NT>(s, g, U, V, a.type, i0, j0, dt, cs, stage, tm, status,
                                                        interior);
             block_reduce_finalize<NT>(cs, st, a.partial, g, true, false, (unsigned)bc.ntiles, e.y, stage == 1);
         }

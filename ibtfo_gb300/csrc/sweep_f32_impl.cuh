@@ -277,8 +277,10 @@ __device__ __forceinline__ void sweep_tile32(SweepSmem32<TX, TY> &s, const GridD
             cs.nans += (isnan(hi[0]) || isnan(hi[1]) || isnan(hi[2]) || isnan(hi[3])) ? 1 : 0;
         }
     }
-    if (tmap && !staged && tid == 0)
-        mbar_wait(&bar, 0); // bounded: the copy that missed the first wait
+    // a copy that missed the first wait is waited for once more (bounded);
+    // the barrier is then released for the next tile of a persistent CTA
+    if (tmap && tid == 0 && (staged || mbar_wait(&bar, 0)))
+        mbar_inval(&bar);
 }
 
 // Shared memory of one FP32 tile in difference form (HLL_Toro): the hi and lo
@@ -466,8 +468,10 @@ __device__ __forceinline__ void sweep_tile32_delta(SweepSmem32D<TX, TY> &s, cons
             cs.nans += (isnan(hi[0]) || isnan(hi[1]) || isnan(hi[2]) || isnan(hi[3])) ? 1 : 0;
         }
     }
-    if (tmap && !staged && tid == 0)
-        mbar_wait(&bar, 0); // bounded: the copy that missed the first wait
+    // a copy that missed the first wait is waited for once more (bounded);
+    // the barrier is then released for the next tile of a persistent CTA
+    if (tmap && tid == 0 && (staged || mbar_wait(&bar, 0)))
+        mbar_inval(&bar);
 }
 
 // Block reduction in FP32 (compensated for the mass); thread 0 converts the

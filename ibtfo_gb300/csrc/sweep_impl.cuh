@@ -479,8 +479,10 @@ __device__ __forceinline__ void sweep_tile64(SweepSmem64<TX, TY> &s, const GridD
                 cell_stats(v, gam, g.dx, g.dy, cs);
         }
     }
-    if (tmap && !staged && tid == 0)
-        mbar_wait(&bar, 0); // bounded: the copy that missed the first wait
+    // a copy that missed the first wait is waited for once more (bounded);
+    // the barrier is then released for the next tile of a persistent CTA
+    if (tmap && tid == 0 && (staged || mbar_wait(&bar, 0)))
+        mbar_inval(&bar);
 }
 
 // one case: one CTA of TILE_X x TILE_Y threads per active tile of TILE_X x TY

@@ -52,6 +52,22 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity)
     return done != 0;
 }
 
+// releases the barrier once its phase has completed and no copy is in
+// flight, so that the next tile of a persistent CTA can initialise it again
+__device__ __forceinline__ void mbar_inval(uint64_t *bar)
+{
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+// a tensor map that the host wrote into global memory (a batch's case
+// table) becomes visible to the tensor-copy unit: acquire fence of the
+// tensormap proxy on its 128 bytes, before the first copy that uses it
+__device__ __forceinline__ void tensormap_acquire(const CUtensorMap *map)
+{
+    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(reinterpret_cast<uint64_t>(map))
+                 : "memory");
+}
+
 // the bounded wait: each try_wait suspends for a hardware-chosen interval,
 // so this gives up after far longer than any copy takes
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity)
