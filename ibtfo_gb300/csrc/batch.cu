@@ -172,7 +172,7 @@ int fill_blocks(const FillArgs &f, int phase)
     const bool split = gfm && f.gb == GB_PERIODIC;
     const long long nring = 2LL * f.g.ng * f.g.n_x + 2LL * f.g.ng * f.g.N;
     const int rblocks = (int)((nring + FILL_THREADS - 1) / FILL_THREADS);
-    const int gblocks = (f.nghost + FILL_THREADS - 1) / FILL_THREADS;
+    const int gblocks = ghost_blocks(f.nghost);
     if (phase == 0)
         return (gfm ? gblocks : 0) + (split ? 0 : rblocks);
     return split ? rblocks : 0;

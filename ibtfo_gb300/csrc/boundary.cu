@@ -19,98 +19,123 @@
 
 namespace ibtfo {
 
+// The buffers of the state after the step (`next`, which the pass writes)
+// and before it (`prev`).  The reference's U_NEW at an updated interior cell
+// is next's value there, elsewhere prev's (the snapshot rule above); which
+// one a read takes is a static property of the geometry, resolved before the
+// pass reads the device state that names the buffers, so that the loads of a
+// record, of its cell types and of that state do not wait on one another.
 struct View
 {
     const double *next, *prev;
-    const uint8_t *type;
     GridDesc g;
-    long long P;
-    int pitch, ng, n_x, n_y;
-    __device__ __forceinline__ bool interior(int i, int j) const
+    __device__ __forceinline__ double S(long long o, int k, bool from_next) const
     {
-        return i >= ng && i < ng + n_x && j >= ng && j < ng + n_y;
-    }
-    // the reference's U_NEW at (i, j) when the boundary routines read it
-    __device__ __forceinline__ double S(int i, int j, int k) const
-    {
-        long long o = (long long)j * pitch + i;
-        const double *b = (interior(i, j) && updated_cell(type[o])) ? next : prev;
-        return state_ld(b, k, o, g);
-    }
-    __device__ __forceinline__ double N_(int i, int j, int k) const
-    {
-        return state_ld(next, k, (long long)j * pitch + i, g);
+        return state_ld(from_next ? next : prev, k, o, g);
     }
 };
 
 // primitives of S at (i, j), as GFM_Bound.cpp:197-212 computes them
-__device__ __forceinline__ void prim(const View &v, int i, int j, double g, double &rho, double &u, double &w,
-                                     double &p)
+__device__ __forceinline__ void prim(const View &v, int i, int j, bool from_next, double g, double &rho, double &u,
+                                     double &w, double &p)
 {
-    rho = v.S(i, j, 0);
-    u = v.S(i, j, 1) / rho;
-    w = v.S(i, j, 2) / rho;
-    p = (g - 1) * (v.S(i, j, 3) - 0.5 * rho * (u * u + w * w));
+    const long long o = (long long)j * v.g.pitch + i;
+    rho = v.S(o, 0, from_next);
+    u = v.S(o, 1, from_next) / rho;
+    w = v.S(o, 2, from_next) / rho;
+    p = (g - 1) * (v.S(o, 3, from_next) - 0.5 * rho * (u * u + w * w));
 }
 
-// inverse-distance average of the four bracket corners, GFM_Bound.cpp:214-217
-__device__ __forceinline__ void idw_average(const View &v, int idx, int idy, const double *a, double g, double w[4])
+// A ghost record is filled by GHOST_LANES consecutive lanes of one warp
+// (a quad): lane c computes the primitives of bracket corner c and the
+// weighted average of primitive c, and stores conserved component c.  Every
+// value is the expression, in the order, that one thread computing all of
+// them evaluates; the quad shortens the chain of dependent loads and FP64
+// divides that bounds the pass (about one ghost record per wall cell).
+struct Quad
 {
-    double r[4], u[4], vv[4], p[4];
-    prim(v, idx, idy, g, r[0], u[0], vv[0], p[0]);
-    prim(v, idx, idy + 1, g, r[1], u[1], vv[1], p[1]);
-    prim(v, idx + 1, idy + 1, g, r[2], u[2], vv[2], p[2]);
-    prim(v, idx + 1, idy, g, r[3], u[3], vv[3], p[3]);
-    double s = a[0] + a[1] + a[2] + a[3];
-    w[0] = (a[0] * r[0] + a[1] * r[1] + a[2] * r[2] + a[3] * r[3]) / s;
-    w[1] = (a[0] * u[0] + a[1] * u[1] + a[2] * u[2] + a[3] * u[3]) / s;
-    w[2] = (a[0] * vv[0] + a[1] * vv[1] + a[2] * vv[2] + a[3] * vv[3]) / s;
-    w[3] = (a[0] * p[0] + a[1] * p[1] + a[2] * p[2] + a[3] * p[3]) / s;
+    unsigned mask; // the quad's lanes in the warp
+    int c;         // this lane's corner / component, 0..3
+    __device__ __forceinline__ double get(double x, int src) const { return __shfl_sync(mask, x, src, GHOST_LANES); }
+};
+
+__device__ __forceinline__ double pick4(int c, double x0, double x1, double x2, double x3)
+{
+    return c == 0 ? x0 : c == 1 ? x1 : c == 2 ? x2 : x3;
+}
+
+// inverse-distance average of the four bracket corners (idx,idy),
+// (idx,idy+1), (idx+1,idy+1), (idx+1,idy), GFM_Bound.cpp:214-217; every lane
+// of the quad receives all four averages.  nxt: bit c set when corner c is
+// read from the new state.
+__device__ __forceinline__ void idw_average(const View &v, const Quad &q, int idx, int idy, int nxt, const double *a,
+                                            double g, double w[4])
+{
+    double r, u, vv, p;
+    prim(v, idx + (q.c >= 2), idy + (q.c == 1 || q.c == 2), (nxt >> q.c) & 1, g, r, u, vv, p);
+    double x[4]; // primitive q.c of corners 0..3
+#pragma unroll
+    for (int s = 0; s < 4; s++)
+    {
+        const double rs = q.get(r, s), us = q.get(u, s), vs = q.get(vv, s), ps = q.get(p, s);
+        x[s] = pick4(q.c, rs, us, vs, ps);
+    }
+    const double sum = a[0] + a[1] + a[2] + a[3];
+    const double mine = (a[0] * x[0] + a[1] * x[1] + a[2] * x[2] + a[3] * x[3]) / sum;
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+        w[k] = q.get(mine, k);
+}
+
+// conserved component q.c of (rho, u, v, p) stored at o
+__device__ __forceinline__ void store_conserved(double *dst, long long o, const GridDesc &gd, const Quad &q, double g,
+                                                double rho, double u, double v, double p)
+{
+    state_st(dst, q.c, o, pick4(q.c, rho, rho * u, rho * v, p / (g - 1) + 0.5 * rho * (u * u + v * v)), gd);
 }
 
 // reflect the normal velocity and store conserved values, GFM_Bound.cpp:219-228
-__device__ __forceinline__ void store_reflected(double *dst, long long o, const GridDesc &gd, double g, double nx,
-                                                double ny, double rho_w, double u_w, double v_w, double p_w)
+__device__ __forceinline__ void store_reflected(double *dst, long long o, const GridDesc &gd, const Quad &q, double g,
+                                                double nx, double ny, double rho_w, double u_w, double v_w,
+                                                double p_w)
 {
     double u_n = u_w * nx + v_w * ny;
     double u_t = u_w * ny - v_w * nx;
     u_n = -u_n;
     u_w = u_n * nx + u_t * ny;
     v_w = u_n * ny - u_t * nx;
-    state_st(dst, 0, o, rho_w, gd);
-    state_st(dst, 1, o, rho_w * u_w, gd);
-    state_st(dst, 2, o, rho_w * v_w, gd);
-    state_st(dst, 3, o, p_w / (g - 1) + 0.5 * rho_w * (u_w * u_w + v_w * v_w), gd);
+    store_conserved(dst, o, gd, q, g, rho_w, u_w, v_w, p_w);
 }
 
-__device__ void fill_ghost(const FillArgs &a, const View &v, double *dst, const GhostRec &h)
+__device__ void fill_ghost(const FillArgs &a, const View &v, double *dst, const GhostRec &h, const Quad &q)
 {
     const double g = a.g.gamma;
     const long long o = (long long)h.j * a.g.pitch + h.i;
     if (a.bc == BC_IDW)
     {
         double w[4];
-        idw_average(v, h.idx, h.idy, h.w, g, w);
-        store_reflected(dst, o, a.g, g, h.nx, h.ny, w[0], w[1], w[2], w[3]);
+        idw_average(v, q, h.idx, h.idy, h.snext, h.w, g, w);
+        store_reflected(dst, o, a.g, q, g, h.nx, h.ny, w[0], w[1], w[2], w[3]);
     }
     else if (a.bc == BC_LINEAR || a.bc == BC_RIEMANNGFM)
     {
-        // LinearBaseGFM/GFM_Bound.cpp:83-575: one corner's primitives (zeros if none is fluid)
+        // LinearBaseGFM/GFM_Bound.cpp:83-575: one corner's primitives (zeros
+        // if none is fluid); pick p is bracket corner p - 1
         double rho = 0, u = 0, w = 0, p = 0;
         if (h.pick > 0)
         {
             const int ci = (h.pick == 1 || h.pick == 2) ? h.idx : h.idx + 1;
             const int cj = (h.pick == 1 || h.pick == 4) ? h.idy : h.idy + 1;
-            prim(v, ci, cj, g, rho, u, w, p);
+            prim(v, ci, cj, (h.snext >> (h.pick - 1)) & 1, g, rho, u, w, p);
         }
-        store_reflected(dst, o, a.g, g, h.nx, h.ny, rho, u, w, p);
+        store_reflected(dst, o, a.g, q, g, h.nx, h.ny, rho, u, w, p);
     }
     else
     {
         // BCGFM/BCGFM_Bound.cpp:89-175 and HBCGFM_Bound.cpp (pure mirror when |phi| > delta)
         double wi[4], we[4];
-        idw_average(v, h.idx, h.idy, h.w, g, wi);
-        idw_average(v, h.idx2, h.idy2, h.w2, g, we);
+        idw_average(v, q, h.idx, h.idy, h.snext, h.w, g, wi);
+        idw_average(v, q, h.idx2, h.idy2, h.snext >> 4, h.w2, g, we);
         const double nx = h.nx, ny = h.ny, delta = h.delta, R_E = h.delta, R_G = h.rg;
         double u_n_i = wi[1] * nx + wi[2] * ny;
         double u_t_i = wi[1] * ny - wi[2] * nx;
@@ -133,18 +158,33 @@ __device__ void fill_ghost(const FillArgs &a, const View &v, double *dst, const 
         }
         double u_m = u_n_m * nx + u_t_m * ny;
         double v_m = u_n_m * ny - u_t_m * nx;
-        state_st(dst, 0, o, rho_m, a.g);
-        state_st(dst, 1, o, rho_m * u_m, a.g);
-        state_st(dst, 2, o, rho_m * v_m, a.g);
-        state_st(dst, 3, o, p_m / (g - 1) + 0.5 * rho_m * (u_m * u_m + v_m * v_m), a.g);
+        store_conserved(dst, o, a.g, q, g, rho_m, u_m, v_m, p_m);
     }
 }
 
-// Global_Boundary, transmissive x / reflective y (Test/Sod/Global_Boudary.cpp:23-75),
-// or the periodic harness plug-in; `ring` enumerates row ghosts then column ghosts.
-__device__ void fill_ring(const FillArgs &a, const View &v, double *dst, long long q)
+// What one domain-edge cell copies: Global_Boundary, transmissive x /
+// reflective y (Test/Sod/Global_Boudary.cpp:23-75), or the periodic harness
+// plug-in; the cells enumerate row ghosts then column ghosts.
+struct RingPlan
 {
-    const int ng = a.g.ng, n_x = a.g.n_x, n_y = a.g.n_y, N = a.g.N, pitch = a.g.pitch;
+    long long o;      // the edge cell
+    long long s0, s1; // sources: s0 every component (a wall row: all but v), s1 a wall row's mirrored v
+    bool n0, n1;      // the source is read from the new state
+    int kind;         // RING_COPY, RING_WALL_ROW, RING_INITIAL
+    int ic;           // RING_INITIAL: the row of the initial ring values
+    bool raw;         // periodic FP32 form: the (hi, lo) pair copied as it is
+};
+enum { RING_COPY = 0, RING_WALL_ROW = 1, RING_INITIAL = 2 };
+
+__device__ __forceinline__ RingPlan ring_plan(const FillArgs &a, long long q)
+{
+    const GridDesc &g = a.g;
+    const int ng = g.ng, n_x = g.n_x, n_y = g.n_y, N = g.N, pitch = g.pitch;
+    auto interior = [&](int i, int j) { return i >= ng && i < ng + n_x && j >= ng && j < ng + n_y; };
+    // S of (i, j) from the new state: an updated interior cell
+    auto from_next = [&](int i, int j) {
+        return interior(i, j) && updated_cell(a.type[(long long)j * pitch + i]);
+    };
     const long long nrow = 2LL * ng * n_x;
     int i, j;
     bool row;
@@ -163,8 +203,9 @@ __device__ void fill_ring(const FillArgs &a, const View &v, double *dst, long lo
         j = (int)(qq - (long long)c * N);
         i = (c < ng) ? c : n_x + c;
     }
-    const long long o = (long long)j * pitch + i;
-    double out[4];
+    RingPlan p{};
+    p.o = (long long)j * pitch + i;
+    p.kind = RING_COPY;
     if (a.gb == GB_PERIODIC)
     {
         // rows from the opposite interior rows of S; columns from the opposite
@@ -177,34 +218,22 @@ __device__ void fill_ring(const FillArgs &a, const View &v, double *dst, long lo
         else if (j >= n_y + ng)
             sj = j - n_y;
         const bool src_interior_row = (sj >= ng && sj < ng + n_y);
-        const long long so = (long long)sj * pitch + si;
-        const double *src;
-        if (row || !src_interior_row || (sj != j))
-            src = (v.interior(si, sj) && updated_cell(v.type[so])) ? v.next : v.prev; // S(.) of an interior cell
-        else
-            src = v.next; // interior row, after the fill
-        if (a.g.f32)
-        {
-            // the FP32 form's (hi, lo) pair copied as it is: a round trip
-            // through FP64 re-splits a pair whose lo is exactly half an ulp
-            const float *sf = reinterpret_cast<const float *>(src);
-            float *df = reinterpret_cast<float *>(dst);
-            for (int k = 0; k < 8; k++)
-                df[k * a.g.plane + o] = sf[k * a.g.plane + so];
-            return;
-        }
-        for (int k = 0; k < 4; k++)
-            out[k] = state_ld(src, k, so, a.g);
+        p.s0 = (long long)sj * pitch + si;
+        // an interior row's column ghosts copy the new state after the fill
+        p.n0 = (row || !src_interior_row || (sj != j)) ? from_next(si, sj) : true;
+        // a round trip through FP64 re-splits a pair whose lo is exactly half an ulp
+        p.raw = g.f32;
     }
     else if (row)
     {
         const bool bottom = j < ng;
         const int src = bottom ? 2 * ng - 1 : n_y + ng - 1;
         const int mir = bottom ? 2 * ng - j - 1 : 2 * (n_y + ng) - 1 - j;
-        out[0] = v.S(i, src, 0);
-        out[1] = v.S(i, src, 1);
-        out[2] = -v.S(i, mir, 2);
-        out[3] = v.S(i, src, 3);
+        p.kind = RING_WALL_ROW;
+        p.s0 = (long long)src * pitch + i;
+        p.s1 = (long long)mir * pitch + i;
+        p.n0 = from_next(i, src);
+        p.n1 = from_next(i, mir);
     }
     else
     {
@@ -214,58 +243,94 @@ __device__ void fill_ring(const FillArgs &a, const View &v, double *dst, long lo
         {
             const int side = (i < ng) ? 0 : 1;
             const int rr = (j < ng) ? j : j - n_y; // [0, 2ng)
-            for (int k = 0; k < 4; k++)
-                out[k] = a.ring_ic[(side * 2 * ng + rr) * 4 + k];
+            p.kind = RING_INITIAL;
+            p.ic = side * 2 * ng + rr;
         }
         else
         {
-            for (int k = 0; k < 4; k++)
-                out[k] = v.S(si, j, k);
+            p.s0 = (long long)j * pitch + si;
+            p.n0 = from_next(si, j);
         }
     }
+    return p;
+}
+
+__device__ __forceinline__ void ring_apply(const FillArgs &a, const View &v, double *dst, const RingPlan &p)
+{
+    if (p.raw)
+    {
+        const float *sf = reinterpret_cast<const float *>(p.n0 ? v.next : v.prev);
+        float *df = reinterpret_cast<float *>(dst);
+        for (int k = 0; k < 8; k++)
+            df[k * a.g.plane + p.o] = sf[k * a.g.plane + p.s0];
+        return;
+    }
+    double out[4];
+    if (p.kind == RING_INITIAL)
+    {
+        for (int k = 0; k < 4; k++)
+            out[k] = a.ring_ic[p.ic * 4 + k];
+    }
+    else
+    {
+        for (int k = 0; k < 4; k++)
+            out[k] = v.S(p.s0, k, p.n0);
+        if (p.kind == RING_WALL_ROW)
+            out[2] = -v.S(p.s1, 2, p.n1);
+    }
     for (int k = 0; k < 4; k++)
-        state_st(dst, k, o, out[k], a.g);
+        state_st(dst, k, p.o, out[k], a.g);
+}
+
+// the state buffer the pass writes; run: the pass has work (a step completed,
+// the initial fill, or a step in flight)
+__device__ __forceinline__ int fill_cur(const FillArgs &a, bool &run)
+{
+    const DevState *st = a.st;
+    if (a.pre_flip)
+    {
+        run = true;
+        return st->step_cur ^ 1; // the buffer the step in flight writes
+    }
+    run = a.init_mode || st->fill_pending;
+    return st->cur;
 }
 
 // one FILL_THREADS block of a case's boundary pass: blocks [0, gblocks) fill
-// the ghost list, the rest the domain edges
+// the ghost list, the rest the domain edges.  What a cell reads is settled
+// (record, types) before the device state names the buffers.
 __device__ __forceinline__ void fill_block(const FillArgs &a, int vb, int do_ghosts, int do_ring)
 {
-    DevState *st = a.st;
-    int cur;
-    if (a.pre_flip)
-        cur = st->step_cur ^ 1; // the buffer the step in flight writes
-    else
-    {
-        if (!a.init_mode && !st->fill_pending)
-            return;
-        cur = st->cur;
-    }
-    View v;
-    v.next = cur ? a.buf1 : a.buf0;
-    v.prev = cur ? a.buf0 : a.buf1;
-    v.type = a.type;
-    v.g = a.g;
-    v.P = a.g.plane;
-    v.pitch = a.g.pitch;
-    v.ng = a.g.ng;
-    v.n_x = a.g.n_x;
-    v.n_y = a.g.n_y;
-    double *dst = cur ? a.buf1 : a.buf0;
-    const int gblocks = do_ghosts ? (a.nghost - a.ghost0 + FILL_THREADS - 1) / FILL_THREADS : 0;
+    const int gblocks = do_ghosts ? ghost_blocks(a.nghost - a.ghost0) : 0;
+    bool run;
     if (vb < gblocks)
     {
-        int t = a.ghost0 + vb * FILL_THREADS + threadIdx.x;
-        if (t < a.nghost)
-            fill_ghost(a, v, dst, a.ghosts[t]);
+        static_assert(FILL_THREADS % GHOST_LANES == 0 && 32 % GHOST_LANES == 0, "a quad sits in one warp");
+        const int t = a.ghost0 + (vb * FILL_THREADS + (int)threadIdx.x) / GHOST_LANES;
+        if (t >= a.nghost) // the quad's lanes share t: all four fill or none
+            return;
+        const GhostRec h = a.ghosts[t];
+        const int cur = fill_cur(a, run);
+        if (!run)
+            return;
+        const int lane = (int)(threadIdx.x & 31);
+        const Quad q{((1u << GHOST_LANES) - 1) << (lane & ~(GHOST_LANES - 1)), lane & (GHOST_LANES - 1)};
+        const View v{cur ? a.buf1 : a.buf0, cur ? a.buf0 : a.buf1, a.g};
+        fill_ghost(a, v, cur ? a.buf1 : a.buf0, h, q);
         return;
     }
     if (!do_ring)
         return;
-    long long q = (long long)(vb - gblocks) * FILL_THREADS + threadIdx.x;
-    long long nring = 2LL * a.g.ng * a.g.n_x + 2LL * a.g.ng * a.g.N;
-    if (q < nring)
-        fill_ring(a, v, dst, q);
+    const long long q = (long long)(vb - gblocks) * FILL_THREADS + threadIdx.x;
+    const long long nring = 2LL * a.g.ng * a.g.n_x + 2LL * a.g.ng * a.g.N;
+    if (q >= nring)
+        return;
+    const RingPlan p = ring_plan(a, q);
+    const int cur = fill_cur(a, run);
+    if (!run)
+        return;
+    const View v{cur ? a.buf1 : a.buf0, cur ? a.buf0 : a.buf1, a.g};
+    ring_apply(a, v, cur ? a.buf1 : a.buf0, p);
 }
 
 __global__ void __launch_bounds__(FILL_THREADS) fill_kernel(const FillArgs a)
@@ -283,13 +348,13 @@ void launch_fill_ghosts(const FillArgs &a, int g0, int g1, cudaStream_t s)
     b.nghost = g1; // records [ghost0, nghost)
     b.do_ghosts = 1;
     b.do_ring = 0;
-    fill_kernel<<<(g1 - g0 + FILL_THREADS - 1) / FILL_THREADS, FILL_THREADS, 0, s>>>(b);
+    fill_kernel<<<ghost_blocks(g1 - g0), FILL_THREADS, 0, s>>>(b);
     count_launch();
 }
 
 void launch_fill(const FillArgs &a, cudaStream_t s)
 {
-    int gblocks = a.do_ghosts ? (a.nghost + FILL_THREADS - 1) / FILL_THREADS : 0;
+    int gblocks = a.do_ghosts ? ghost_blocks(a.nghost) : 0;
     long long nring = 2LL * a.g.ng * a.g.n_x + 2LL * a.g.ng * a.g.N;
     int rblocks = a.do_ring ? (int)((nring + FILL_THREADS - 1) / FILL_THREADS) : 0;
     if (gblocks + rblocks == 0)

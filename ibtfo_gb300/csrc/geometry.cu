@@ -181,6 +181,22 @@ __device__ int linear_pick(int t1, int t2, int t3, int t4, bool xbig, bool ybig)
     return 0;
 }
 
+// corners c = 0..3 of a bracket, (idx,idy), (idx,idy+1), (idx+1,idy+1),
+// (idx+1,idy), whose value the boundary pass takes from the new state: the
+// updated interior cells (a static property of the geometry)
+__device__ int next_corners(const GridDesc &g, const uint8_t *type, int idx, int idy)
+{
+    int m = 0;
+    for (int c = 0; c < 4; c++)
+    {
+        const int i = idx + (c >= 2), j = idy + (c == 1 || c == 2);
+        const bool in = i >= g.ng && i < g.ng + g.n_x && j >= g.ng && j < g.ng + g.n_y;
+        if (in && updated_cell(type[(long long)j * g.pitch + i]))
+            m |= 1 << c;
+    }
+    return m;
+}
+
 __global__ void scheme_index_kernel(GridDesc g, int bc, const double *__restrict__ phi, const double *__restrict__ nxa,
                                     const double *__restrict__ nya, const uint8_t *__restrict__ type, GhostRec *gl,
                                     int n)
@@ -241,7 +257,9 @@ __global__ void scheme_index_kernel(GridDesc g, int bc, const double *__restrict
         r.idy2 = bracket_y(g, r.ym2, 0);
         idw_weights(g, type, r.idx, r.idy, r.xm, r.ym, true, r.w);
         idw_weights(g, type, r.idx2, r.idy2, r.xm2, r.ym2, true, r.w2);
+        r.snext = next_corners(g, type, r.idx2, r.idy2) << 4;
     }
+    r.snext |= next_corners(g, type, r.idx, r.idy);
     gl[t] = r;
 }
 

@@ -51,6 +51,8 @@ struct GhostRec
     int idx2, idy2; // bracket of the extra point (BCGFM/HBCGFM)
     int pick;       // LinearBaseGFM: chosen corner 1..4, 0 if none is fluid
     int hmirror;    // HBCGFM: |phi| > delta (pure mirror)
+    int snext;      // bit c (c + 4): corner c of the image (extra) bracket is an
+                    // updated interior cell, read from the new state
     double xm, ym;  // image point
     double xm2, ym2; // extra point
     double w[4];    // inverse-distance weights, corners (idx,idy),(idx,idy+1),(idx+1,idy+1),(idx+1,idy)
@@ -299,6 +301,9 @@ constexpr int BATCH_THREADS = 256;
 // records are few (about one per wall cell), so small blocks spread them
 // over every SM
 constexpr int FILL_THREADS = 64;
+// lanes that fill one ghost record together (one bracket corner each)
+constexpr int GHOST_LANES = 4;
+constexpr int ghost_blocks(long long n) { return (int)((n * GHOST_LANES + FILL_THREADS - 1) / FILL_THREADS); }
 
 struct BatchKernel
 {

@@ -116,13 +116,15 @@ def alone(req, precision="fp32c"):
 
 
 def stream(n, seed=7):
+    # arrivals in groups of three, 4 ms apart: a group's requests are active
+    # together however fast each one runs
     rng = np.random.default_rng(seed)
     out = []
     for k in range(n):
         nx = int(rng.choice([64, 96, 128, 160]))
         ny = int(nx // rng.choice([1, 2]))
         out.append((k, nx, ny, float(rng.uniform(1.5, 4.0)), float(rng.uniform(0.05, 0.2)),
-                    float(rng.uniform(0.35, 0.7)), float(rng.uniform(0.3, 0.7)), 0.004 * k))
+                    float(rng.uniform(0.35, 0.7)), float(rng.uniform(0.3, 0.7)), 0.004 * (k // 3)))
     return out
 
 
