@@ -570,6 +570,21 @@ __global__ void cur_rows_to_aos_kernel(const double *b0, const double *b1, const
         aos[c * 4 + k] = state_ld(soa, k, o, g);
 }
 
+// one cell of a host-layout array: two 16-byte stores where the array allows
+// (page-locked host memory written over the host link moves in whole sectors)
+__device__ __forceinline__ void store_aos_cell(double *aos, long long c, const double v[4])
+{
+    double *p = aos + c * 4;
+    if ((reinterpret_cast<uintptr_t>(aos) & 15) == 0)
+    {
+        reinterpret_cast<double2 *>(p)[0] = make_double2(v[0], v[1]);
+        reinterpret_cast<double2 *>(p)[1] = make_double2(v[2], v[3]);
+    }
+    else
+        for (int k = 0; k < 4; k++)
+            p[k] = v[k];
+}
+
 __global__ void snapshot_rows_to_aos_kernel(const double *b0, const double *b1, const DevState *__restrict__ st,
                                             const uint8_t *__restrict__ type, double *__restrict__ aos, GridDesc g,
                                             int r0, int r1, int c0, int c1)
@@ -585,8 +600,10 @@ __global__ void snapshot_rows_to_aos_kernel(const double *b0, const double *b1, 
     const bool out = type[o] == CELL_FLUID ||
                      (type[o] == CELL_GHOST && i >= g.ng && i < g.ng + g.n_x && j >= g.ng && j < g.ng + g.n_y);
     const double *src = out ? (cur ? b0 : b1) : (cur ? b1 : b0);
+    double v[4];
     for (int k = 0; k < 4; k++)
-        aos[c * 4 + k] = state_ld(src, k, o, g);
+        v[k] = state_ld(src, k, o, g);
+    store_aos_cell(aos, c, v);
 }
 
 void launch_snapshot_to_aos_rows(const double *b0, const double *b1, const DevState *st, const uint8_t *type,
@@ -625,8 +642,10 @@ __global__ void ring_to_aos_kernel(const double *b0, const double *b1, const Dev
     }
     const double *src = st->cur ? b1 : b0;
     const long long o = (long long)j * g.pitch + i, c = (long long)j * g.M + i;
+    double v[4];
     for (int k = 0; k < 4; k++)
-        aos[c * 4 + k] = state_ld(src, k, o, g);
+        v[k] = state_ld(src, k, o, g);
+    store_aos_cell(aos, c, v);
 }
 
 void launch_ring_to_aos(const double *b0, const double *b1, const DevState *st, double *aos, const GridDesc &g,

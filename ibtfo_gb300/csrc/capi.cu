@@ -109,7 +109,8 @@ static void set_derived_constants(GridDesc &g)
 }
 
 static constexpr int NBANDS = 8; // row bands of ibtfo_step_host
-static constexpr int NSW = 2;    // streams the bands' sweeps alternate on
+static constexpr int NSW = 4;    // streams the bands' sweeps alternate on
+static constexpr int NFIN = 4;   // streams the bands' finishing work alternates on
 
 struct ibtfo_case
 {
@@ -129,15 +130,11 @@ struct ibtfo_case
     double *ring_ic = nullptr; // [2][2*ng][4]
     int tma = 0;                // tensor maps of buf[0], buf[1] below are valid
     CUtensorMap tmap[2];        // boxes of TILE_X x tile_y cells and their halo
-    CUtensorMap tmap8[2];       // boxes of TILE_X x TILE_Y cells (the host step's bands)
     unsigned *tiles = nullptr;  // active sweep tiles (TILE_X x tile_y)
     int ntiles = 0;
-    // the host step's bands sweep TILE_X x TILE_Y tiles (shorter CTAs fill and
-    // drain the band pipeline faster): their list when tile_y differs, and
-    // the launcher for them
-    unsigned *tiles8 = nullptr;
-    int ntiles8 = 0;
-    SweepLaunch sweep8 = nullptr;
+    // the same tiles in row order: the row bands of the host-array step
+    unsigned *band_list = nullptr;
+    int nband_list = 0;
     // cut cells (BC_CCM): volume fractions, apertures, small-cell mixing lists
     double *alpha = nullptr, *ax = nullptr, *ay = nullptr;
     MixExchange *mix_ex = nullptr;
@@ -165,9 +162,13 @@ struct ibtfo_case
     const double *mirror_in = nullptr;
     std::vector<int> band_ghosts; // NBANDS + 1 offsets into the ghost list (rows of each band)
     std::vector<int> ghost_ready; // NBANDS: the last band whose fluid cells the band's ghost fills read
-    cudaStream_t h2d = nullptr, d2h = nullptr, sw[NSW] = {}, fin = nullptr;
+    // copies (h2d, d2h), band sweeps (sw), and at the highest priority the
+    // short kernels the bands wait on: conversions in (conv) and each band's
+    // ghost fill and conversion out (fin), whose blocks then take the next
+    // free SM slot ahead of the sweeps' pending tiles
+    cudaStream_t h2d = nullptr, d2h = nullptr, sw[NSW] = {}, fin[NFIN] = {}, conv = nullptr;
     cudaEvent_t ev_in[NBANDS] = {}, ev_conv[NBANDS] = {}, ev_out[NBANDS] = {}, ev_swept[NBANDS] = {},
-                ev_sw[NSW] = {}, ev_fin = nullptr, ev_done = nullptr;
+                ev_sw[NSW] = {}, ev_fin[NFIN] = {}, ev_done = nullptr, ev_cv = nullptr;
     // the banded step captured as a CUDA graph for one pair of page-locked host arrays
     cudaGraphExec_t host_graph = nullptr;
     const double *host_graph_in = nullptr;
@@ -176,12 +177,14 @@ struct ibtfo_case
 };
 
 // the streams of ibtfo_step_host besides the case's own
-static std::array<cudaStream_t, 3 + NSW> helper_streams(const ibtfo_case *c)
+static std::array<cudaStream_t, 3 + NSW + NFIN> helper_streams(const ibtfo_case *c)
 {
-    std::array<cudaStream_t, 3 + NSW> a;
-    a[0] = c->h2d, a[1] = c->d2h, a[2] = c->fin;
+    std::array<cudaStream_t, 3 + NSW + NFIN> a;
+    a[0] = c->h2d, a[1] = c->d2h, a[2] = c->conv;
     for (int q = 0; q < NSW; q++)
         a[3 + q] = c->sw[q];
+    for (int q = 0; q < NFIN; q++)
+        a[3 + NSW + q] = c->fin[q];
     return a;
 }
 
@@ -210,7 +213,7 @@ static void drop_graphs(ibtfo_case *c)
 static void make_bands(ibtfo_case *c, const std::vector<unsigned> &tiles)
 {
     const GridDesc &g = c->g;
-    const int nty = (g.n_y + TILE_Y - 1) / TILE_Y;
+    const int nty = (g.n_y + c->tile_y - 1) / c->tile_y;
     c->band_rows.assign(NBANDS + 1, 0);
     c->out_rows.assign(NBANDS + 1, 0);
     c->band_tiles.assign(NBANDS + 1, 0);
@@ -221,8 +224,8 @@ static void make_bands(ibtfo_case *c, const std::vector<unsigned> &tiles)
         // the first and the last band half as tall as the others: the
         // pipeline waits for the first chunk alone and drains the last one alone
         const int tb = (k == NBANDS) ? nty : (int)((long long)(2 * k - 1) * nty / (2 * NBANDS - 2));
-        c->band_rows[k] = (k == NBANDS) ? g.N : std::min(g.N, g.ng + tb * TILE_Y + 2);
-        c->out_rows[k] = (k == NBANDS) ? g.N : std::min(g.N, g.ng + tb * TILE_Y);
+        c->band_rows[k] = (k == NBANDS) ? g.N : std::min(g.N, g.ng + tb * c->tile_y + 2);
+        c->out_rows[k] = (k == NBANDS) ? g.N : std::min(g.N, g.ng + tb * c->tile_y);
         while (t < tiles.size() && tile_jy(tiles[t]) < tb)
             t++;
         c->band_tiles[k] = (k == NBANDS) ? (int)tiles.size() : (int)t;
@@ -309,8 +312,8 @@ static void make_in_boxes(ibtfo_case *c, const std::vector<unsigned> &tiles)
     const int halo = std::max(2, g.ng);
     for (unsigned t : tiles)
     {
-        const int i0 = g.ng + tile_ix(t) * TILE_X, j0 = g.ng + tile_jy(t) * TILE_Y;
-        add(j0 - halo, j0 + TILE_Y + halo, i0 - halo, i0 + TILE_X + halo);
+        const int i0 = g.ng + tile_ix(t) * TILE_X, j0 = g.ng + tile_jy(t) * c->tile_y;
+        add(j0 - halo, j0 + c->tile_y + halo, i0 - halo, i0 + TILE_X + halo);
     }
     for (int k = 0; k < NBANDS; k++)
         add(std::max(c->out_rows[k], g.ng), std::min(c->out_rows[k + 1], g.ng + g.n_y), c->fluid_cols[2 * k],
@@ -357,21 +360,51 @@ static void make_in_boxes(ibtfo_case *c, const std::vector<unsigned> &tiles)
 
 // the domain ring of the current state into u_out: two runs of whole rows
 // and two strided runs of the side columns
-static ibtfo_status ring_to_host(ibtfo_case *c, double *u_out)
+// The device-side address of a page-locked host array the kernels can write
+// directly, or null (pageable memory, or no mapping).
+static double *device_view(double *host)
+{
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, host) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? static_cast<double *>(at.devicePointer) : nullptr;
+}
+
+// the domain ring to the host layout on stream ks, and its copies on cs; with
+// zc (u_out's device view) the kernel writes the host array itself, after the
+// row copies queued on the second copy stream when those cover the ring
+// (full rows back: their ring cells are stale)
+static ibtfo_status ring_to_host(ibtfo_case *c, double *u_out, cudaStream_t ks, cudaStream_t cs, double *zc,
+                                 bool after_rows)
 {
     const GridDesc &g = c->g;
     const size_t row = sizeof(double) * 4 * (size_t)g.M, cell = sizeof(double) * 4;
-    launch_ring_to_aos(c->buf[0], c->buf[1], c->st, c->staging, g, c->stream);
-    CK(cudaEventRecord(c->ev_done, c->stream));
-    CK(cudaStreamWaitEvent(c->d2h, c->ev_done, 0));
+    if (zc)
+    {
+        if (after_rows)
+        {
+            CK(cudaEventRecord(c->ev_done, c->d2h));
+            CK(cudaStreamWaitEvent(ks, c->ev_done, 0));
+        }
+        launch_ring_to_aos(c->buf[0], c->buf[1], c->st, zc, g, ks);
+        return IBTFO_OK;
+    }
+    launch_ring_to_aos(c->buf[0], c->buf[1], c->st, c->staging, g, ks);
+    if (cs != ks)
+    {
+        CK(cudaEventRecord(c->ev_done, ks));
+        CK(cudaStreamWaitEvent(cs, c->ev_done, 0));
+    }
     const size_t top = (size_t)(g.ng + g.n_y) * g.M * 4, side = (size_t)g.ng * g.M * 4;
-    CK(cudaMemcpyAsync(u_out, c->staging, row * g.ng, cudaMemcpyDeviceToHost, c->d2h));
-    CK(cudaMemcpyAsync(u_out + top, c->staging + top, row * g.ng, cudaMemcpyDeviceToHost, c->d2h));
-    CK(cudaMemcpy2DAsync(u_out + side, row, c->staging + side, row, cell * g.ng, g.n_y, cudaMemcpyDeviceToHost,
-                         c->d2h));
+    CK(cudaMemcpyAsync(u_out, c->staging, row * g.ng, cudaMemcpyDeviceToHost, cs));
+    CK(cudaMemcpyAsync(u_out + top, c->staging + top, row * g.ng, cudaMemcpyDeviceToHost, cs));
+    CK(cudaMemcpy2DAsync(u_out + side, row, c->staging + side, row, cell * g.ng, g.n_y, cudaMemcpyDeviceToHost, cs));
     const size_t right = side + (size_t)(g.ng + g.n_x) * 4;
     CK(cudaMemcpy2DAsync(u_out + right, row, c->staging + right, row, cell * g.ng, g.n_y, cudaMemcpyDeviceToHost,
-                         c->d2h));
+                         cs));
     return IBTFO_OK;
 }
 
@@ -408,16 +441,12 @@ static int make_state_tmaps(ibtfo_case *c)
     const cuuint64_t dims[3] = {(cuuint64_t)g.M, (cuuint64_t)g.N, (cuuint64_t)(f32 ? 8 : 4)};
     const cuuint64_t strides[2] = {(cuuint64_t)g.pitch * elem, (cuuint64_t)g.plane * elem};
     const cuuint32_t estr[3] = {1, 1, 1};
-    for (int h = 0; h < 2; h++)
-    {
-        const cuuint32_t box[3] = {TILE_X + 4, (cuuint32_t)(h ? TILE_Y : c->tile_y) + 4, 4};
-        CUtensorMap *maps = h ? c->tmap8 : c->tmap;
-        for (int b = 0; b < 2; b++)
-            if (encode(&maps[b], f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3,
-                       c->buf[b], dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                       CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-                return 0;
-    }
+    const cuuint32_t box[3] = {TILE_X + 4, (cuuint32_t)c->tile_y + 4, 4};
+    for (int b = 0; b < 2; b++)
+        if (encode(&c->tmap[b], f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, c->buf[b],
+                   dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return 0;
     return 1;
 }
 
@@ -496,14 +525,17 @@ ibtfo_status ibtfo_destroy(ibtfo_case *c)
     for (cudaEvent_t e : c->ev_sw)
         if (e)
             cudaEventDestroy(e);
-    for (cudaEvent_t e : {c->ev_fin, c->ev_done})
+    for (cudaEvent_t e : c->ev_fin)
+        if (e)
+            cudaEventDestroy(e);
+    for (cudaEvent_t e : {c->ev_done, c->ev_cv})
         if (e)
             cudaEventDestroy(e);
     // stream-ordered frees: the memory returns to the device pool without a
     // device-wide synchronisation (other cases keep running)
     cudaStream_t fs = c->own ? c->own : c->stream;
     void *bufs[] = {c->buf[0], c->buf[1], c->ic, c->staging, c->phi, c->nx, c->ny, c->type, c->ghosts,
-                    c->st, c->partial, c->ring_ic, c->tiles, c->tiles8, c->alpha, c->ax, c->ay, c->mix_ex, c->mix_part,
+                    c->st, c->partial, c->ring_ic, c->tiles, c->band_list, c->alpha, c->ax, c->ay, c->mix_ex, c->mix_part,
                     c->mix_links, c->mix_e};
     for (void *p : bufs)
         if (p)
@@ -576,7 +608,6 @@ ibtfo_status ibtfo_create(const ibtfo_config *cfg, ibtfo_case **out)
                     ? FAST_TILE_Y
                     : TILE_Y;
     c->sweep = sweep_launcher(k.scheme, k.riemann, k.limiter, k.precision, c->tile_y);
-    c->sweep8 = c->tile_y == TILE_Y ? c->sweep : sweep_launcher(k.scheme, k.riemann, k.limiter, k.precision, TILE_Y);
     if (k.boundary == IBTFO_BOUNDARY_CCM)
         c->ccm = ccm_launcher(k.scheme, k.riemann, k.limiter, k.precision);
 
@@ -677,18 +708,9 @@ static ibtfo_status geometry_from_phi(ibtfo_case *c)
         rc = setup_geometry(g, c->cfg.boundary, c->phi, c->nx, c->ny, c->type, &c->ghosts, &c->nghost, c->stream);
     std::vector<unsigned> tile_list;
     if (rc == 0)
-        rc = active_tiles(g, c->type, TILE_Y, &c->tiles8, &c->ntiles8, c->stream, &tile_list);
-    if (rc == 0 && c->tile_y != TILE_Y)
+        rc = active_tiles(g, c->type, c->tile_y, &c->band_list, &c->nband_list, c->stream, &tile_list, true);
+    if (rc == 0)
         rc = active_tiles(g, c->type, c->tile_y, &c->tiles, &c->ntiles, c->stream);
-    else if (rc == 0)
-    {
-        std::swap(c->tiles, c->tiles8); // one list: the sweep's, tiles8 left empty
-        if (c->tiles8)
-            cudaFreeAsync(c->tiles8, c->stream);
-        c->tiles8 = nullptr;
-        c->ntiles = c->ntiles8;
-        c->ntiles8 = 0;
-    }
     if (rc == 0)
     {
         make_bands(c, tile_list);
@@ -1515,9 +1537,16 @@ static cudaError_t ensure_pipeline(ibtfo_case *c)
     cudaError_t e = cudaSuccess;
     if (!c->ev_done)
     {
-        for (cudaStream_t *s : {&c->h2d, &c->d2h, &c->fin})
+        int least = 0, greatest = 0;
+        e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        for (cudaStream_t *s : {&c->h2d, &c->d2h})
             if (e == cudaSuccess)
                 e = cudaStreamCreateWithFlags(s, cudaStreamNonBlocking);
+        if (e == cudaSuccess)
+            e = cudaStreamCreateWithPriority(&c->conv, cudaStreamNonBlocking, greatest);
+        for (cudaStream_t &s : c->fin)
+            if (e == cudaSuccess)
+                e = cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, greatest);
         for (cudaStream_t &s : c->sw)
             if (e == cudaSuccess)
                 e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
@@ -1528,7 +1557,10 @@ static cudaError_t ensure_pipeline(ibtfo_case *c)
         for (cudaEvent_t &v : c->ev_sw)
             if (e == cudaSuccess)
                 e = cudaEventCreateWithFlags(&v, cudaEventDisableTiming);
-        for (cudaEvent_t *v : {&c->ev_fin, &c->ev_done})
+        for (cudaEvent_t &v : c->ev_fin)
+            if (e == cudaSuccess)
+                e = cudaEventCreateWithFlags(&v, cudaEventDisableTiming);
+        for (cudaEvent_t *v : {&c->ev_cv, &c->ev_done})
             if (e == cudaSuccess)
                 e = cudaEventCreateWithFlags(v, cudaEventDisableTiming);
     }
@@ -1587,17 +1619,26 @@ static ibtfo_status step_host_plain(ibtfo_case *c, const double *u_in, double *u
 }
 
 // The banded pipeline.  Row chunk k goes host -> device on one copy stream;
-// the case's stream converts it into the current state buffer; band k of the
+// a conversion stream converts it into the current state buffer; band k of the
 // sweep (the tiles of its tile rows, which read array rows up to the end of
-// chunk k) runs on one of two sweep streams, so that consecutive bands
-// overlap on the SMs.  A finishing stream then fills the ghost cells of band
-// k's rows (once every band their image points read has been swept),
-// converts the band's rows back (fluid and ghost cells from the step's
-// output, other cells from its input) and hands them to the second copy
-// stream, while later bands compute.  After the last band the domain edges
-// are filled and go back by two row copies and two strided column copies.
-// Every copy of u_in lands before any write to u_out, so u_out may be u_in.
-// In place (u_out == u_in) the host array already holds every cell the step
+// chunk k) runs on one of NSW sweep streams, so that consecutive bands
+// overlap on the SMs.  One of NFIN finishing streams then fills the ghost
+// cells of band k's rows (once every band their image points read has been
+// swept), converts the band's rows back (fluid and ghost cells from the
+// step's output, other cells from its input) and hands them to the second
+// copy stream, while later bands compute (the copy engines move them at the
+// link's rate without holding SMs the sweeps need; kernels writing the host
+// array across the link would hold their SM slots for as long).  The domain
+// edges are filled and go back by two row copies and two strided column
+// copies, or to a page-locked u_out by the conversion kernel itself (a few
+// hundred KB; the strided copies move 2-cell pieces row by row): in place between
+// walls (they read swept cells and the step's input only) as soon as every
+// band is swept, beside the bands' finishing work; otherwise after it
+// (periodic edges copy interior cells, ghost cells included, and full-row
+// copies back cover the edges).
+// The chunks partition the rows and band k writes back only rows below the
+// start of chunk k + 1, which it has read; the ring goes back after every
+// chunk has landed: so u_out may be u_in.  In place (u_out == u_in) the host array already holds every cell the step
 // leaves alone (solid cells are never written), so each band copies back
 // only its interior rows over the columns of its fluid and ghost cells, and
 // (boxes) copies in only the cells some part of the step reads.
@@ -1606,6 +1647,7 @@ static ibtfo_status step_host_banded(ibtfo_case *c, const double *u_in, double *
     const GridDesc &g = c->g;
     const size_t row = sizeof(double) * 4 * (size_t)g.M, cell = sizeof(double) * 4;
     const bool inplace = (u_out == u_in);
+    double *zc = device_view(u_out);
     for (int k = 0; k < NBANDS; k++)
     {
         const HostBoxes b = chunk_boxes(c, k, boxes);
@@ -1621,23 +1663,19 @@ static ibtfo_status step_host_banded(ibtfo_case *c, const double *u_in, double *
         }
         CK(cudaEventRecord(c->ev_in[k], c->h2d));
     }
-    // the bands sweep TILE_X x TILE_Y tiles
+    // the bands sweep the case's tiles, in row order
     SweepArgs a = sweep_args(c, 0);
-    if (c->tiles8)
-    {
-        a.tiles = c->tiles8;
-        a.tmap[0] = c->tmap8[0];
-        a.tmap[1] = c->tmap8[1];
-    }
-    a.nblocks = c->tiles8 ? c->ntiles8 : c->ntiles;
+    a.tiles = c->band_list;
+    a.nblocks = c->nband_list;
     FillArgs f = fill_args(c);
     const bool gfm = c->cfg.boundary != IBTFO_BOUNDARY_REGULAR;
     auto finish = [&](int k) -> ibtfo_status {
         // band k's ghost cells, its rows back to the host layout, and their copy
+        cudaStream_t fs = c->fin[k % NFIN];
         for (int b = 0; b <= c->ghost_ready[k]; b++)
-            CK(cudaStreamWaitEvent(c->fin, c->ev_swept[b], 0));
+            CK(cudaStreamWaitEvent(fs, c->ev_swept[b], 0));
         if (gfm)
-            launch_fill_ghosts(f, c->band_ghosts[k], c->band_ghosts[k + 1], c->fin);
+            launch_fill_ghosts(f, c->band_ghosts[k], c->band_ghosts[k + 1], fs);
         int o0 = c->out_rows[k], o1 = c->out_rows[k + 1], x0 = 0, x1 = g.M;
         if (inplace)
         {
@@ -1646,8 +1684,8 @@ static ibtfo_status step_host_banded(ibtfo_case *c, const double *u_in, double *
             x0 = c->fluid_cols[2 * k];
             x1 = c->fluid_cols[2 * k + 1];
         }
-        launch_snapshot_to_aos_rows(c->buf[0], c->buf[1], c->st, c->type, c->staging, g, o0, o1, x0, x1, c->fin);
-        CK(cudaEventRecord(c->ev_out[k], c->fin));
+        launch_snapshot_to_aos_rows(c->buf[0], c->buf[1], c->st, c->type, c->staging, g, o0, o1, x0, x1, fs);
+        CK(cudaEventRecord(c->ev_out[k], fs));
         CK(cudaStreamWaitEvent(c->d2h, c->ev_out[k], 0));
         if (o1 > o0 && x1 > x0)
             CK(cudaMemcpy2DAsync(u_out + ((size_t)o0 * g.M + x0) * 4, row, c->staging + ((size_t)o0 * g.M + x0) * 4,
@@ -1658,17 +1696,17 @@ static ibtfo_status step_host_banded(ibtfo_case *c, const double *u_in, double *
     int next = 0; // the next band to finish
     for (int k = 0; k < NBANDS; k++)
     {
-        CK(cudaStreamWaitEvent(c->stream, c->ev_in[k], 0));
+        CK(cudaStreamWaitEvent(c->conv, c->ev_in[k], 0));
         launch_aos_to_cur_boxes(c->staging, c->buf[0], c->buf[1], c->st, g, chunk_boxes(c, k, boxes), k == 0, true,
-                                c->stream);
-        CK(cudaEventRecord(c->ev_conv[k], c->stream));
+                                c->conv);
+        CK(cudaEventRecord(c->ev_conv[k], c->conv));
         cudaStream_t s = c->sw[k % NSW];
         CK(cudaStreamWaitEvent(s, c->ev_conv[k], 0));
         const int t0 = c->band_tiles[k], t1 = c->band_tiles[k + 1];
         if (t1 > t0)
         {
             a.tile0 = t0;
-            c->sweep8(a, dim3(t1 - t0), dim3(TILE_X * TILE_Y), s);
+            c->sweep(a, dim3(t1 - t0), dim3(TILE_X * TILE_Y), s);
             count_launch();
         }
         CK(cudaEventRecord(c->ev_swept[k], s));
@@ -1685,21 +1723,45 @@ static ibtfo_status step_host_banded(ibtfo_case *c, const double *u_in, double *
         if (st != IBTFO_OK)
             return st;
     }
-    // the domain edges once every band and every ghost cell is done (periodic
-    // edges copy interior cells, ghost cells included)
+    const bool early_ring = inplace && c->cfg.global_boundary != IBTFO_GLOBAL_PERIODIC;
+    // the ring's kernels and copies: the conversion stream (idle once the
+    // last chunk is in) or, after everything else, the case's stream
+    cudaStream_t rk = early_ring ? c->conv : c->stream, rc = early_ring ? c->conv : c->d2h;
     for (int q = 0; q < NSW; q++)
     {
         CK(cudaEventRecord(c->ev_sw[q], c->sw[q]));
-        CK(cudaStreamWaitEvent(c->stream, c->ev_sw[q], 0));
+        CK(cudaStreamWaitEvent(rk, c->ev_sw[q], 0));
     }
-    CK(cudaEventRecord(c->ev_fin, c->fin));
-    CK(cudaStreamWaitEvent(c->stream, c->ev_fin, 0));
+    auto join_finishing = [&]() -> ibtfo_status {
+        for (int q = 0; q < NFIN; q++)
+        {
+            CK(cudaEventRecord(c->ev_fin[q], c->fin[q]));
+            CK(cudaStreamWaitEvent(c->stream, c->ev_fin[q], 0));
+        }
+        return IBTFO_OK;
+    };
+    if (!early_ring)
+    {
+        ibtfo_status js = join_finishing();
+        if (js != IBTFO_OK)
+            return js;
+        CK(cudaEventRecord(c->ev_cv, c->conv));
+        CK(cudaStreamWaitEvent(c->stream, c->ev_cv, 0));
+    }
     f.do_ghosts = 0;
     f.do_ring = 1;
-    launch_fill(f, c->stream);
-    ibtfo_status rs = ring_to_host(c, u_out);
+    launch_fill(f, rk);
+    ibtfo_status rs = ring_to_host(c, u_out, rk, rc, zc, !inplace);
     if (rs != IBTFO_OK)
         return rs;
+    if (early_ring)
+    {
+        ibtfo_status js = join_finishing();
+        if (js != IBTFO_OK)
+            return js;
+        CK(cudaEventRecord(c->ev_cv, c->conv));
+        CK(cudaStreamWaitEvent(c->stream, c->ev_cv, 0));
+    }
     CK(cudaEventRecord(c->ev_done, c->d2h));
     CK(cudaStreamWaitEvent(c->stream, c->ev_done, 0));
     return IBTFO_OK;
@@ -1811,7 +1873,8 @@ ibtfo_status ibtfo_step_host(ibtfo_case *c, const double *u_in, double *u_out, i
             return st;
         if (e != cudaSuccess)
             return cuda_fail(e, "capturing the host step");
-        e = cudaGraphInstantiate(&c->host_graph, gr, 0);
+        // kernel nodes keep the priorities of the streams they were captured from
+        e = cudaGraphInstantiate(&c->host_graph, gr, cudaGraphInstantiateFlagUseNodePriority);
         cudaGraphDestroy(gr);
         if (e != cudaSuccess)
             return cuda_fail(e, "instantiating the host step");

@@ -293,7 +293,7 @@ __global__ void tile_counts_kernel(GridDesc g, const uint8_t *__restrict__ type,
 }
 
 int active_tile_list(const GridDesc &g, const uint8_t *d_type, int tx, int ty, std::vector<unsigned> &list,
-                     cudaStream_t s)
+                     cudaStream_t s, bool row_order)
 {
     const int ntx = (g.n_x + tx - 1) / tx, nty = (g.n_y + ty - 1) / ty;
     const int n = ntx * nty;
@@ -320,12 +320,12 @@ int active_tile_list(const GridDesc &g, const uint8_t *d_type, int tx, int ty, s
         }
     if (list.empty())
         list.push_back(0u); // a tile without fluid still runs the loop accounting
-    else if (tx == TILE_X && ty == FAST_TILE_Y)
+    else if (!row_order && tx == TILE_X && ty == FAST_TILE_Y)
     {
         // the 32x16 sweeps solve only the faces their fluid cells read, so a
         // tile's time follows its fluid count: longest first, so that the last
-        // CTAs of a launch are the short ones (the row-band lists of the
-        // host-array step keep row order)
+        // CTAs of a launch are the short ones (the row-band list of the
+        // host-array step keeps row order)
         std::vector<int> idx(list.size());
         for (size_t k = 0; k < idx.size(); k++)
             idx[k] = (int)k;
@@ -339,10 +339,10 @@ int active_tile_list(const GridDesc &g, const uint8_t *d_type, int tx, int ty, s
 }
 
 int active_tiles(const GridDesc &g, const uint8_t *d_type, int ty, unsigned **d_tiles, int *ntiles, cudaStream_t s,
-                 std::vector<unsigned> *host_list)
+                 std::vector<unsigned> *host_list, bool row_order)
 {
     std::vector<unsigned> list;
-    int rc = active_tile_list(g, d_type, TILE_X, ty, list, s);
+    int rc = active_tile_list(g, d_type, TILE_X, ty, list, s, row_order);
     if (rc)
         return rc;
     if (host_list)

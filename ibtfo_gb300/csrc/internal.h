@@ -246,7 +246,8 @@ void launch_aos_to_cur_boxes(const double *aos, double *b0, double *b1, const De
                              const HostBoxes &bx, bool first, bool both, cudaStream_t s);
 // rows [r0, r1), columns [c0, c1) of a step in flight: fluid and ghost-fluid
 // cells from the step's output buffer (the ghost cells of these rows are
-// filled by then), the rest from its input (st->step_cur)
+// filled by then), the rest from its input (st->step_cur).  `aos` (here and
+// below) is a device buffer or a page-locked host array the device writes.
 void launch_snapshot_to_aos_rows(const double *b0, const double *b1, const DevState *st, const uint8_t *type,
                                  double *aos, const GridDesc &g, int r0, int r1, int c0, int c1, cudaStream_t s);
 // the domain ring of the current buffer into the host-layout array
@@ -341,12 +342,13 @@ void vtk_writer_destroy(VtkWriter *w, cudaStream_t s);
 // geometry set-up (geometry.cu)
 // the tiles of TILE_X x ty cells holding fluid cells, on the device and (host_list) on the host
 int active_tiles(const GridDesc &g, const uint8_t *d_type, int ty, unsigned **d_tiles, int *ntiles, cudaStream_t s,
-                 std::vector<unsigned> *host_list = nullptr);
+                 std::vector<unsigned> *host_list = nullptr, bool row_order = false);
 // host list of the tx x ty tiles holding at least one fluid cell (bx | by << 16,
-// with TILE_INTERIOR where it applies);
+// with TILE_INTERIOR where it applies): 32x16 tiles longest first unless
+// row_order, others in row order;
 // 0, or 2 (allocation) / 5 (CUDA error)
 int active_tile_list(const GridDesc &g, const uint8_t *d_type, int tx, int ty, std::vector<unsigned> &list,
-                     cudaStream_t s);
+                     cudaStream_t s, bool row_order = false);
 int setup_geometry(const GridDesc &g, int bc, const double *d_phi, double *d_nx, double *d_ny, uint8_t *d_type,
                    GhostRec **d_ghosts, int *nghost, cudaStream_t s);
 
