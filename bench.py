@@ -424,9 +424,9 @@ def ccm_leg(steps=40, warmup=3, n_x=8192, n_y=4096, full=False):
     """Mach 3 shock over 24 seeded obstacles with cut cells (8192x4096 on
     [0,4]x[0,2]): set-up time (level set, cut-cell geometry, mixing lists,
     initial state, all on the GPU), then `steps` timed steps of the FP32 form
-    with HLL and with Steger-Warming and of FP64 with HLL; the FP32 density
-    against FP64's after the same steps.  full: also the FP32 HLL run to
-    t_end = 1.0."""
+    with HLL_Toro and with Steger-Warming and of FP64 with HLL_Toro; the FP32
+    density against FP64's after the same steps.  full: also the FP32
+    HLL_Toro run to t_end = 1.0."""
     import torch
     import ibtfo_gb300 as ib
     from ibtfo_gb300 import cases
@@ -439,7 +439,7 @@ def ccm_leg(steps=40, warmup=3, n_x=8192, n_y=4096, full=False):
                        f"cut cells, CFL {w.cfl}", "cells": cells, "steps": steps, "legs": {}}
     rho = {}
     peak = measured_peaks()[0]
-    for riemann, prec in (("HLLC", "fp32c"), ("StegerWarming", "fp32c"), ("HLLC", "fp64_fast")):
+    for riemann, prec in (("HLL_Toro", "fp32c"), ("StegerWarming", "fp32c"), ("HLL_Toro", "fp64_fast")):
         stream = torch.cuda.Stream()
         with ib.Case.from_workload(w, riemann=riemann, precision=prec, t_end=1e300, max_iter=2 ** 31 - 1) as c:
             c.set_stream(stream.cuda_stream)
@@ -470,7 +470,7 @@ def ccm_leg(steps=40, warmup=3, n_x=8192, n_y=4096, full=False):
                 "sweep_and_mixing_ms": sweep_ms / steps,
                 "roofline_frac": BYTES_PER_CELL * cells / (sweep_ms / steps * 1e-3) / 1e9 / peak,
                 "setup_s": setup_s, "nan_cells": p["nan_cells"], "now_t": p["now_t"]}
-            if riemann == "HLLC":
+            if riemann == "HLL_Toro":
                 rho[prec] = c.density()
     a, b = rho["fp32c"], rho["fp64_fast"]
     d = np.abs(a - b)

@@ -370,5 +370,5 @@ def shock_obstacles(n_x=8192, n_y=4096):
     cell (alpha >= 0.5) sees up to twice a full cell's Courant number in an
     unsplit update."""
     return Workload(f"shock_obstacles_{n_x}x{n_y}", Grid(n_x, n_y, 2, 0.0, 0.0, 4.0, 2.0), 1.4, 0.3, 1.0,
-                    "MUSCL", "HLLC", "minmod", "CCM", extra={"mach": 3.0, "x_shock": 0.5, "seed": 20261203})
+                    "MUSCL", "HLL_Toro", "minmod", "CCM", extra={"mach": 3.0, "x_shock": 0.5, "seed": 20261203})
 

@@ -572,8 +572,10 @@ ibtfo_status ibtfo_create(const ibtfo_config *cfg, ibtfo_case **out)
         return fail(IBTFO_EINVAL, "Time = RK2 runs without cut cells");
     if (k.precision == IBTFO_PRECISION_FP32_COMPENSATED && k.riemann == IBTFO_RIEMANN_PVRS)
         return fail(IBTFO_EINVAL, "PVRS is available in the FP64 precisions only");
-    if (k.boundary == IBTFO_BOUNDARY_CCM && k.riemann == IBTFO_RIEMANN_PVRS)
-        return fail(IBTFO_EINVAL, "the cut-cell method runs HLL/HLLC, Steger-Warming or HLLC_Toro, not PVRS");
+    if (k.boundary == IBTFO_BOUNDARY_CCM && k.riemann != IBTFO_RIEMANN_HLL_TORO &&
+        k.riemann != IBTFO_RIEMANN_STEGER_WARMING && k.riemann != IBTFO_RIEMANN_HLLC_TORO)
+        return fail(IBTFO_EINVAL, "the cut-cell method runs HLL_Toro, StegerWarming or HLLC_Toro (the reference's "
+                                  "HLL and PVRS have no cut-cell form)");
     if (k.global_boundary == IBTFO_GLOBAL_PERIODIC && (k.n_x < k.num_ghost_cell || k.n_y < k.num_ghost_cell))
         return fail(IBTFO_EINVAL, "periodic boundaries need n_x, n_y >= num_ghost_cell");
 

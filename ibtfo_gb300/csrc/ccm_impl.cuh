@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y, PREC == 2 ? 4 : 1) ccm_sweep_k
                     lo[k] = U[(4 + k) * P + o];
                     two_float_sub(hi[k], lo[k], d);
                 }
-                if constexpr (RIE == HLLCT)
+                if constexpr (safeguarded(RIE))
                 {
                     float e;
                     if (pressure_floor_energy(hi, e))
@@ -228,7 +228,7 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y, PREC == 2 ? 4 : 1) ccm_sweep_k
                     const double x = s.sU[k][r + 2][c + 2] - lx * (s.sF[k][r + 1][c + 1] - s.sF[k][r + 1][c]);
                     v[k] = x - ly * (s.sG[k][r + 1][c] - s.sG[k][r][c]);
                 }
-                if constexpr (RIE == HLLCT)
+                if constexpr (safeguarded(RIE))
                     pressure_floor(v);
 #pragma unroll
                 for (int k = 0; k < 4; k++)
@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(TILE_X *TILE_Y, PREC == 2 ? 4 : 1) ccm_sweep_k
             }
             // the floor only where no mixing follows: a small cell's swept state
             // is provisional (divided by a small alpha) until it is mixed
-            if constexpr (RIE == HLLCT)
+            if constexpr (safeguarded(RIE))
                 if (al >= 0.5)
                     pressure_floor(v);
 #pragma unroll
@@ -321,18 +321,19 @@ void launch_ccm_sweep(const CcmArgs &a, dim3 grid, dim3 block, cudaStream_t s)
     ccm_sweep_kernel<SCH, RIE, LIM, PREC><<<grid, block, sizeof(CcmSmem<T, TILE_X, ccm_tile_rows<PREC>()>), s>>>(a);
 }
 
-// every Riemann solver and limiter of one scheme and precision (the HLLC key
-// is the plain HLL here; PVRS has no cut-cell form)
+// every Riemann solver and limiter of one scheme and precision: HLL_Toro,
+// Steger-Warming, HLLC_Toro (the reference's HLL and PVRS have no cut-cell
+// form)
 template <int SCH, int PREC>
 CcmLaunch ccm_launcher_scheme(int riemann, int limiter)
 {
     const bool vl = (limiter == VANLEER);
     switch (riemann)
     {
-    case PVRS: return nullptr;
     case SW: return vl ? &launch_ccm_sweep<SCH, SW, VANLEER, PREC> : &launch_ccm_sweep<SCH, SW, MINMOD, PREC>;
     case HLLCT: return vl ? &launch_ccm_sweep<SCH, HLLCT, VANLEER, PREC> : &launch_ccm_sweep<SCH, HLLCT, MINMOD, PREC>;
-    default: return vl ? &launch_ccm_sweep<SCH, HLL, VANLEER, PREC> : &launch_ccm_sweep<SCH, HLL, MINMOD, PREC>;
+    case HLLT: return vl ? &launch_ccm_sweep<SCH, HLLT, VANLEER, PREC> : &launch_ccm_sweep<SCH, HLLT, MINMOD, PREC>;
+    default: return nullptr;
     }
 }
 

@@ -469,12 +469,14 @@ __device__ __forceinline__ int y_face_fast(const T c0[4], const T c1[4], const T
 // ---------------------------------------------------------------- cut cells
 //
 // The cut-cell method has no reference counterpart, so its faces use the
-// plain HLL flux in both directions (no Y-face slot reuse), Steger-Warming, or
-// the contact-restoring HLLC.
+// HLL flux with Toro's wave speeds in both directions (HLL_Toro: no Y-face
+// slot reuse), Steger-Warming, or the contact-restoring HLLC_Toro; the
+// reference's HLL (the HLL and HLLC keys) has no cut-cell form.
 
 template <typename T, int NRM, int RIE>
 __device__ __forceinline__ void ccm_solve(const T UL[4], const T UR[4], const GasConst<T> &K, T F[4])
 {
+    static_assert(RIE == SW || RIE == HLLCT || RIE == HLLT, "no cut-cell form of this solver");
     if constexpr (RIE == SW)
         sw_fast<T, NRM>(UL, UR, K, F);
     else if constexpr (RIE == HLLCT)

@@ -187,7 +187,7 @@ def read_ref_record(path: str) -> dict:
 
 # ------------------------------------------------------------------ cut cells
 
-CCM_RIEMANNS = {"HLL": 0, "HLLC": 1, "StegerWarming": 3, "HLLC_Toro": 4}
+CCM_RIEMANNS = {"StegerWarming": 3, "HLLC_Toro": 4, "HLL_Toro": 5}
 
 
 def _ccm_lib():
@@ -212,7 +212,7 @@ class CcmOracle:
     """One cut-cell case on the CPU (FP64 restatement of the library's cut-cell method)."""
 
     def __init__(self, n_x, n_y, ng=2, lo=(0.0, 0.0), hi=(1.0, 1.0), gamma=1.4, cfl=0.45, t_end=1e300,
-                 scheme="MUSCL", riemann="HLL", limiter="minmod", gbc="walls"):
+                 scheme="MUSCL", riemann="HLL_Toro", limiter="minmod", gbc="walls"):
         self.L = _ccm_lib()
         self.n_x, self.n_y, self.ng = n_x, n_y, ng
         self.M, self.N = n_x + 2 * ng, n_y + 2 * ng

@@ -20,7 +20,7 @@
 
 enum { T_FLUID = 0, T_SOLID = 1, T_GHOST = 2, T_CUT = 3 };
 enum { S_MUSCL = 0, S_MHM = 1, S_GODUNOV = 2 };
-enum { R_HLL = 0, R_HLLC = 1, R_SW = 3, R_HLLCT = 4 };
+enum { R_SW = 3, R_HLLCT = 4, R_HLLT = 5 }; /* the library's solver keys */
 
 typedef struct
 {
@@ -452,7 +452,7 @@ static void solve(const double UL[4], const double UR[4], int nrm, const ccm_cas
     }
     else if (c->riemann == R_HLLCT)
         hllc_toro(UL, UR, nrm, c, F);
-    else
+    else /* R_HLLT */
         hll_plain(UL, UR, nrm, c, F);
 }
 
@@ -734,7 +734,7 @@ static void step(ccm_case *c)
                     double x = u0[k] - lx * (Fe[k] - Fw[k]);
                     v[k] = x - ly * (Gn[k] - Gs[k]);
                 }
-                if (c->riemann == R_HLLCT)
+                if (c->riemann == R_HLLCT || c->riemann == R_HLLT)
                     pressure_floor(v);
                 stats_full(c, v, &st);
             }
@@ -754,7 +754,7 @@ static void step(ccm_case *c)
                     double gy = face_term(an, Gn[k]) - face_term(as, Gs[k]);
                     v[k] = (al * u0[k] - lxd * fx - lyd * gy - lw * W[k]) / al;
                 }
-                if (c->riemann == R_HLLCT && al >= 0.5)
+                if ((c->riemann == R_HLLCT || c->riemann == R_HLLT) && al >= 0.5)
                     pressure_floor(v);
                 st.mass += al * v[0] * (c->dx * c->dy);
                 if (al >= 0.5)

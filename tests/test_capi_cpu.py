@@ -57,11 +57,21 @@ def test_unknown_key_rejected():
         ib.Case(16, 8, time="RK3")
 
 
-@pytest.mark.parametrize("bad", [dict(scheme="Lax", precision="fp32c"), dict(scheme="Lax", boundary="CCM", riemann="HLL"),
-                                 dict(time="RK2", boundary="CCM", riemann="HLL")])
+@pytest.mark.parametrize("bad", [dict(scheme="Lax", precision="fp32c"), dict(scheme="Lax", boundary="CCM", riemann="HLL_Toro"),
+                                 dict(time="RK2", boundary="CCM", riemann="HLL_Toro")])
 def test_lax_and_rk2_limits_rejected_without_gpu(bad):
     with pytest.raises(ib.IbtfoError, match="Lax|RK2") as e:
         ib.Case(16, 8, **bad)
+    assert e.value.code == 1
+
+
+@pytest.mark.parametrize("riemann", ["HLL", "HLLC", "PVRS"])
+def test_cut_cells_reject_the_reference_solvers_without_gpu(riemann):
+    """A solver key names one solver whatever the boundary: the cut-cell sweep
+    runs HLL_Toro, StegerWarming and HLLC_Toro, and has no form of the
+    reference's HLL (the HLL and HLLC keys) or of PVRS."""
+    with pytest.raises(ib.IbtfoError, match="cut-cell") as e:
+        ib.Case(16, 8, boundary="CCM", riemann=riemann)
     assert e.value.code == 1
 
 

@@ -298,7 +298,7 @@ def test_cut_cells_full_size_matches_oracle():
             dts, ms = steps_with_progress(c, steps)
             res[precision] = (u0, p0, dts, ms, c.get_state())
     o = oracle.CcmOracle(g.n_x, g.n_y, g.ng, (g.lo_x, g.lo_y), (g.hi_x, g.hi_y), w.gamma, w.cfl, 1e300, w.scheme,
-                         "HLL", w.limiter, w.gbc)
+                         w.riemann, w.limiter, w.gbc)
     try:
         o.setup(phi)
         oa, oax, oay, ot = o.geometry()

@@ -246,7 +246,7 @@ def test_step_host_equals_put_step_get(kind, precision, in_place, pinned):
         g = _c.Grid(192, 128, 2, 0.0, 0.0, 1.5, 1.0)
 
         def make():
-            c = ib.Case(g.n_x, g.n_y, lo=(0, 0), hi=(1.5, 1.0), cfl=0.3, riemann="HLLC", boundary="CCM",
+            c = ib.Case(g.n_x, g.n_y, lo=(0, 0), hi=(1.5, 1.0), cfl=0.3, riemann="HLL_Toro", boundary="CCM",
                         precision=precision)
             c.setup_geometry(_c.cylinder_phi(g, 0.6, 0.5, 0.2))
             c.set_state(_c.shock_init(g, c.cell_types(), 2.0, 0.2))

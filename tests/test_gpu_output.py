@@ -110,7 +110,7 @@ def _sod(precision):
 
 def _ccm(precision):
     g = cases.Grid(96, 64, 2, 0.0, 0.0, 1.5, 1.0)
-    w = cases.Workload("ccm", g, 1.4, 0.3, 1e300, "MUSCL", "HLLC", "minmod", "CCM")
+    w = cases.Workload("ccm", g, 1.4, 0.3, 1e300, "MUSCL", "HLL_Toro", "minmod", "CCM")
     phi = cases.cylinder_phi(g, 0.6, 0.5, 0.2)
     c = ib.Case.from_workload(w, precision=precision, max_iter=2 ** 31 - 1)
     c.setup_geometry(phi)
