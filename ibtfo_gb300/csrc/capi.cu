@@ -1026,14 +1026,38 @@ ibtfo_status ibtfo_put_state(ibtfo_case *c, const double *u)
     return IBTFO_OK;
 }
 
+// A page-locked record per host thread for the loop state read back after
+// every step (a pageable destination goes through a staging buffer of the
+// driver); allocated once, portable across devices, never freed, so that
+// creating and destroying cases still never synchronises the device.  Null
+// when page-locked memory is not available.
+static DevState *progress_record()
+{
+    thread_local DevState *rec = nullptr;
+    thread_local bool tried = false;
+    if (!tried)
+    {
+        tried = true;
+        void *p = nullptr;
+        if (cudaHostAlloc(&p, sizeof(DevState), cudaHostAllocPortable) == cudaSuccess)
+            rec = static_cast<DevState *>(p);
+        else
+            cudaGetLastError();
+    }
+    return rec;
+}
+
 ibtfo_status ibtfo_get_progress(ibtfo_case *c, ibtfo_progress *p)
 {
     if (!c || !p)
         return fail(IBTFO_EINVAL, "null argument");
     cudaSetDevice(c->device);
     DevState s;
-    CK(cudaMemcpyAsync(&s, c->st, sizeof(DevState), cudaMemcpyDeviceToHost, c->stream));
+    DevState *rec = progress_record();
+    CK(cudaMemcpyAsync(rec ? rec : &s, c->st, sizeof(DevState), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    if (rec)
+        s = *rec;
     p->iter = s.iter;
     p->status = s.status;
     p->nan_cells = s.nan_cells;
