@@ -358,8 +358,6 @@ static void make_in_boxes(ibtfo_case *c, const std::vector<unsigned> &tiles)
     }
 }
 
-// the domain ring of the current state into u_out: two runs of whole rows
-// and two strided runs of the side columns
 // The device-side address of a page-locked host array the kernels can write
 // directly, or null (pageable memory, or no mapping).
 static double *device_view(double *host)
@@ -373,10 +371,12 @@ static double *device_view(double *host)
     return at.type == cudaMemoryTypeHost ? static_cast<double *>(at.devicePointer) : nullptr;
 }
 
-// the domain ring to the host layout on stream ks, and its copies on cs; with
-// zc (u_out's device view) the kernel writes the host array itself, after the
-// row copies queued on the second copy stream when those cover the ring
-// (full rows back: their ring cells are stale)
+// The domain ring of the current state into u_out: converted to the host
+// layout on stream ks and copied on cs (two runs of whole rows and two
+// strided runs of the side columns), or, with zc (u_out's device view),
+// written into the host array by the conversion kernel itself, after the row
+// copies queued on the second copy stream when those cover the ring (full
+// rows back: their ring cells are stale).
 static ibtfo_status ring_to_host(ibtfo_case *c, double *u_out, cudaStream_t ks, cudaStream_t cs, double *zc,
                                  bool after_rows)
 {
