@@ -286,7 +286,7 @@ __device__ __forceinline__ void hllc_toro(const T UL[4], const T UR[4], const Ga
 }
 
 // HLL flux in either direction with Toro's PVRS wave-speed estimates
-// (the HLL_Toro key, and the cut-cell method's HLL/HLLC keys)
+// (the HLL_Toro key, in the ghost-fluid and the cut-cell sweeps)
 // (p* >= 0, q_K = 1 for p* <= p_K; Toro 2009, eqs. 10.59-10.60), which stay
 // defined in strong expansions where the reference's HLL estimate takes the
 // square root of a negative number

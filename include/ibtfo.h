@@ -59,8 +59,10 @@ enum { IBTFO_TIME_SINGLESTEP = 0, IBTFO_TIME_RK2 = 1 };
  * p* <= p_K, so no square root of a negative number behind a strong
  * shock), no Y-face slot reuse, and the same two safeguards; like every HLL
  * flux it does not suffer the carbuncle / odd-even decoupling of
- * contact-restoring solvers at strong grid-aligned shocks.  Under the
- * cut-cell method it is the same solver as the HLL/HLLC keys. */
+ * contact-restoring solvers at strong grid-aligned shocks.  The cut-cell
+ * method (IBTFO_BOUNDARY_CCM) runs HLL_TORO, STEGER_WARMING and HLLC_TORO;
+ * the reference's HLL (the HLL and HLLC keys) and PVRS have no cut-cell
+ * form, and ibtfo_create rejects them there (IBTFO_EINVAL). */
 enum {
     IBTFO_RIEMANN_HLL = 0,
     IBTFO_RIEMANN_HLLC = 1,
@@ -82,8 +84,8 @@ enum {
      * Riemann problem, first-order faces next to the body, and conservative
      * mixing of cut cells with volume fraction below 0.5 with their
      * neighbours (FP64 for the geometry, the cut-cell update and the
-     * mixing); plain HLL for the HLL/HLLC keys, Steger-Warming, HLLC_TORO;
-     * both FP64 precision keys run the same FP64 arithmetic */
+     * mixing); solvers HLL_TORO, Steger-Warming, HLLC_TORO; both FP64
+     * precision keys run the same FP64 arithmetic */
     IBTFO_BOUNDARY_CCM = 6
 };
 enum { IBTFO_GLOBAL_WALLS = 0, IBTFO_GLOBAL_PERIODIC = 1 };
